@@ -1,0 +1,235 @@
+/*
+ * xcore_gb300.h -- C ABI of the GB300 (sm_103a) drop-in for the per-timestep
+ * hot path of xcore.jl (aelligp/xcore.jl).
+ *
+ * The reference's "operator API" is a set of plain Julia functions that mutate
+ * caller-allocated state structs in place (src/phsevo.jl, src/fluidmech.jl,
+ * src/noise.jl, src/update.jl, src/store.jl, src/diagnose.jl).  This library
+ * keeps that state resident in GPU memory inside an opaque context with the
+ * reference's field names and sizes (column-major, z the leading dimension,
+ * src/state.jl:101-122, 218-258; src/noise.jl:82-92), and exports one entry
+ * point per reference function.  Julia binds them with ccall (see
+ * INTEGRATION.md); no torch or CUDA types appear in any signature.
+ *
+ * Conventions
+ *  - Every function returns an xc_status; on failure xc_last_error() holds a
+ *    one-line message for the calling thread.  Nothing throws across the ABI.
+ *  - A context owns its device buffers and a non-blocking CUDA stream; all work
+ *    of that context is ordered on that stream.  A context is not thread safe;
+ *    separate contexts are independent.  Functions that return host scalars
+ *    synchronise the stream; the others only enqueue work.
+ *  - The library never frees caller memory.  Host arrays passed in are read or
+ *    written during the call only.
+ *  - There is no CPU fallback: without a usable CUDA device every call that
+ *    needs one returns XC_NO_DEVICE.
+ */
+#ifndef XCORE_GB300_H
+#define XCORE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum xc_status {
+  XC_OK = 0,
+  XC_BAD_ARG = 1,        /* size / scheme / BC argument the reference rejects
+                            (@assert and ArgumentError, advect.jl:378-385,421;
+                            ghosts.jl:35,47; timing.jl:35) */
+  XC_NOT_CONVERGED = 2,  /* iterative Stokes solve hit its iteration limit */
+  XC_NAN = 3,            /* non-finite residual (diagnose.jl:80 raises) */
+  XC_TIMEOUT = 4,        /* a bounded device wait gave up */
+  XC_CUDA = 5,           /* a CUDA runtime call failed */
+  XC_NO_DEVICE = 6       /* no CUDA device available */
+} xc_status;
+
+/* advection schemes, par.ADVN (src/parameters.jl:74; advect.jl:346-355) */
+typedef enum xc_scheme {
+  XC_CENTR = 0, XC_UPWD1 = 1, XC_QUICK = 2, XC_FROMM = 3,
+  XC_WENO3 = 4, XC_WENO5 = 5, XC_TVDIM = 6
+} xc_scheme;
+
+/* boundary conditions per axis (ghosts.jl:18-51) */
+typedef enum xc_bc { XC_PERIODIC = 0, XC_CLOSED = 1 } xc_bc;
+
+/* time integrators, par.TINT (src/timing.jl:18-36) */
+typedef enum xc_tint { XC_BE1IM = 0, XC_BD2IM = 1, XC_CN2SI = 2, XC_BD2SI = 3 } xc_tint;
+
+/* Stokes solver kinds (the reference always factorises with UMFPACK,
+   fluidmech.jl:512-522; these replace that solve) */
+typedef enum xc_solver_kind {
+  XC_SOLVER_FGMRES_FP64 = 0,   /* FP64 FGMRES + FP64 multigrid / Schur preconditioner */
+  XC_SOLVER_MIXED = 1          /* FP32 FGMRES + FP32 multigrid inside FP64 iterative refinement */
+} xc_solver_kind;
+
+/*
+ * Scalars of Parameters{Float64} (src/parameters.jl:12-89) and Scales
+ * (src/scales.jl:13-57) that the path reads, plus the boundary keywords of
+ * run! (src/run.jl:174-180).  Scales are computed by the caller (they are
+ * one-off host scalars in the reference) and passed in.
+ */
+typedef struct xc_params {
+  int Nz, Nx;              /* grid.Nz, grid.Nx (src/grid.jl:311-334) */
+  double h, D;             /* grid.h, par.D */
+  double rhom0, rhox0, d0, g0, etam0, etax0;
+  double AA[4], BB[4], CC[4];  /* 2x2 rheology matrices, row-major [11,12,21,22] */
+  double Xi, Ptop, alpha, gamma, CFL, dtmax, etacntr;
+  int open_sgr;            /* 0/1 */
+  /* scales */
+  double L0, l0, L0h, l0h, D0, txi0, G0, bnd_w, dt0;
+  int ADVN;                /* xc_scheme */
+  int TINT;                /* xc_tint */
+  int xBC, zBC;            /* xc_bc; the reference default is periodic x, closed z */
+  int sds, top_cnv, bot_cnv, open_cnv;   /* fluidmech! keywords (fluidmech.jl:71-80) */
+} xc_params;
+
+typedef struct xc_solver_opts {
+  int kind;          /* xc_solver_kind */
+  double rtol;       /* relative residual target of the (scaled) saddle system */
+  int maxit;         /* outer iteration cap */
+  int restart;       /* FGMRES restart length */
+  double inner_rtol; /* mixed: relative reduction per FP32 inner solve */
+  int inner_maxit;   /* mixed: FP32 FGMRES iterations per refinement pass */
+} xc_solver_opts;
+
+typedef struct xc_solver_stats {
+  int iterations;          /* FP64 FGMRES iterations, or FP32 inner iterations in total */
+  int refinements;         /* mixed: FP64 refinement passes */
+  double rel_residual;     /* final ||RR - LL x|| / ||RR|| of the scaled system, FP64 */
+  int converged;           /* 1 when rel_residual <= rtol */
+  double seconds;          /* device time of the solve */
+} xc_solver_stats;
+
+typedef struct xc_step_stats {
+  double resnorm[16];      /* compute_resnorm per Picard sweep (diagnose.jl:57-71) */
+  int sweeps;
+  int solver_iterations;   /* summed over sweeps */
+  double solver_rel_residual;  /* worst final residual over the sweeps */
+  double dt_next;          /* update_dt (update.jl:494-502) */
+} xc_step_stats;
+
+typedef struct xc_ctx xc_ctx;
+
+/* ------------------------------------------------------------------ */
+/* context and fields                                                  */
+/* ------------------------------------------------------------------ */
+
+/* Allocate device state for one grid, all fields zero (FluidState /
+   PhaseState / NoiseState constructors, src/state.jl:101-122, 218-258,
+   src/noise.jl:61-93, incl. the Gaussian filter precompute noise.jl:68-78). */
+int xc_ctx_create(const xc_params* par, xc_ctx** out);
+int xc_ctx_destroy(xc_ctx* ctx);
+
+/* Field registry: ids 0..xc_field_count()-1 name every state field. */
+int xc_field_count(void);
+const char* xc_field_name(int id);
+int xc_field_id(const char* name);            /* -1 when unknown */
+/* rows, cols and element size (8 = Float64, 1 = Bool) of a field */
+int xc_field_shape(const xc_ctx* ctx, int id, int* rows, int* cols, int* elem_bytes);
+/* Device address of a field (column-major, leading dimension = rows). */
+int xc_field_device_ptr(const xc_ctx* ctx, int id, void** dev_ptr);
+/* Copy a whole field host -> device / device -> host (synchronous). */
+int xc_field_upload(xc_ctx* ctx, int id, const void* host);
+int xc_field_download(xc_ctx* ctx, int id, void* host);
+/* Wait for all work of the context. */
+int xc_synchronize(xc_ctx* ctx);
+
+/* ------------------------------------------------------------------ */
+/* one entry point per reference function                              */
+/* ------------------------------------------------------------------ */
+
+/* store_previous!(fluid, phase)                         src/store.jl:13-30 */
+int xc_store_previous(xc_ctx* ctx);
+/* store_noise!(ns)                                      src/noise.jl:115-120 */
+int xc_store_noise(xc_ctx* ctx);
+/* snapshot!(res, phase, fluid)                          src/diagnose.jl:42-49 */
+int xc_snapshot(xc_ctx* ctx);
+/* phsevo!(phase, fluid, grid, par, scales; ADVN, xBC, zBC, a1..b3, dt, alpha)
+                                                         src/phsevo.jl:164-214
+   coefs = (a1, a2, a3, b1, b2, b3); scheme = xc_scheme (par.ADVN when < 0) */
+int xc_phsevo(xc_ctx* ctx, int scheme, const double coefs[6], double dt, double alpha);
+/* fluidmech!(fluid, grid, par; phase, sds, top_cnv, bot_cnv, open_cnv, xBC,
+   zBC, dt, a1..b3)                                      src/fluidmech.jl:71-534
+   The UMFPACK factorisation is replaced by the iterative solver in opts
+   (NULL = FP64 FGMRES to rtol 1e-10).  stats may be NULL. */
+int xc_fluidmech(xc_ctx* ctx, const double coefs[6], double dt,
+                 const xc_solver_opts* opts, xc_solver_stats* stats);
+/* fluidmech! in MMS mode (bnchm_data != nothing): src_* and *_exact arrays are
+   host arrays sized like W (Nz+1,Nx+2), U (Nz+2,Nx+1), P (Nz+2,Nx+2).
+                                                         src/fluidmech.jl:115,218,243,320,421-476 */
+int xc_fluidmech_mms(xc_ctx* ctx, const double* src_W, const double* src_U, const double* src_P,
+                     const double* W_exact, const double* U_exact, const double* P_exact,
+                     const double coefs[6], double dt,
+                     const xc_solver_opts* opts, xc_solver_stats* stats);
+/* noise!(ns, phase, grid, par, scales, dt; first_iter)  src/noise.jl:138-239
+   The white noise that the reference draws with randn!(ns.rng, ...) on the
+   first sweep (noise.jl:154-157) is passed in: re/rs are host (Nz, Nx) arrays
+   copied in when first_iter != 0; NULL keeps the draws already on the device. */
+int xc_noise(xc_ctx* ctx, double dt, int first_iter, const double* re, const double* rs);
+/* update_phase_velocities!(phase, fluid, ns, grid, par; xBC, zBC)
+   incl. update_segregation_speed!                       src/store.jl:47-105 */
+int xc_update_phase_velocities(xc_ctx* ctx);
+/* update!(phase, fluid, grid, par, scales; xBC, zBC)    src/update.jl:525-538 */
+int xc_update(xc_ctx* ctx);
+/* dt = update_dt(phase, fluid, grid, par, dt_prev)      src/update.jl:494-502 */
+int xc_update_dt(xc_ctx* ctx, double dt_prev, double* dt_out);
+/* (resnorm, res_mass, res_mmnt) = compute_resnorm(res, phase, fluid, dt)
+                                                         src/diagnose.jl:57-71 */
+int xc_resnorm(xc_ctx* ctx, double dt, double out[3]);
+/* FP64 conservation sums of record_history!             src/history.jl:121-145
+   out = {sumB, sumM, sumX, sumGx, top_aX, bot_aX, top_aM, bot_aM,
+          top_dX, bot_dX, top_dM, bot_dM} */
+int xc_conservation_sums(xc_ctx* ctx, double out[12]);
+/* Fresh-start initialize! (src/run.jl:71-140) with the initial crystal
+   fraction x (host (Nz,Nx)) in place of the MersenneTwister perturbation
+   (run.jl:98-108) and the first white-noise draw re/rs. */
+int xc_initialize(xc_ctx* ctx, const double* x_init, const double* re, const double* rs);
+/* One outer time step of run! (src/run.jl:204-274): time_coefs, store_previous!,
+   store_noise!, `sweeps` Picard sweeps of phsevo! -> fluidmech! -> noise! ->
+   update_phase_velocities! -> update! -> compute_resnorm, then update_dt.
+   re/rs are the step's white-noise draw (host arrays, or NULL to keep the
+   device ones).  stats may be NULL. */
+int xc_step(xc_ctx* ctx, int step, double dt, int sweeps, const double* re, const double* rs,
+            const xc_solver_opts* opts, xc_step_stats* stats);
+
+/* ------------------------------------------------------------------ */
+/* stencil-level entry points on caller device pointers                */
+/* (sizes exactly as the reference's; stream = cudaStream_t or NULL)   */
+/* ------------------------------------------------------------------ */
+
+/* fill_ghosts!(f, halo; zBC, xBC), f is (Nz+2halo, Nx+2halo)   src/kernels/ghosts.jl:18-51 */
+int xc_fill_ghosts(double* f, int Nz, int Nx, int halo, int zBC, int xBC, void* stream);
+/* advect!(adv, f_halo, u, w, h, scheme)                          src/kernels/advect.jl:374-425
+   f_halo (Nz+2g, Nx+2g); u (Nz, Nx+1) or (Nz, Nx+3) for tvdim; w (Nz+1, Nx) or (Nz+3, Nx) */
+int xc_advect(double* adv, const double* f_halo, const double* u, const double* w,
+              int Nz, int Nx, double h, int scheme, void* stream);
+/* advect_with_flux!(adv, qx, qz, f_halo, u, w, h, scheme; xBC, zBC)
+   qx (Nz+2, Nx+1), qz (Nz+1, Nx+2)                                src/kernels/advect.jl:717-798 */
+int xc_advect_with_flux(double* adv, double* qx, double* qz, const double* f_halo,
+                        const double* u, const double* w, int Nz, int Nx, double h,
+                        int scheme, int xBC, int zBC, void* stream);
+/* advect_centered_with_flux!(adv, qx, qz, f, u, w, h, scheme; xBC, zBC):
+   f (Nz, Nx) without halo; ghost fill fused into the tile load  src/phsevo.jl:90-128 */
+int xc_advect_centered_with_flux(double* adv, double* qx, double* qz, const double* f,
+                                 const double* u, const double* w, int Nz, int Nx, double h,
+                                 int scheme, int xBC, int zBC, void* stream);
+/* diffus!(dff, f_halo, k_halo, h; halo=1)                        src/kernels/diffus.jl:109-121 */
+int xc_diffus(double* dff, const double* f_halo, const double* k_halo, int Nz, int Nx,
+              double h, void* stream);
+/* diffus_with_flux!(dff, qx, qz, f_halo, k_halo, h; halo=1, xBC, zBC)
+                                                                 src/kernels/diffus.jl:169-211 */
+int xc_diffus_with_flux(double* dff, double* qx, double* qz, const double* f_halo,
+                        const double* k_halo, int Nz, int Nx, double h, int xBC, int zBC,
+                        void* stream);
+
+/* time_coefs(Float64, TINT, step) -> (a1, a2, a3, b1, b2, b3)    src/timing.jl:18-36 */
+int xc_time_coefs(int tint, int step, double out[6]);
+
+/* Last error message of the calling thread ("" when none). */
+const char* xc_last_error(void);
+/* Library version string. */
+const char* xc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XCORE_GB300_H */

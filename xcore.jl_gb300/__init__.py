@@ -1,0 +1,491 @@
+"""xcore_gb300 -- Python host side of the GB300 drop-in for xcore.jl's time-step path.
+
+This module mirrors the reference's host-facing API (aelligp/xcore.jl, pure
+Julia) over the C ABI of ``libxcore_gb300.so`` (include/xcore_gb300.h):
+
+* ``Parameters`` / ``Grid`` / ``compute_scales`` restate the host-side scalar
+  setup (src/parameters.jl:12-89, src/grid.jl:311-334, src/scales.jl:85-185);
+* ``State`` owns one device context holding FluidState + PhaseState +
+  NoiseState + StepResidual with the reference's field names and sizes, and
+  exposes the reference's mutating functions as methods: ``phsevo``
+  (phsevo!), ``fluidmech`` (fluidmech!), ``noise`` (noise!), ``update``
+  (update!), ``update_phase_velocities``, ``store_previous``, ``store_noise``,
+  ``snapshot``, ``update_dt``, ``compute_resnorm``, ``initialize``, ``step``;
+* module functions ``advect`` / ``advect_with_flux`` / ``diffus`` /
+  ``diffus_with_flux`` / ``fill_ghosts`` take device arrays (torch CUDA
+  tensors) exactly as the reference kernels take arrays.
+
+Arrays cross the boundary column-major with z the leading dimension, like the
+Julia matrices.  Host arrays here are numpy arrays indexed ``[z, x]``.
+There is no CPU fallback: the library must be built (``build()``) and a CUDA
+device present, otherwise calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libxcore_gb300.so")
+
+XC_OK, XC_BAD_ARG, XC_NOT_CONVERGED, XC_NAN, XC_TIMEOUT, XC_CUDA, XC_NO_DEVICE = range(7)
+SCHEMES = {"centr": 0, "upwd1": 1, "quick": 2, "fromm": 3, "weno3": 4, "weno5": 5, "tvdim": 6}
+BCS = {"periodic": 0, "closed": 1}
+TINTS = {"be1im": 0, "bd2im": 1, "cn2si": 2, "bd2si": 3}
+SOLVERS = {"fgmres64": 0, "mixed": 1}
+EPS = float(np.finfo(np.float64).eps)
+
+
+class XcoreError(RuntimeError):
+    """A non-OK status from the library, with its message."""
+
+    def __init__(self, status, msg):
+        super().__init__(f"xcore_gb300 status {status}: {msg}")
+        self.status = status
+
+
+class NotConverged(XcoreError):
+    pass
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("Nz", ctypes.c_int), ("Nx", ctypes.c_int), ("h", ctypes.c_double), ("D", ctypes.c_double),
+                ("rhom0", ctypes.c_double), ("rhox0", ctypes.c_double), ("d0", ctypes.c_double),
+                ("g0", ctypes.c_double), ("etam0", ctypes.c_double), ("etax0", ctypes.c_double),
+                ("AA", ctypes.c_double * 4), ("BB", ctypes.c_double * 4), ("CC", ctypes.c_double * 4),
+                ("Xi", ctypes.c_double), ("Ptop", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("CFL", ctypes.c_double), ("dtmax", ctypes.c_double),
+                ("etacntr", ctypes.c_double), ("open_sgr", ctypes.c_int),
+                ("L0", ctypes.c_double), ("l0", ctypes.c_double), ("L0h", ctypes.c_double),
+                ("l0h", ctypes.c_double), ("D0", ctypes.c_double), ("txi0", ctypes.c_double),
+                ("G0", ctypes.c_double), ("bnd_w", ctypes.c_double), ("dt0", ctypes.c_double),
+                ("ADVN", ctypes.c_int), ("TINT", ctypes.c_int), ("xBC", ctypes.c_int), ("zBC", ctypes.c_int),
+                ("sds", ctypes.c_int), ("top_cnv", ctypes.c_int), ("bot_cnv", ctypes.c_int),
+                ("open_cnv", ctypes.c_int)]
+
+
+class SolverOpts(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
+                ("restart", ctypes.c_int), ("inner_rtol", ctypes.c_double), ("inner_maxit", ctypes.c_int)]
+
+
+class SolverStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("refinements", ctypes.c_int), ("rel_residual", ctypes.c_double),
+                ("converged", ctypes.c_int), ("seconds", ctypes.c_double)]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [("resnorm", ctypes.c_double * 16), ("sweeps", ctypes.c_int), ("solver_iterations", ctypes.c_int),
+                ("solver_rel_residual", ctypes.c_double), ("dt_next", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libxcore_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: run xcore_gb300.build() first (no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        D6 = ctypes.POINTER(ctypes.c_double)
+        sig = {
+            "xc_ctx_create": (ip, [ctypes.POINTER(_Params), ctypes.POINTER(vp)]),
+            "xc_ctx_destroy": (ip, [vp]),
+            "xc_field_count": (ip, []),
+            "xc_field_name": (ctypes.c_char_p, [ip]),
+            "xc_field_id": (ip, [ctypes.c_char_p]),
+            "xc_field_shape": (ip, [vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip), ctypes.POINTER(ip)]),
+            "xc_field_device_ptr": (ip, [vp, ip, ctypes.POINTER(vp)]),
+            "xc_field_upload": (ip, [vp, ip, vp]),
+            "xc_field_download": (ip, [vp, ip, vp]),
+            "xc_synchronize": (ip, [vp]),
+            "xc_store_previous": (ip, [vp]),
+            "xc_store_noise": (ip, [vp]),
+            "xc_snapshot": (ip, [vp]),
+            "xc_phsevo": (ip, [vp, ip, D6, dp, dp]),
+            "xc_fluidmech": (ip, [vp, D6, dp, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)]),
+            "xc_fluidmech_mms": (ip, [vp, vp, vp, vp, vp, vp, vp, D6, dp, ctypes.POINTER(SolverOpts),
+                                      ctypes.POINTER(SolverStats)]),
+            "xc_noise": (ip, [vp, dp, ip, vp, vp]),
+            "xc_update_phase_velocities": (ip, [vp]),
+            "xc_update": (ip, [vp]),
+            "xc_update_dt": (ip, [vp, dp, D6]),
+            "xc_resnorm": (ip, [vp, dp, D6]),
+            "xc_conservation_sums": (ip, [vp, D6]),
+            "xc_initialize": (ip, [vp, vp, vp, vp]),
+            "xc_step": (ip, [vp, ip, dp, ip, vp, vp, ctypes.POINTER(SolverOpts), ctypes.POINTER(StepStats)]),
+            "xc_fill_ghosts": (ip, [vp, ip, ip, ip, ip, ip, vp]),
+            "xc_advect": (ip, [vp, vp, vp, vp, ip, ip, dp, ip, vp]),
+            "xc_advect_with_flux": (ip, [vp, vp, vp, vp, vp, vp, ip, ip, dp, ip, ip, ip, vp]),
+            "xc_advect_centered_with_flux": (ip, [vp, vp, vp, vp, vp, vp, ip, ip, dp, ip, ip, ip, vp]),
+            "xc_diffus": (ip, [vp, vp, vp, ip, ip, dp, vp]),
+            "xc_diffus_with_flux": (ip, [vp, vp, vp, vp, vp, ip, ip, dp, ip, ip, vp]),
+            "xc_time_coefs": (ip, [ip, ip, D6]),
+            "xc_last_error": (ctypes.c_char_p, []),
+            "xc_version": (ctypes.c_char_p, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != XC_OK:
+        msg = lib().xc_last_error().decode()
+        if status == XC_NOT_CONVERGED:
+            raise NotConverged(status, msg)
+        raise XcoreError(status, msg)
+
+
+def build(force: bool = False) -> str:
+    """Compile the CUDA sources in-tree (nvcc, sm_103a) and return the .so path."""
+    from importlib import util
+    spec = util.spec_from_file_location("_xcore_gb300_build", os.path.join(_HERE, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def field_names():
+    L = lib()
+    return [L.xc_field_name(i).decode() for i in range(L.xc_field_count())]
+
+
+# ---------------------------------------------------------------------------
+# host-side scalar setup (restated from the reference)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class Parameters:
+    """Parameters{Float64} fields the path reads (src/parameters.jl:12-89)."""
+    D: float = 10.0
+    N: int = 100
+    L: float = 10.0
+    x0: float = EPS
+    dxr: float = 0.1
+    rhom0: float = 2700.0
+    rhox0: float = 3200.0
+    d0: float = 0.01
+    g0: float = 10.0
+    etam0: float = 10.0
+    etax0: float = 1e18
+    AA: tuple = ((0.72, 0.19), (0.81, 0.20))
+    BB: tuple = ((0.63, 0.37), (0.999, 0.001))
+    CC: tuple = ((2.09, 0.09), (0.37, 1.45))
+    L0: float = 0.1
+    l0: float = 0.1
+    Da: float = 0.01
+    Xi: float = 0.5
+    Ptop: float = 1e5
+    open_sgr: bool = False
+    TINT: str = "bd2im"
+    ADVN: str = "weno5"
+    CFL: float = 0.5
+    alpha: float = 0.9
+    gamma: float = 1e-3
+    dtmax: float = 1e32
+    etacntr: float = 1e8
+
+
+@dataclass
+class Grid:
+    """src/grid.jl:311-334."""
+    Nx: int
+    Nz: int
+    h: float
+    D: float
+    L: float
+
+    @classmethod
+    def from_params(cls, p: Parameters) -> "Grid":
+        h = p.D / p.N
+        return cls(Nx=max(1, int(round(p.L / h))), Nz=p.N, h=h, D=p.D, L=p.L)
+
+
+def compute_scales(p: Parameters, g: Grid, tol: float = 1e-9, maxiter: int = 200) -> dict:
+    """The scales the path reads, from the fixed point of src/scales.jl:85-185."""
+    D, d0, x0, Da, h = p.D, p.d0, p.x0, p.Da, g.h
+    rho0, Drho0, eta0, g0 = p.rhom0, p.rhox0 - p.rhom0, p.etam0, p.g0
+    D0 = D / 10
+    L0, l0 = p.L0, p.l0
+    L0h, l0h = (L0 + h) / 2, (l0 + h) / 2
+    bnd_w = l0 / 2 + D / 100
+    chi0, Dchi0 = (Da, Da / 10) if Da > 0 else (x0, x0 / 10)
+    W0 = Dchi0 * Drho0 * g0 * (D0 * D0) / eta0
+    w0 = Drho0 * g0 * (d0 * d0) / eta0
+    W0t = math.sqrt(Dchi0 * Drho0 * g0 * (D0 * D0 * D0) / ((L0 * L0) * rho0))
+    W0i = math.sqrt(Dchi0 * Drho0 * g0 * D / rho0)
+    Ri2 = (W0i / W0t) ** 2
+    fReL0 = 1 - math.exp(-(W0 * L0 / (eta0 / rho0)))
+    for _ in range(maxiter):
+        W0p, w0p = W0, w0
+        fReL0 = 1 - math.exp(-(W0 * L0 / (eta0 / rho0)))
+        fRel0 = 1 - math.exp(-(w0 * l0 / (eta0 / rho0)))
+        W0 = (math.sqrt(4 / Ri2 * Dchi0 * Drho0 * g0 * rho0 * fReL0 * (L0 * L0) * D0 + eta0 * eta0) - eta0) \
+            * D0 / (2 * fReL0 * (L0 * L0) * rho0 / Ri2)
+        w0 = (math.sqrt(4 * Drho0 * g0 * rho0 * fRel0 * l0 * (d0 * d0) + eta0 * eta0) - eta0) / (2 * fRel0 * l0 * rho0)
+        if abs(W0 - W0p) / W0 + abs(w0 - w0p) / w0 <= tol:
+            break
+    ke0 = (W0 / D0) * (L0 * L0)
+    ks0 = w0 * l0
+    kx0 = ks0 + fReL0 * ke0
+    tW0, tw0, tk0, ti0 = D / W0, D / w0, (D * D) / kx0, D / W0i
+    t0 = 1.0 / (1 / (ti0 + tW0) + 1 / tw0 + 1 / tk0)
+    return dict(D0=D0, L0=L0, L0h=L0h, l0=l0, l0h=l0h, bnd_w=bnd_w, W0=W0, w0=w0, kx0=kx0,
+                txi0=p.rhox0 * (d0 * d0) / 18 / eta0, t0=t0,
+                dt0=min((h / 2) * (h / 2) / kx0, (h / 2) / (W0 + w0)), G0=Da * rho0 / t0 * D / D0)
+
+
+def time_coefs(TINT: str, step: int):
+    """time_coefs(Float64, TINT, step) through the library (src/timing.jl:18-36)."""
+    out = (ctypes.c_double * 6)()
+    _check(lib().xc_time_coefs(TINTS[TINT], int(step), out))
+    return tuple(out)
+
+
+# ---------------------------------------------------------------------------
+# device state
+# ---------------------------------------------------------------------------
+
+
+def _host(arr, shape, dtype=np.float64):
+    a = np.asarray(arr, dtype=dtype)
+    if a.shape != tuple(shape):
+        raise ValueError(f"expected shape {tuple(shape)}, got {a.shape}")
+    return np.asfortranarray(a)
+
+
+class State:
+    """FluidState + PhaseState + NoiseState + StepResidual resident on the GPU."""
+
+    def __init__(self, par: Parameters, grid: Grid | None = None, scales: dict | None = None,
+                 xBC="periodic", zBC="closed", sds=-1, top_cnv=1, bot_cnv=1, open_cnv=False):
+        self.par = par
+        self.grid = grid or Grid.from_params(par)
+        self.scales = scales or compute_scales(par, self.grid)
+        g, s = self.grid, self.scales
+        P = _Params()
+        P.Nz, P.Nx, P.h, P.D = g.Nz, g.Nx, g.h, g.D
+        for k in ("rhom0", "rhox0", "d0", "g0", "etam0", "etax0", "Xi", "Ptop", "alpha", "gamma", "CFL",
+                  "dtmax", "etacntr"):
+            setattr(P, k, float(getattr(par, k)))
+        for k in ("AA", "BB", "CC"):
+            m = getattr(par, k)
+            getattr(P, k)[:] = [m[0][0], m[0][1], m[1][0], m[1][1]]
+        P.open_sgr = int(bool(par.open_sgr))
+        for k in ("L0", "l0", "L0h", "l0h", "D0", "txi0", "G0", "bnd_w", "dt0"):
+            setattr(P, k, float(s[k]))
+        P.ADVN, P.TINT = SCHEMES[par.ADVN], TINTS[par.TINT]
+        P.xBC, P.zBC = BCS[xBC], BCS[zBC]
+        P.sds, P.top_cnv, P.bot_cnv, P.open_cnv = int(sds), int(top_cnv), int(bot_cnv), int(bool(open_cnv))
+        self._p = P
+        h = ctypes.c_void_p()
+        _check(lib().xc_ctx_create(ctypes.byref(P), ctypes.byref(h)))
+        self._h = h
+        self._ids = {n: i for i, n in enumerate(field_names())}
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().xc_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- fields ------------------------------------------------------------
+    def shape(self, name):
+        r, c, e = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().xc_field_shape(self._h, self._ids[name], ctypes.byref(r), ctypes.byref(c), ctypes.byref(e)))
+        return (r.value, c.value), e.value
+
+    def __getitem__(self, name):
+        shp, eb = self.shape(name)
+        out = np.empty(shp, dtype=np.float64 if eb == 8 else np.uint8, order="F")
+        _check(lib().xc_field_download(self._h, self._ids[name], out.ctypes.data))
+        return np.ascontiguousarray(out) if eb == 8 else out.astype(bool)
+
+    def __setitem__(self, name, value):
+        shp, eb = self.shape(name)
+        a = _host(value, shp, np.float64 if eb == 8 else np.uint8)
+        _check(lib().xc_field_upload(self._h, self._ids[name], a.ctypes.data))
+
+    def device_ptr(self, name) -> int:
+        p = ctypes.c_void_p()
+        _check(lib().xc_field_device_ptr(self._h, self._ids[name], ctypes.byref(p)))
+        return p.value
+
+    def synchronize(self):
+        _check(lib().xc_synchronize(self._h))
+
+    # -- the reference's functions ------------------------------------------
+    def store_previous(self):
+        """store_previous!(fluid, phase) -- src/store.jl:13-30."""
+        _check(lib().xc_store_previous(self._h))
+
+    def store_noise(self):
+        """store_noise!(ns) -- src/noise.jl:115-120."""
+        _check(lib().xc_store_noise(self._h))
+
+    def snapshot(self):
+        """snapshot!(res, phase, fluid) -- src/diagnose.jl:42-49."""
+        _check(lib().xc_snapshot(self._h))
+
+    def phsevo(self, coefs, dt, ADVN=None, alpha=None):
+        """phsevo!(phase, fluid, grid, par, scales; ADVN, a1..b3, dt, alpha) -- src/phsevo.jl:164-214."""
+        c6 = (ctypes.c_double * 6)(*coefs)
+        scheme = -1 if ADVN is None else SCHEMES[ADVN]
+        _check(lib().xc_phsevo(self._h, scheme, c6, float(dt), float(self.par.alpha if alpha is None else alpha)))
+
+    def fluidmech(self, coefs, dt, solver="fgmres64", rtol=1e-10, maxit=500, restart=40,
+                  inner_rtol=1e-4, inner_maxit=60, mms=None):
+        """fluidmech!(fluid, grid, par; phase, ..., dt, a1..b3) -- src/fluidmech.jl:71-534.
+
+        The sparse LU of the reference is replaced by an iterative solve;
+        returns its statistics.  ``mms`` = dict of src_W/src_U/src_P/W_exact/
+        U_exact/P_exact host arrays selects the manufactured-solution branch."""
+        c6 = (ctypes.c_double * 6)(*coefs)
+        o = SolverOpts(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit))
+        st = SolverStats()
+        if mms is None:
+            status = lib().xc_fluidmech(self._h, c6, float(dt), ctypes.byref(o), ctypes.byref(st))
+        else:
+            g = self.grid
+            arrs = [_host(mms[k], shp) for k, shp in (
+                ("src_W", (g.Nz + 1, g.Nx + 2)), ("src_U", (g.Nz + 2, g.Nx + 1)), ("src_P", (g.Nz + 2, g.Nx + 2)),
+                ("W_exact", (g.Nz + 1, g.Nx + 2)), ("U_exact", (g.Nz + 2, g.Nx + 1)),
+                ("P_exact", (g.Nz + 2, g.Nx + 2)))]
+            status = lib().xc_fluidmech_mms(self._h, *[a.ctypes.data for a in arrs], c6, float(dt),
+                                            ctypes.byref(o), ctypes.byref(st))
+        _check(status)
+        return {k: getattr(st, k) for k, _ in SolverStats._fields_}
+
+    def noise(self, dt, first_iter=True, re=None, rs=None):
+        """noise!(ns, phase, grid, par, scales, dt; first_iter) -- src/noise.jl:138-239.
+        re/rs replace the reference's randn! draw on the first sweep."""
+        g = self.grid
+        a = _host(re, (g.Nz, g.Nx)) if re is not None else None
+        b = _host(rs, (g.Nz, g.Nx)) if rs is not None else None
+        _check(lib().xc_noise(self._h, float(dt), int(bool(first_iter)),
+                              a.ctypes.data if a is not None else None, b.ctypes.data if b is not None else None))
+
+    def update_phase_velocities(self):
+        """update_phase_velocities!(phase, fluid, ns, grid, par) -- src/store.jl:80-105."""
+        _check(lib().xc_update_phase_velocities(self._h))
+
+    def update(self):
+        """update!(phase, fluid, grid, par, scales) -- src/update.jl:525-538."""
+        _check(lib().xc_update(self._h))
+
+    def update_dt(self, dt_prev):
+        """update_dt(phase, fluid, grid, par, dt_prev) -- src/update.jl:494-502."""
+        out = ctypes.c_double()
+        _check(lib().xc_update_dt(self._h, float(dt_prev), ctypes.byref(out)))
+        return out.value
+
+    def compute_resnorm(self, dt):
+        """compute_resnorm(res, phase, fluid, dt) -- src/diagnose.jl:57-71."""
+        out = (ctypes.c_double * 3)()
+        _check(lib().xc_resnorm(self._h, float(dt), out))
+        return tuple(out)
+
+    def conservation_sums(self):
+        """FP64 sums of record_history! -- src/history.jl:121-145."""
+        out = (ctypes.c_double * 12)()
+        _check(lib().xc_conservation_sums(self._h, out))
+        keys = ("sumB", "sumM", "sumX", "sumGx", "top_aX", "bot_aX", "top_aM", "bot_aM", "top_dX", "bot_dX",
+                "top_dM", "bot_dM")
+        return dict(zip(keys, out))
+
+    def initialize(self, x_init, re, rs):
+        """Fresh-start initialize! -- src/run.jl:71-140 (x_init replaces the
+        seeded perturbation, re/rs the first noise draw)."""
+        g = self.grid
+        x = _host(x_init, (g.Nz, g.Nx))
+        a, b = _host(re, (g.Nz, g.Nx)), _host(rs, (g.Nz, g.Nx))
+        _check(lib().xc_initialize(self._h, x.ctypes.data, a.ctypes.data, b.ctypes.data))
+
+    def step(self, step, dt, re=None, rs=None, sweeps=3, solver="fgmres64", rtol=1e-10, maxit=500,
+             restart=40, inner_rtol=1e-4, inner_maxit=60):
+        """One outer step of run! (src/run.jl:204-274) with `sweeps` Picard sweeps."""
+        g = self.grid
+        a = _host(re, (g.Nz, g.Nx)) if re is not None else None
+        b = _host(rs, (g.Nz, g.Nx)) if rs is not None else None
+        o = SolverOpts(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit))
+        st = StepStats()
+        _check(lib().xc_step(self._h, int(step), float(dt), int(sweeps),
+                             a.ctypes.data if a is not None else None, b.ctypes.data if b is not None else None,
+                             ctypes.byref(o), ctypes.byref(st)))
+        return dict(resnorm=list(st.resnorm[:st.sweeps]), sweeps=st.sweeps, solver_iterations=st.solver_iterations,
+                    solver_rel_residual=st.solver_rel_residual, dt_next=st.dt_next)
+
+
+# ---------------------------------------------------------------------------
+# stencil-level functions on device arrays (torch CUDA tensors laid out
+# column-major: a (rows, cols) Julia matrix is a contiguous torch tensor of
+# shape (cols, rows))
+# ---------------------------------------------------------------------------
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    return ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+
+
+def fill_ghosts(f, halo, zBC="closed", xBC="periodic", stream=None):
+    """fill_ghosts!(f, halo; zBC, xBC) -- src/kernels/ghosts.jl:18-51."""
+    Nx, Nz = f.shape[0] - 2 * halo, f.shape[1] - 2 * halo
+    _check(lib().xc_fill_ghosts(_ptr(f), Nz, Nx, halo, BCS[zBC], BCS[xBC], _stream(stream)))
+
+
+def advect(adv, f_halo, u, w, h, scheme, stream=None):
+    """advect!(adv, f_halo, u, w, h, scheme) -- src/kernels/advect.jl:374-425."""
+    Nx, Nz = adv.shape
+    _check(lib().xc_advect(_ptr(adv), _ptr(f_halo), _ptr(u), _ptr(w), Nz, Nx, float(h), SCHEMES[scheme],
+                           _stream(stream)))
+
+
+def advect_with_flux(adv, qx, qz, f_halo, u, w, h, scheme, xBC="periodic", zBC="closed", stream=None):
+    """advect_with_flux! -- src/kernels/advect.jl:717-798."""
+    Nx, Nz = adv.shape
+    _check(lib().xc_advect_with_flux(_ptr(adv), _ptr(qx), _ptr(qz), _ptr(f_halo), _ptr(u), _ptr(w), Nz, Nx,
+                                     float(h), SCHEMES[scheme], BCS[xBC], BCS[zBC], _stream(stream)))
+
+
+def advect_centered_with_flux(adv, qx, qz, f, u, w, h, scheme, xBC="periodic", zBC="closed", stream=None):
+    """advect_centered_with_flux! -- src/phsevo.jl:90-128 (qx/qz may be None)."""
+    Nx, Nz = adv.shape
+    _check(lib().xc_advect_centered_with_flux(_ptr(adv), _ptr(qx) if qx is not None else None,
+                                              _ptr(qz) if qz is not None else None, _ptr(f), _ptr(u), _ptr(w),
+                                              Nz, Nx, float(h), SCHEMES[scheme], BCS[xBC], BCS[zBC],
+                                              _stream(stream)))
+
+
+def diffus(dff, f_halo, k_halo, h, stream=None):
+    """diffus!(dff, f_halo, k_halo, h) -- src/kernels/diffus.jl:109-121."""
+    Nx, Nz = dff.shape
+    _check(lib().xc_diffus(_ptr(dff), _ptr(f_halo), _ptr(k_halo), Nz, Nx, float(h), _stream(stream)))
+
+
+def diffus_with_flux(dff, qx, qz, f_halo, k_halo, h, xBC="periodic", zBC="closed", stream=None):
+    """diffus_with_flux! -- src/kernels/diffus.jl:169-211."""
+    Nx, Nz = dff.shape
+    _check(lib().xc_diffus_with_flux(_ptr(dff), _ptr(qx), _ptr(qz), _ptr(f_halo), _ptr(k_halo), Nz, Nx,
+                                     float(h), BCS[xBC], BCS[zBC], _stream(stream)))

@@ -1,0 +1,216 @@
+// Internal declarations shared by the translation units of libxcore_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cstddef>
+#include <cstdio>
+#include <string>
+
+#include "xcore_gb300.h"
+
+// ---------------------------------------------------------------------------
+// field registry: name, shape code, element size.  Shape codes follow the
+// reference sizes (src/state.jl:57-69, 143-163; src/noise.jl:25-35).
+// ---------------------------------------------------------------------------
+enum ShapeCode : int {
+  SH_C = 0,   // (Nz,   Nx)
+  SH_ZF,      // (Nz+1, Nx)     z-faces, x-interior
+  SH_XF,      // (Nz,   Nx+1)   x-faces, z-interior
+  SH_W,       // (Nz+1, Nx+2)   W-shaped (z-faces with x ghost columns), also qz
+  SH_U,       // (Nz+2, Nx+1)   U-shaped (x-faces with z ghost rows), also qx
+  SH_CO,      // (Nz+1, Nx+1)   corners
+  SH_P        // (Nz+2, Nx+2)   pressure with ghost ring
+};
+
+// X-macro: (identifier, shape, element bytes)
+#define XC_FIELDS(F)                                                                   \
+  F(W, SH_W, 8) F(U, SH_U, 8) F(P, SH_P, 8) F(eta, SH_C, 8) F(etaco, SH_CO, 8)         \
+  F(rho, SH_C, 8) F(rhow, SH_ZF, 8) F(rhou, SH_XF, 8) F(Drho, SH_ZF, 8)                \
+  F(rhoo, SH_C, 8) F(rhooo, SH_C, 8) F(drhodt, SH_C, 8) F(drhodto, SH_C, 8)            \
+  F(drhodtoo, SH_C, 8) F(MFS, SH_C, 8) F(rhoWo, SH_ZF, 8) F(rhoWoo, SH_ZF, 8)          \
+  F(rhoUo, SH_XF, 8) F(rhoUoo, SH_XF, 8)                                               \
+  F(x, SH_C, 8) F(m, SH_C, 8) F(X, SH_C, 8) F(M, SH_C, 8) F(Xo, SH_C, 8)               \
+  F(Xoo, SH_C, 8) F(Mo, SH_C, 8) F(Moo, SH_C, 8) F(chi, SH_C, 8) F(mu, SH_C, 8)        \
+  F(hasx, SH_C, 1) F(hasm, SH_C, 1)                                                    \
+  F(chiw, SH_W, 8) F(muw, SH_W, 8) F(chiu, SH_U, 8) F(muu, SH_U, 8)                    \
+  F(x_w, SH_ZF, 8) F(m_w, SH_ZF, 8) F(x_u, SH_XF, 8) F(m_u, SH_XF, 8)                  \
+  F(Drhom, SH_ZF, 8) F(Drhox, SH_ZF, 8) F(Pl, SH_C, 8) F(Pt, SH_C, 8)                  \
+  F(etamix, SH_C, 8) F(etae, SH_C, 8) F(ke, SH_C, 8) F(kx, SH_C, 8)                    \
+  F(etat, SH_C, 8) F(etas, SH_C, 8) F(etasw, SH_ZF, 8) F(ks, SH_C, 8)                  \
+  F(V, SH_C, 8) F(Div_V, SH_C, 8) F(exx, SH_C, 8) F(ezz, SH_C, 8) F(exz, SH_CO, 8)     \
+  F(eII, SH_C, 8) F(vx, SH_C, 8) F(vm, SH_C, 8) F(txx, SH_C, 8) F(tzz, SH_C, 8)        \
+  F(txz, SH_CO, 8) F(tII, SH_C, 8) F(fReL, SH_C, 8) F(ReL, SH_C, 8) F(ReD, SH_C, 8)    \
+  F(Ra, SH_C, 8) F(fRel, SH_C, 8) F(Rel, SH_C, 8) F(Red, SH_C, 8) F(Rc, SH_C, 8)       \
+  F(Wx, SH_W, 8) F(Wm, SH_W, 8) F(Ux, SH_U, 8) F(Um, SH_U, 8) F(wx, SH_W, 8)           \
+  F(wm, SH_W, 8) F(bndtaperw, SH_W, 8) F(bndshape, SH_C, 8)                            \
+  F(advn_X, SH_C, 8) F(advn_M, SH_C, 8) F(advn_rho, SH_C, 8)                           \
+  F(qx_advn_X, SH_U, 8) F(qz_advn_X, SH_W, 8) F(qx_advn_M, SH_U, 8)                    \
+  F(qz_advn_M, SH_W, 8) F(qx_dffn_X, SH_U, 8) F(qz_dffn_X, SH_W, 8)                    \
+  F(qx_dffn_M, SH_U, 8) F(qz_dffn_M, SH_W, 8) F(dffn_X, SH_C, 8) F(Gx, SH_C, 8)        \
+  F(dXdt, SH_C, 8) F(dXdto, SH_C, 8) F(dXdtoo, SH_C, 8)                                \
+  F(psie, SH_C, 8) F(psix, SH_C, 8) F(psis, SH_C, 8) F(psieo, SH_C, 8)                 \
+  F(psixo, SH_C, 8) F(psiso, SH_C, 8) F(re, SH_C, 8) F(rs, SH_C, 8)                    \
+  F(xiew, SH_W, 8) F(xieu, SH_U, 8) F(xixw, SH_W, 8) F(xixu, SH_U, 8)                  \
+  F(xisw, SH_W, 8) F(xisu, SH_U, 8) F(xie, SH_C, 8) F(xix, SH_C, 8) F(xis, SH_C, 8)    \
+  F(res_Wo, SH_W, 8) F(res_Uo, SH_U, 8) F(res_Po, SH_P, 8) F(res_Xo, SH_C, 8)          \
+  F(res_MFSo, SH_C, 8)
+
+enum FieldId : int {
+#define XC_ENUM(name, sh, eb) FLD_##name,
+  XC_FIELDS(XC_ENUM)
+#undef XC_ENUM
+  FLD_COUNT
+};
+
+struct Shape { int rows, cols; };
+
+inline Shape shape_of(int code, int Nz, int Nx) {
+  switch (code) {
+    case SH_C: return {Nz, Nx};
+    case SH_ZF: return {Nz + 1, Nx};
+    case SH_XF: return {Nz, Nx + 1};
+    case SH_W: return {Nz + 1, Nx + 2};
+    case SH_U: return {Nz + 2, Nx + 1};
+    case SH_CO: return {Nz + 1, Nx + 1};
+    default: return {Nz + 2, Nx + 2};
+  }
+}
+
+// ---------------------------------------------------------------------------
+// error handling
+// ---------------------------------------------------------------------------
+void xc_set_error(const char* fmt, ...);
+
+#define XC_CUDA_TRY(call)                                                               \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      xc_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));  \
+      return XC_CUDA;                                                                   \
+    }                                                                                   \
+  } while (0)
+
+#define XC_LAUNCH_CHECK() XC_CUDA_TRY(cudaGetLastError())
+
+#define XC_TRY(expr)               \
+  do {                             \
+    int s_ = (expr);               \
+    if (s_ != XC_OK) return s_;    \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device views
+// ---------------------------------------------------------------------------
+struct DView {        // column-major view of a field (or a sub-block of one)
+  double* p;
+  int ld;             // leading dimension (rows of the parent array)
+};
+
+struct CView {
+  const double* p;
+  int ld;
+};
+
+__host__ __device__ inline DView dview(double* p, int ld) { return DView{p, ld}; }
+__host__ __device__ inline CView cview(const double* p, int ld) { return CView{p, ld}; }
+
+#define AT(v, j, i) ((v).p[(size_t)(i) * (size_t)(v).ld + (size_t)(j)])
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct NoisePlan;     // xc_noise.cu
+struct StokesWork;    // xc_stokes.cu
+
+struct xc_ctx {
+  xc_params p;
+  int Nz, Nx;
+  int device;
+  cudaStream_t stream;
+  char* arena;
+  size_t arena_bytes;
+  void* field[FLD_COUNT];
+  Shape shape[FLD_COUNT];
+  int elem[FLD_COUNT];
+  // scratch
+  double* red_partials;      // block partials of reductions
+  int red_partials_len;
+  double* dscal;             // device scalars (64 slots)
+  double* hscal;             // pinned host mirror of dscal
+  double* tmp[8];            // full-size (Nz+2)x(Nx+2) FP64 temporaries
+  NoisePlan* noise;
+  StokesWork* stokes;
+};
+
+// device scalar slots
+enum ScalarSlot : int {
+  SC_EMAX_ETA = 0,
+  SC_EMAX_ETAS = 1,
+  SC_MFS_MEAN = 2,
+  SC_NOISE_STATS = 8,       // 3 fields x 4 values (raw mean, raw std, flt mean, flt std)
+  SC_RESNORM = 24,          // 8 sums of squares
+  SC_DT = 40,               // 5 maxima
+  SC_SUMS = 48,             // 12 conservation sums
+};
+
+inline DView F(xc_ctx* c, int id) { return DView{(double*)c->field[id], c->shape[id].rows}; }
+inline CView CF(xc_ctx* c, int id) { return CView{(const double*)c->field[id], c->shape[id].rows}; }
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+constexpr int kNumSMs = 152;
+
+inline dim3 grid2d(int rows, int cols, dim3 blk) {
+  return dim3((unsigned)((rows + blk.x - 1) / blk.x), (unsigned)((cols + blk.y - 1) / blk.y));
+}
+
+// deterministic reductions (xc_reduce.cu): block partials + single-block final
+enum RedOp : int { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2, RED_SUMSQ = 3, RED_MAXABS = 4,
+                   RED_SUMSQDIFF = 5 };
+// reduce a column-major view of rows x cols into dscal[slot] (device); b may be
+// null unless op == RED_SUMSQDIFF (sum of (a-b)^2)
+int reduce_view(xc_ctx* c, int op, CView a, CView b, int rows, int cols, int slot);
+// general form: optional center (sum of (a - *center)^2), result / divisor into *out
+int reduce_to(xc_ctx* c, int op, CView a, CView b, const double* center, int rows, int cols,
+              double* out, cudaStream_t s, double divisor = 1.0);
+int reduce_partials_len();
+// copy device scalars [first, first+n) to the pinned host mirror and wait
+int fetch_scalars(xc_ctx* c, int first, int n);
+
+// ---------------------------------------------------------------------------
+// entry points implemented per translation unit (status-returning, on c->stream)
+// ---------------------------------------------------------------------------
+int stencil_advect_flux(const double* f, int ldf, bool halod, int Nz, int Nx, int scheme,
+                        int xBC, int zBC, CView u, CView w, double h,
+                        DView adv, DView qx_int, DView qz_int, cudaStream_t s);
+int stencil_diffus_flux(const double* f, const double* k, int ld, bool halod, int Nz, int Nx,
+                        int xBC, int zBC, double h, DView dff, DView qx_int, DView qz_int,
+                        cudaStream_t s);
+int pad_face_fluxes(DView qx, DView qz, int Nz, int Nx, int xBC, int zBC, cudaStream_t s);
+int scheme_halo(int scheme);
+
+int phsevo_impl(xc_ctx* c, int scheme, const double coefs[6], double dt, double alpha);
+int update_impl(xc_ctx* c);
+int phase_velocities_impl(xc_ctx* c);
+int store_previous_impl(xc_ctx* c);
+int store_noise_impl(xc_ctx* c);
+int snapshot_impl(xc_ctx* c);
+int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out);
+int resnorm_impl(xc_ctx* c, double dt, double out[3]);
+int sums_impl(xc_ctx* c, double out[12]);
+
+int noise_plan_create(xc_ctx* c);
+void noise_plan_destroy(xc_ctx* c);
+int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const double* rs);
+
+int stokes_create(xc_ctx* c);
+void stokes_destroy(xc_ctx* c);
+struct MmsData { const double *src_W, *src_U, *src_P, *W_exact, *U_exact, *P_exact; };
+int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_opts* opts,
+                   xc_solver_stats* stats, const MmsData* mms);
+
+// machine epsilon of Float64 and its square root (eps(T), sqrt(eps(T)))
+#define XC_EPS 2.220446049250313080847e-16
+#define XC_SQRT_EPS 1.4901161193847656e-08

@@ -1,0 +1,519 @@
+// Constitutive update!, store_previous!, update_phase_velocities!, update_dt,
+// compute_resnorm and the FP64 conservation sums on the GPU.
+//
+// Reference: src/update.jl, src/store.jl, src/diagnose.jl:42-71,
+// src/history.jl:121-145.  Each kernel keeps the reference's per-element
+// operation order; compiled with -fmad=false.  exp / pow are CUDA's, so
+// results agree with the reference arithmetic to a few ulp (the reference's
+// own libm differs from any other libm by as much).
+#include <cmath>
+
+#include "xc_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ int icz_at(int j, int Nz, int zBC) {   // icz[j], j = 0..Nz+1
+  if (j == 0) return zBC == XC_PERIODIC ? Nz - 1 : 0;
+  if (j == Nz + 1) return zBC == XC_PERIODIC ? 0 : Nz - 1;
+  return j - 1;
+}
+__device__ __forceinline__ int icx_at(int i, int Nx, int xBC) {   // icx[i], i = 0..Nx+1
+  if (i == 0) return xBC == XC_PERIODIC ? Nx - 1 : 0;
+  if (i == Nx + 1) return xBC == XC_PERIODIC ? 0 : Nx - 1;
+  return i - 1;
+}
+__device__ __forceinline__ double clampd(double x, double lo, double hi) {
+  return x > hi ? hi : (x < lo ? lo : x);
+}
+
+struct Rheo {
+  double A11, A12, A21, A22, B11, B12, B21, B22, iC11, iC12, iC21, iC22, ex, em;
+};
+
+// compute_volfrac_kernel! (update.jl:18-35) fused with compute_rheology_kernel!
+// (update.jl:144-177), one thread per cell
+__global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rhox0, Rheo r,
+                                        CView x, CView m, DView rho, DView chi, DView mu,
+                                        uint8_t* hasx, uint8_t* hasm, DView etamix) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j >= Nz || i >= Nx) return;
+  double xc = AT(x, j, i), mc = AT(m, j, i);
+  double rh = 1.0 / (mc / rhom0 + xc / rhox0);
+  AT(rho, j, i) = rh;
+  double f1 = clampd((xc * rh) / rhox0, XC_EPS, 1.0 - XC_EPS);
+  double f2 = clampd((mc * rh) / rhom0, XC_EPS, 1.0 - XC_EPS);
+  AT(chi, j, i) = f1;
+  AT(mu, j, i) = f2;
+  size_t o = (size_t)i * Nz + j;
+  hasx[o] = xc >= XC_SQRT_EPS;
+  hasm[o] = mc >= XC_SQRT_EPS;
+  double s11 = pow(f1 / r.B11, r.iC11), s12 = pow(f2 / r.B12, r.iC12);
+  double s21 = pow(f1 / r.B21, r.iC21), s22 = pow(f2 / r.B22, r.iC22);
+  double n1 = s11 + s12, n2 = s21 + s22;
+  double Sf11 = s11 / n1, Sf12 = s12 / n1, Sf21 = s21 / n2, Sf22 = s22 / n2;
+  double a1 = r.A11 * Sf11 + r.A12 * Sf12;
+  double a2 = r.A21 * Sf21 + r.A22 * Sf22;
+  double Xf11 = a1 * f1 + (1.0 - a1) * Sf11;
+  double Xf12 = a1 * f2 + (1.0 - a1) * Sf12;
+  double Xf21 = a2 * f1 + (1.0 - a2) * Sf21;
+  double Xf22 = a2 * f2 + (1.0 - a2) * Sf22;
+  double thtv1 = pow(r.ex / r.ex, Xf11) * pow(r.em / r.ex, Xf12);
+  double thtv2 = pow(r.ex / r.em, Xf21) * pow(r.em / r.em, Xf22);
+  double etaf1 = r.ex * thtv1, etaf2 = r.em * thtv2;
+  AT(etamix, j, i) = f1 * etaf1 + f2 * etaf2;
+}
+
+// update_interpolations! (update.jl:73-107) without the row mean; one thread
+// per (j, i) of the (Nz+2, Nx+2) bounding box
+__global__ void interp_kernel(int Nz, int Nx, int xBC, int zBC, double rhom0, double rhox0,
+                              CView rho, CView chi, CView mu, CView x, CView m, DView rhow,
+                              DView rhou, DView Drhom, DView Drhox, DView chiw, DView muw,
+                              DView chiu, DView muu, DView x_w, DView m_w, DView x_u,
+                              DView m_u) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz + 1 || i > Nx + 1) return;
+  if (j <= Nz && i < Nx) {   // (Nz+1, Nx)
+    int a = icz_at(j, Nz, zBC), b = icz_at(j + 1, Nz, zBC);
+    double rw = (AT(rho, a, i) + AT(rho, b, i)) / 2.0;
+    AT(rhow, j, i) = rw;
+    AT(Drhom, j, i) = rhom0 - rw;
+    AT(Drhox, j, i) = rhox0 - rw;
+    AT(x_w, j, i) = (AT(x, a, i) + AT(x, b, i)) / 2.0;
+    AT(m_w, j, i) = (AT(m, a, i) + AT(m, b, i)) / 2.0;
+  }
+  if (j < Nz && i <= Nx) {   // (Nz, Nx+1)
+    int a = icx_at(i, Nx, xBC), b = icx_at(i + 1, Nx, xBC);
+    AT(rhou, j, i) = (AT(rho, j, a) + AT(rho, j, b)) / 2.0;
+    AT(x_u, j, i) = (AT(x, j, a) + AT(x, j, b)) / 2.0;
+    AT(m_u, j, i) = (AT(m, j, a) + AT(m, j, b)) / 2.0;
+  }
+  if (j <= Nz) {             // (Nz+1, Nx+2)
+    int a = icz_at(j, Nz, zBC), b = icz_at(j + 1, Nz, zBC), ci = icx_at(i, Nx, xBC);
+    AT(chiw, j, i) = (AT(chi, a, ci) + AT(chi, b, ci)) / 2.0;
+    AT(muw, j, i) = (AT(mu, a, ci) + AT(mu, b, ci)) / 2.0;
+  }
+  if (i <= Nx) {             // (Nz+2, Nx+1)
+    int cj = icz_at(j, Nz, zBC), a = icx_at(i, Nx, xBC), b = icx_at(i + 1, Nx, xBC);
+    AT(chiu, j, i) = (AT(chi, cj, a) + AT(chi, cj, b)) / 2.0;
+    AT(muu, j, i) = (AT(mu, cj, a) + AT(mu, cj, b)) / 2.0;
+  }
+}
+
+// mean(rhow, dims=2) (sequential over columns, as Julia reduces a
+// non-leading dimension) and the lithostatic z-scan of update_pressure!
+// (update.jl:119-131).  One CTA; rhoref and Pl_col go to scratch.
+__global__ void rowmean_scan_kernel(int Nz, int Nx, CView rhow, double g0, double h, double Ptop,
+                                    double* rhoref, double* plcol) {
+  for (int j = threadIdx.x; j <= Nz; j += blockDim.x) {
+    double acc = 0.0;
+    for (int i = 0; i < Nx; ++i) acc = acc + AT(rhow, j, i);
+    rhoref[j] = acc / (double)Nx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double p = ((rhoref[0] * g0) * h) / 2.0 + Ptop;
+    plcol[0] = p;
+    for (int j = 1; j < Nz; ++j) {
+      p = p + (rhoref[j] * g0) * h;
+      plcol[j] = p;
+    }
+  }
+}
+
+// Drho = rhow - rhoref (update.jl:86-87); Pl, Pt (update.jl:132-134)
+__global__ void drho_pressure_kernel(int Nz, int Nx, double Ptop, const double* rhoref,
+                                     const double* plcol, CView rhow, DView Drho, CView P,
+                                     DView Pl, DView Pt) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz || i >= Nx) return;
+  AT(Drho, j, i) = AT(rhow, j, i) - rhoref[j];
+  if (j < Nz) {
+    double pl = plcol[j];
+    AT(Pl, j, i) = pl;
+    AT(Pt, j, i) = fmax(Ptop / 100.0, pl + AT(P, j + 1, i + 1));
+  }
+}
+
+__device__ __forceinline__ double exz_at(CView W, CView U, int j, int i, double invh) {
+  double dUdz = (AT(U, j + 1, i) - AT(U, j, i)) * invh;
+  double dWdx = (AT(W, j, i + 1) - AT(W, j, i)) * invh;
+  return (dUdz + dWdx) / 2.0;
+}
+
+// update_kinematics! (update.jl:202-280): exz on corners, the rest on cells
+__global__ void kinematics_kernel(int Nz, int Nx, double invh, CView W, CView U, CView wx,
+                                  CView wm, DView exz, DView exx, DView ezz, DView Div_V,
+                                  DView eII, DView V, DView vx, DView vm) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz || i > Nx) return;
+  AT(exz, j, i) = exz_at(W, U, j, i, invh);
+  if (j >= Nz || i >= Nx) return;
+  double Ux_c = (AT(U, j + 1, i + 1) - AT(U, j + 1, i)) * invh;
+  double Wz_c = (AT(W, j + 1, i + 1) - AT(W, j, i + 1)) * invh;
+  double div = Ux_c + Wz_c;
+  AT(Div_V, j, i) = div;
+  double ex = Ux_c - div / 3.0, ez = Wz_c - div / 3.0;
+  AT(exx, j, i) = ex;
+  AT(ezz, j, i) = ez;
+  double e1 = exz_at(W, U, j, i, invh), e2 = exz_at(W, U, j + 1, i, invh);
+  double e3 = exz_at(W, U, j, i + 1, invh), e4 = exz_at(W, U, j + 1, i + 1, invh);
+  double exz_sq = (((e1 * e1 + e2 * e2) + e3 * e3) + e4 * e4) / 4.0;
+  AT(eII, j, i) = sqrt((XC_EPS + (ex * ex + ez * ez) / 2.0) + exz_sq);
+  double wc = (AT(W, j, i + 1) + AT(W, j + 1, i + 1)) / 2.0;
+  double uc = (AT(U, j + 1, i) + AT(U, j + 1, i + 1)) / 2.0;
+  AT(V, j, i) = sqrt(wc * wc + uc * uc);
+  double t = (AT(wx, j, i + 1) + AT(wx, j + 1, i + 1)) / 2.0;
+  AT(vx, j, i) = sqrt(t * t + XC_EPS);
+  t = (AT(wm, j, i + 1) + AT(wm, j + 1, i + 1)) / 2.0;
+  AT(vm, j, i) = sqrt(t * t + XC_EPS);
+}
+
+// compute_viscblend_kernel! (update.jl:286-308); etai -> scratch
+__global__ void viscblend_kernel(int Nz, int Nx, double L0, CView etamix, CView eII, CView rho,
+                                 CView V, DView etai, DView etae, DView ke, DView kx, DView ReL,
+                                 DView fReL) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j >= Nz || i >= Nx) return;
+  double r = AT(rho, j, i), em = AT(etamix, j, i);
+  double k = (AT(eII, j, i) * L0) * L0;
+  double Re = (AT(V, j, i) * L0) / (em / r);
+  double f = 1.0 - exp(-Re);
+  double ee = (f * k) * r;
+  AT(etai, j, i) = em + ee;
+  AT(etae, j, i) = ee;
+  AT(ke, j, i) = k;
+  AT(kx, j, i) = k;
+  AT(ReL, j, i) = Re;
+  AT(fReL, j, i) = f;
+}
+
+// contrast cap + Picard blend of eta (update.jl:331-337) fused with
+// compute_segvisc_kernel! (update.jl:345-370); etasi -> scratch
+__global__ void blend_segvisc_kernel(int Nz, int Nx, const double* min_etai, double etacntr,
+                                     double D0, double l0, CView etai, DView eta, CView V,
+                                     CView rho, DView ReD, CView vx, CView etamix, CView ke,
+                                     CView fReL, DView Rel, DView fRel, DView ks, DView etat,
+                                     DView etasi, DView kx, DView Rc) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j >= Nz || i >= Nx) return;
+  double emax = (*min_etai) * etacntr;
+  double e = 1.0 / (1.0 / emax + 1.0 / AT(etai, j, i));
+  double en = 0.5 * e + 0.5 * AT(eta, j, i);
+  AT(eta, j, i) = en;
+  double r = AT(rho, j, i), v = AT(V, j, i);
+  AT(ReD, j, i) = (v * D0) / (en / r);
+  double vxc = AT(vx, j, i), em = AT(etamix, j, i);
+  double Re = ((vxc * l0) * r) / em;
+  double f = 1.0 - exp(-Re);
+  double k = vxc * l0;
+  double et = (f * k) * r;
+  AT(etasi, j, i) = em + et;
+  AT(Rel, j, i) = Re;
+  AT(fRel, j, i) = f;
+  AT(ks, j, i) = k;
+  AT(etat, j, i) = et;
+  AT(kx, j, i) = k + AT(fReL, j, i) * AT(ke, j, i);
+  AT(Rc, j, i) = v / fmax(vxc, XC_EPS);
+}
+
+// cap + blend of etas and Red (update.jl:396-402)
+__global__ void etas_blend_kernel(int Nz, int Nx, const double* min_etasi, double etacntr,
+                                  double d0, CView etasi, DView etas, CView vx, CView rho,
+                                  DView Red) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j >= Nz || i >= Nx) return;
+  double emax = (*min_etasi) * etacntr;
+  double e = 1.0 / (1.0 / emax + 1.0 / AT(etasi, j, i));
+  double en = 0.5 * e + 0.5 * AT(etas, j, i);
+  AT(etas, j, i) = en;
+  AT(Red, j, i) = (AT(vx, j, i) * d0) / (en / AT(rho, j, i));
+}
+
+// compute_corner_eta! (update.jl:411-426, always periodic x / closed z as
+// update_viscosity! calls it, update.jl:341) and etasw (update.jl:405-407)
+__global__ void corner_eta_etasw_kernel(int Nz, int Nx, int zBC, CView eta, DView etaco,
+                                        CView etas, DView etasw) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz || i > Nx) return;
+  int a = icz_at(j, Nz, XC_CLOSED), b = icz_at(j + 1, Nz, XC_CLOSED);
+  int c = icx_at(i, Nx, XC_PERIODIC), d = icx_at(i + 1, Nx, XC_PERIODIC);
+  double e00 = AT(eta, a, c), e10 = AT(eta, b, c), e01 = AT(eta, a, d), e11 = AT(eta, b, d);
+  AT(etaco, j, i) = pow(((e00 * e10) * e01) * e11, 0.25);
+  if (i < Nx) {
+    int p = icz_at(j, Nz, zBC), q = icz_at(j + 1, Nz, zBC);
+    AT(etasw, j, i) = sqrt(AT(etas, p, i) * AT(etas, q, i));
+  }
+}
+
+// update_stresses! (update.jl:432-476)
+__global__ void stress_kernel(int Nz, int Nx, double D0, CView etaco, CView exz, DView txz,
+                              CView eta, CView exx, CView ezz, DView txx, DView tzz, DView tII,
+                              CView V, CView kx, DView Ra) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz || i > Nx) return;
+  AT(txz, j, i) = AT(etaco, j, i) * AT(exz, j, i);
+  if (j >= Nz || i >= Nx) return;
+  double e = AT(eta, j, i);
+  double tx = e * AT(exx, j, i), tz = e * AT(ezz, j, i);
+  AT(txx, j, i) = tx;
+  AT(tzz, j, i) = tz;
+  double t1 = AT(etaco, j, i) * AT(exz, j, i), t2 = AT(etaco, j + 1, i) * AT(exz, j + 1, i);
+  double t3 = AT(etaco, j, i + 1) * AT(exz, j, i + 1);
+  double t4 = AT(etaco, j + 1, i + 1) * AT(exz, j + 1, i + 1);
+  double txz_sq = (((t1 * t1 + t2 * t2) + t3 * t3) + t4 * t4) / 4.0;
+  AT(tII, j, i) = sqrt((XC_EPS + (tx * tx + tz * tz) / 2.0) + txz_sq);
+  AT(Ra, j, i) = (AT(V, j, i) * D0) / AT(kx, j, i);
+}
+
+// update_segregation_speed! + update_phase_velocities! (store.jl:47-105),
+// one thread per (j, i) of the (Nz+2, Nx+2) bounding box
+__global__ void phase_velocities_kernel(int Nz, int Nx, int xBC, int zBC, double d0, double g0,
+                                        CView etasw, CView Drhox, CView bndtaperw, CView x_w,
+                                        CView m_w, CView x_u, CView m_u, CView W, CView U,
+                                        CView xisw, CView xixw, CView xiew, CView xisu,
+                                        CView xixu, CView xieu, DView wx, DView wm, DView Wx,
+                                        DView Wm, DView Ux, DView Um) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz + 1 || i > Nx + 1) return;
+  if (j <= Nz) {   // W-shaped (Nz+1, Nx+2)
+    // the ghost columns copy the tapered interior columns periodically
+    // (store.jl:272-273 applies the copy for every xBC)
+    int is = (i == 0) ? Nx : (i == Nx + 1 ? 1 : i);
+    double w = (((d0 * d0) / AT(etasw, j, is - 1)) * AT(Drhox, j, is - 1)) * g0;
+    w = w * AT(bndtaperw, j, is);
+    AT(wx, j, i) = w;
+    int ci = icx_at(i, Nx, xBC);
+    double xe = AT(x_w, j, ci), me = fmax(AT(m_w, j, ci), XC_EPS);
+    double wmv = ((-xe) / me) * w;
+    AT(wm, j, i) = wmv;
+    double sx = AT(xisw, j, i) + AT(xixw, j, i);
+    double Wv = AT(W, j, i), xe_w = AT(xiew, j, i);
+    AT(Wx, j, i) = ((Wv + w) + sx) + xe_w;
+    AT(Wm, j, i) = ((Wv + wmv) - ((xe / me) * sx)) + xe_w;
+  }
+  if (i <= Nx) {   // U-shaped (Nz+2, Nx+1)
+    int cj = icz_at(j, Nz, zBC);
+    double xe = AT(x_u, cj, i), me = fmax(AT(m_u, cj, i), XC_EPS);
+    double sx = AT(xisu, j, i) + AT(xixu, j, i);
+    double Uv = AT(U, j, i), xe_u = AT(xieu, j, i);
+    AT(Ux, j, i) = (Uv + sx) + xe_u;
+    AT(Um, j, i) = (Uv + (((-xe) / me) * sx)) + xe_u;
+  }
+}
+
+// store_previous! (store.jl:13-30)
+__global__ void store_previous_kernel(int Nz, int Nx, DView X, DView Xo, DView Xoo, DView M,
+                                      DView Mo, DView Moo, DView dXdt, DView dXdto, DView dXdtoo,
+                                      DView rho, DView rhoo, DView rhooo, DView drhodt,
+                                      DView drhodto, DView drhodtoo, CView rhow, CView W,
+                                      DView rhoWo, DView rhoWoo, CView rhou, CView U,
+                                      DView rhoUo, DView rhoUoo) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j > Nz || i > Nx) return;
+  if (j < Nz && i < Nx) {
+    AT(Xoo, j, i) = AT(Xo, j, i); AT(Xo, j, i) = AT(X, j, i);
+    AT(Moo, j, i) = AT(Mo, j, i); AT(Mo, j, i) = AT(M, j, i);
+    AT(dXdtoo, j, i) = AT(dXdto, j, i); AT(dXdto, j, i) = AT(dXdt, j, i);
+    AT(rhooo, j, i) = AT(rhoo, j, i); AT(rhoo, j, i) = AT(rho, j, i);
+    AT(drhodtoo, j, i) = AT(drhodto, j, i); AT(drhodto, j, i) = AT(drhodt, j, i);
+  }
+  if (i < Nx) {    // (Nz+1, Nx)
+    AT(rhoWoo, j, i) = AT(rhoWo, j, i);
+    AT(rhoWo, j, i) = AT(rhow, j, i) * AT(W, j, i + 1);
+  }
+  if (j < Nz) {    // (Nz, Nx+1)
+    AT(rhoUoo, j, i) = AT(rhoUo, j, i);
+    AT(rhoUo, j, i) = AT(rhou, j, i) * AT(U, j + 1, i);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+int update_impl(xc_ctx* c) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  const xc_params& p = c->p;
+  cudaStream_t s = c->stream;
+  dim3 blk(32, 8);
+  Rheo r{p.AA[0], p.AA[1], p.AA[2], p.AA[3], p.BB[0], p.BB[1], p.BB[2], p.BB[3],
+         1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0};
+  volfrac_rheology_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
+      Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
+      F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix));
+  XC_LAUNCH_CHECK();
+  interp_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, s>>>(
+      Nz, Nx, p.xBC, p.zBC, p.rhom0, p.rhox0, CF(c, FLD_rho), CF(c, FLD_chi), CF(c, FLD_mu),
+      CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rhow), F(c, FLD_rhou), F(c, FLD_Drhom),
+      F(c, FLD_Drhox), F(c, FLD_chiw), F(c, FLD_muw), F(c, FLD_chiu), F(c, FLD_muu),
+      F(c, FLD_x_w), F(c, FLD_m_w), F(c, FLD_x_u), F(c, FLD_m_u));
+  XC_LAUNCH_CHECK();
+  double* rhoref = c->tmp[6];
+  double* plcol = c->tmp[6] + (Nz + 8);
+  rowmean_scan_kernel<<<1, 1024, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), p.g0, p.h, p.Ptop, rhoref, plcol);
+  XC_LAUNCH_CHECK();
+  drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, s>>>(
+      Nz, Nx, p.Ptop, rhoref, plcol, CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
+      F(c, FLD_Pt));
+  XC_LAUNCH_CHECK();
+  const double invh = 1.0 / p.h;
+  kinematics_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
+      Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
+      F(c, FLD_exx), F(c, FLD_ezz), F(c, FLD_Div_V), F(c, FLD_eII), F(c, FLD_V), F(c, FLD_vx),
+      F(c, FLD_vm));
+  XC_LAUNCH_CHECK();
+  DView etai{c->tmp[0], Nz}, etasi{c->tmp[1], Nz};
+  viscblend_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
+      Nz, Nx, p.L0, CF(c, FLD_etamix), CF(c, FLD_eII), CF(c, FLD_rho), CF(c, FLD_V), etai,
+      F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL));
+  XC_LAUNCH_CHECK();
+  XC_TRY(reduce_view(c, RED_MIN, CView{etai.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETA));
+  blend_segvisc_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
+      Nz, Nx, c->dscal + SC_EMAX_ETA, p.etacntr, p.D0, p.l0, CView{etai.p, Nz}, F(c, FLD_eta),
+      CF(c, FLD_V), CF(c, FLD_rho), F(c, FLD_ReD), CF(c, FLD_vx), CF(c, FLD_etamix),
+      CF(c, FLD_ke), CF(c, FLD_fReL), F(c, FLD_Rel), F(c, FLD_fRel), F(c, FLD_ks),
+      F(c, FLD_etat), etasi, F(c, FLD_kx), F(c, FLD_Rc));
+  XC_LAUNCH_CHECK();
+  XC_TRY(reduce_view(c, RED_MIN, CView{etasi.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETAS));
+  etas_blend_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
+      Nz, Nx, c->dscal + SC_EMAX_ETAS, p.etacntr, p.d0, CView{etasi.p, Nz}, F(c, FLD_etas),
+      CF(c, FLD_vx), CF(c, FLD_rho), F(c, FLD_Red));
+  XC_LAUNCH_CHECK();
+  corner_eta_etasw_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
+      Nz, Nx, p.zBC, CF(c, FLD_eta), F(c, FLD_etaco), CF(c, FLD_etas), F(c, FLD_etasw));
+  XC_LAUNCH_CHECK();
+  stress_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
+      Nz, Nx, p.D0, CF(c, FLD_etaco), CF(c, FLD_exz), F(c, FLD_txz), CF(c, FLD_eta),
+      CF(c, FLD_exx), CF(c, FLD_ezz), F(c, FLD_txx), F(c, FLD_tzz), F(c, FLD_tII), CF(c, FLD_V),
+      CF(c, FLD_kx), F(c, FLD_Ra));
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+int phase_velocities_impl(xc_ctx* c) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  dim3 blk(32, 8);
+  phase_velocities_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, c->stream>>>(
+      Nz, Nx, c->p.xBC, c->p.zBC, c->p.d0, c->p.g0, CF(c, FLD_etasw), CF(c, FLD_Drhox),
+      CF(c, FLD_bndtaperw), CF(c, FLD_x_w), CF(c, FLD_m_w), CF(c, FLD_x_u), CF(c, FLD_m_u),
+      CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_xisw), CF(c, FLD_xixw), CF(c, FLD_xiew),
+      CF(c, FLD_xisu), CF(c, FLD_xixu), CF(c, FLD_xieu), F(c, FLD_wx), F(c, FLD_wm),
+      F(c, FLD_Wx), F(c, FLD_Wm), F(c, FLD_Ux), F(c, FLD_Um));
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+int store_previous_impl(xc_ctx* c) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  dim3 blk(32, 8);
+  store_previous_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, c->stream>>>(
+      Nz, Nx, F(c, FLD_X), F(c, FLD_Xo), F(c, FLD_Xoo), F(c, FLD_M), F(c, FLD_Mo), F(c, FLD_Moo),
+      F(c, FLD_dXdt), F(c, FLD_dXdto), F(c, FLD_dXdtoo), F(c, FLD_rho), F(c, FLD_rhoo),
+      F(c, FLD_rhooo), F(c, FLD_drhodt), F(c, FLD_drhodto), F(c, FLD_drhodtoo), CF(c, FLD_rhow),
+      CF(c, FLD_W), F(c, FLD_rhoWo), F(c, FLD_rhoWoo), CF(c, FLD_rhou), CF(c, FLD_U),
+      F(c, FLD_rhoUo), F(c, FLD_rhoUoo));
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+static int copy_field(xc_ctx* c, int dst, int src) {
+  size_t n = (size_t)c->shape[src].rows * c->shape[src].cols * c->elem[src];
+  XC_CUDA_TRY(cudaMemcpyAsync(c->field[dst], c->field[src], n, cudaMemcpyDeviceToDevice, c->stream));
+  return XC_OK;
+}
+
+int store_noise_impl(xc_ctx* c) {
+  XC_TRY(copy_field(c, FLD_psieo, FLD_psie));
+  XC_TRY(copy_field(c, FLD_psixo, FLD_psix));
+  return copy_field(c, FLD_psiso, FLD_psis);
+}
+
+int snapshot_impl(xc_ctx* c) {
+  XC_TRY(copy_field(c, FLD_res_Wo, FLD_W));
+  XC_TRY(copy_field(c, FLD_res_Uo, FLD_U));
+  XC_TRY(copy_field(c, FLD_res_Po, FLD_P));
+  XC_TRY(copy_field(c, FLD_res_Xo, FLD_X));
+  return copy_field(c, FLD_res_MFSo, FLD_MFS);
+}
+
+static inline CView whole(xc_ctx* c, int id) { return CF(c, id); }
+static const CView kNone{nullptr, 0};
+
+int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  XC_TRY(reduce_view(c, RED_MAX, whole(c, FLD_kx), kNone, Nz, Nx, SC_DT + 0));
+  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Wx), kNone, Nz + 1, Nx + 2, SC_DT + 1));
+  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Wm), kNone, Nz + 1, Nx + 2, SC_DT + 2));
+  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Ux), kNone, Nz + 2, Nx + 1, SC_DT + 3));
+  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Um), kNone, Nz + 2, Nx + 1, SC_DT + 4));
+  XC_TRY(fetch_scalars(c, SC_DT, 5));
+  const double* m = c->hscal + SC_DT;
+  const double h = c->p.h;
+  double dtk = (h / 2.0) * (h / 2.0) / m[0];
+  double vmax = std::fmax(std::fmax(std::fmax(m[1], m[2]), m[3]), m[4]) + XC_EPS;
+  double dta = (h / 2.0) / vmax;
+  *dt_out = std::fmin(std::fmin(1.5 * dt_prev, std::fmin(dtk, c->p.CFL * dta)), c->p.dtmax);
+  return XC_OK;
+}
+
+int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  const int b = SC_RESNORM;
+  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_rho), kNone, Nz, Nx, b + 0));
+  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_X), whole(c, FLD_res_Xo), Nz, Nx, b + 1));
+  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_MFS), whole(c, FLD_res_MFSo), Nz, Nx, b + 2));
+  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_W), whole(c, FLD_res_Wo), Nz + 1, Nx + 2, b + 3));
+  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_W), kNone, Nz + 1, Nx + 2, b + 4));
+  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_U), whole(c, FLD_res_Uo), Nz + 2, Nx + 1, b + 5));
+  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_U), kNone, Nz + 2, Nx + 1, b + 6));
+  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_P), whole(c, FLD_res_Po), Nz + 2, Nx + 2, b + 7));
+  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_P), kNone, Nz + 2, Nx + 2, b + 8));
+  XC_TRY(fetch_scalars(c, b, 9));
+  const double* q = c->hscal + b;
+  const double ep = XC_EPS;
+  double nrho = std::sqrt(q[0]);
+  double res_mass = std::sqrt(q[1]) / (nrho + ep) + std::sqrt(q[2]) / (nrho / dt + ep);
+  double res_mmnt = (std::sqrt(q[3]) / (std::sqrt(q[4]) + ep) + std::sqrt(q[5]) / (std::sqrt(q[6]) + ep)) +
+                    std::sqrt(q[7]) / (std::sqrt(q[8]) + ep);
+  out[0] = res_mass + res_mmnt;
+  out[1] = res_mass;
+  out[2] = res_mmnt;
+  return XC_OK;
+}
+
+int sums_impl(xc_ctx* c, double out[12]) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  const int b = SC_SUMS;
+  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_rho), kNone, Nz, Nx, b + 0));
+  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_M), kNone, Nz, Nx, b + 1));
+  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_X), kNone, Nz, Nx, b + 2));
+  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_Gx), kNone, Nz, Nx, b + 3));
+  const int fl[4] = {FLD_qz_advn_X, FLD_qz_advn_M, FLD_qz_dffn_X, FLD_qz_dffn_M};
+  for (int k = 0; k < 4; ++k) {
+    CView q = CF(c, fl[k]);
+    CView top{q.p + q.ld, q.ld};                 // row 0, columns 1..Nx
+    CView bot{q.p + q.ld + Nz, q.ld};            // row Nz, columns 1..Nx
+    XC_TRY(reduce_view(c, RED_SUM, top, kNone, 1, Nx, b + 4 + 2 * k));
+    XC_TRY(reduce_view(c, RED_SUM, bot, kNone, 1, Nx, b + 5 + 2 * k));
+  }
+  XC_TRY(fetch_scalars(c, b, 12));
+  const double* q = c->hscal + b;
+  const double h = c->p.h, h2 = h * h;
+  out[0] = q[0] * h2 + XC_EPS;
+  out[1] = q[1] * h2 + XC_EPS;
+  out[2] = q[2] * h2 + XC_EPS;
+  out[3] = q[3] * h2;
+  for (int k = 4; k < 12; ++k) out[k] = q[k] * h;
+  return XC_OK;
+}
