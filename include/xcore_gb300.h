@@ -224,6 +224,23 @@ int xc_diffus_with_flux(double* dff, double* qx, double* qz, const double* f_hal
 /* time_coefs(Float64, TINT, step) -> (a1, a2, a3, b1, b2, b3)    src/timing.jl:18-36 */
 int xc_time_coefs(int tint, int step, double out[6]);
 
+/* ------------------------------------------------------------------ */
+/* instrumentation (no counterpart in the reference)                   */
+/* ------------------------------------------------------------------ */
+/* The context's CUDA stream (cudaStream_t), for events recorded by a caller. */
+void* xc_stream(xc_ctx* ctx);
+/* Kernels launched by this library since load (host-side count). */
+long long xc_launch_count(void);
+/* Time one kernel of the path on the context's current state with CUDA
+   events on the context stream: `iters` back-to-back launches after one
+   warm-up launch.  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
+   1 FP64 Stokes operator apply, 2 FP32 velocity Jacobi sweep (finest level),
+   3 FP64 velocity Jacobi sweep, 4 FFT line filter (z pass of psie),
+   5 volume fractions + rheology.  out = {ms per launch, algorithmic bytes per
+   launch, algorithmic flops per launch, units per launch}.  Kernels 1-3 need
+   a previous xc_fluidmech call (2 needs the mixed solver). */
+int xc_bench_kernel(xc_ctx* ctx, int which, int iters, double out[4]);
+
 /* Last error message of the calling thread ("" when none). */
 const char* xc_last_error(void);
 /* Library version string. */

@@ -1,0 +1,98 @@
+"""GPU Stokes solve (fluidmech!) against the oracle's sparse-LU solution.
+
+The reference factorises the scaled saddle system with UMFPACK; the oracle uses
+SuperLU on the identically assembled system.  The GPU solves the same system
+matrix-free with FGMRES + multigrid.  Tolerances: FP64 FGMRES to relative
+residual 1e-10 must give W, U, P within 1e-8 (max-norm, relative to the field's
+max) of the LU solution; the mixed FP32/FP64 solver to 1e-9 within 1e-7."""
+import math
+
+import numpy as np
+import pytest
+
+import xcore_oracle as O
+from gpu_helpers import assert_fields, device_state, realistic_state, rel_err
+from mms import mms_sources
+
+pytestmark = pytest.mark.gpu
+pytest.importorskip("torch")
+import xcore_gb300 as xc  # noqa: E402
+
+
+def _maxrel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("shape", [(32, 32), (40, 24)])
+@pytest.mark.parametrize("solver,rtol,tol", [("fgmres64", 1e-10, 1e-8), ("mixed", 1e-9, 1e-7)])
+def test_fluidmech_matches_lu(shape, solver, rtol, tol):
+    par, g, sc, ns, st, dt, rng = realistic_state(N=shape[0], Nx=shape[1], steps=2)
+    ds = device_state(par, g, sc, st)
+    coefs = O.time_coefs("bd2im", 3)
+    O.fluidmech(st, g, par, coefs, dt)
+    info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol)
+    assert info["converged"] and info["rel_residual"] <= rtol, info
+    for k in ("W", "U", "P"):
+        e = _maxrel(ds[k], getattr(st, k))
+        assert e <= tol, (k, e, info)
+    assert_fields(ds, st, ["MFS", "drhodt"], exact=True)
+
+
+def _mms_device(N):
+    m = mms_sources(N, 10.0)
+    # x0 only feeds the host-side scales, which the Stokes solve does not read
+    par = O.Params(D=10.0, N=N, L=10.0, etam0=1e3, g0=10.0, rhom0=2700, rhox0=3200, d0=1e-2, Da=0.0, Xi=0.0,
+                   gamma=0.0, x0=0.1)
+    g = O.make_grid(par)
+    sc = O.compute_scales(par, g)
+    s = xc.State(xc.Parameters(**{k: getattr(par, k) for k in xc.Parameters.__dataclass_fields__ if hasattr(par, k)}),
+                 grid=xc.Grid(Nx=g.Nx, Nz=g.Nz, h=g.h, D=g.D, L=g.L), scales=sc, sds=-1, top_cnv=-1, bot_cnv=-1)
+    for k in ("eta", "etaco", "rho", "rhow", "rhou", "Drho", "MFS"):
+        s[k] = m[k]
+    return par, g, s, m
+
+
+def test_mms_convergence_gpu():
+    """test/test_mms.jl:4-71 through the GPU solver: order > 1.8 for W, U, P,
+    and the same solution as the sparse LU (fluidmech.jl MMS branch)."""
+    errs = {"W": [], "U": [], "P": []}
+    for N in (32, 64, 128):
+        par, g, s, m = _mms_device(N)
+        info = s.fluidmech((1.0, 1.0, 0.0, 1.0, 0.0, 0.0), 1e32, rtol=1e-11, maxit=2000, mms=m)
+        assert info["converged"], info
+        for k in errs:
+            errs[k].append(np.linalg.norm(s[k] - m[k + "_exact"]) / np.linalg.norm(m[k + "_exact"]))
+        if N == 32:
+            st = O.State(g.Nz, g.Nx)
+            for k in ("eta", "etaco", "rho", "rhow", "rhou", "Drho", "MFS"):
+                setattr(st, k, m[k].copy())
+            bn = O.Bnchm(m["src_W"], m["src_U"], m["src_P"], m["W_exact"], m["U_exact"], m["P_exact"])
+            O.fluidmech(st, g, par, (1.0, 1.0, 0.0, 1.0, 0.0, 0.0), 1e32, bn=bn, sds=-1, top_cnv=-1, bot_cnv=-1)
+            for k in ("W", "U", "P"):
+                assert _maxrel(s[k], getattr(st, k)) <= 1e-8, k
+    for k, e in errs.items():
+        assert math.log2(e[0] / e[1]) > 1.8, (k, e)
+        assert math.log2(e[1] / e[2]) > 1.8, (k, e)
+
+
+def test_step_matches_oracle():
+    """One outer step of run! (3 Picard sweeps) on the GPU vs the oracle."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=32, Nx=32, steps=1)
+    ds = device_state(par, g, sc, st)
+    ds.snapshot()
+    re, rs = rng.standard_normal((g.Nz, g.Nx)), rng.standard_normal((g.Nz, g.Nx))
+    dt_o, norms = O.timestep(st, g, par, sc, ns, 2, dt, re, rs)
+    info = ds.step(2, dt, re, rs, sweeps=3, rtol=1e-11)
+    assert info["dt_next"] == pytest.approx(dt_o, rel=1e-8)
+    np.testing.assert_allclose(info["resnorm"], [n[0] for n in norms], rtol=1e-5)
+    for k in ("X", "x", "M", "W", "U", "P", "eta", "MFS", "psie", "xie", "Wx", "kx"):
+        assert rel_err(ds[k], getattr(st, k)) <= 1e-8, (k, rel_err(ds[k], getattr(st, k)))
+
+
+def test_not_converged_is_reported():
+    """An iteration cap that cannot be met returns XC_NOT_CONVERGED (the
+    solve's failure is detected on the host, no device fault involved)."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=32, Nx=32, steps=1)
+    ds = device_state(par, g, sc, st)
+    with pytest.raises(xc.NotConverged):
+        ds.fluidmech(O.time_coefs("bd2im", 2), dt, rtol=1e-14, maxit=2)

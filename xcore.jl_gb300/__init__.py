@@ -128,6 +128,9 @@ def lib():
             "xc_diffus": (ip, [vp, vp, vp, ip, ip, dp, vp]),
             "xc_diffus_with_flux": (ip, [vp, vp, vp, vp, vp, ip, ip, dp, ip, ip, vp]),
             "xc_time_coefs": (ip, [ip, ip, D6]),
+            "xc_stream": (vp, [vp]),
+            "xc_launch_count": (ctypes.c_longlong, []),
+            "xc_bench_kernel": (ip, [vp, ip, ip, D6]),
             "xc_last_error": (ctypes.c_char_p, []),
             "xc_version": (ctypes.c_char_p, []),
         }
@@ -332,6 +335,18 @@ class State:
     def synchronize(self):
         _check(lib().xc_synchronize(self._h))
 
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t (for events recorded by the caller)."""
+        return lib().xc_stream(self._h)
+
+    def bench_kernel(self, which: int, iters: int = 20):
+        """CUDA-event timing of one kernel on the current state:
+        (ms per launch, algorithmic bytes, algorithmic flops, units)."""
+        out = (ctypes.c_double * 4)()
+        _check(lib().xc_bench_kernel(self._h, int(which), int(iters), out))
+        return tuple(out)
+
+
     # -- the reference's functions ------------------------------------------
     def store_previous(self):
         """store_previous!(fluid, phase) -- src/store.jl:13-30."""
@@ -489,3 +504,8 @@ def diffus_with_flux(dff, qx, qz, f_halo, k_halo, h, xBC="periodic", zBC="closed
     Nx, Nz = dff.shape
     _check(lib().xc_diffus_with_flux(_ptr(dff), _ptr(qx), _ptr(qz), _ptr(f_halo), _ptr(k_halo), Nz, Nx,
                                      float(h), BCS[xBC], BCS[zBC], _stream(stream)))
+
+
+def launch_count() -> int:
+    """Kernels launched by the library since it was loaded."""
+    return int(lib().xc_launch_count())

@@ -302,7 +302,7 @@ extern "C" int xc_initialize(xc_ctx* c, const double* x_init, const double* re, 
   const int n = Nz * Nx;
   seed_phase_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(
       n, (const double*)c->field[FLD_rho], (const double*)c->field[FLD_x],
-      (const double*)c->field[FLD_m], (double*)c->field[FLD_X], (double*)c->field[FLD_M]);
+      (const double*)c->field[FLD_m], (double*)c->field[FLD_X], (double*)c->field[FLD_M]); xc_count_launch();
   XC_LAUNCH_CHECK();
   XC_TRY(noise_impl(c, p.dt0, 1, re, rs));
   XC_TRY(phase_velocities_impl(c));
@@ -352,5 +352,51 @@ extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double*
   local.sweeps = sweeps;
   XC_TRY(update_dt_impl(c, dt, &local.dt_next));
   if (stats) *stats = local;
+  return XC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// instrumentation
+// ---------------------------------------------------------------------------
+long long g_xc_launches = 0;
+
+extern "C" void* xc_stream(xc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+extern "C" long long xc_launch_count(void) { return g_xc_launches; }
+
+int noise_bench_zpass(xc_ctx* c, int iters, double out[4]);
+
+extern "C" int xc_bench_kernel(xc_ctx* c, int which, int iters, double out[4]) {
+  XC_TRY(check_ctx(c));
+  if (!out || iters < 1) { xc_set_error("xc_bench_kernel: bad arguments"); return XC_BAD_ARG; }
+  if (which == 1 || which == 2 || which == 3) return stokes_bench(c, which, iters, out);
+  if (which == 4) return noise_bench_zpass(c, iters, out);
+  if (which != 0) { xc_set_error("xc_bench_kernel: unknown kernel %d", which); return XC_BAD_ARG; }
+  const int Nz = c->Nz, Nx = c->Nx;
+  DView Wx = F(c, FLD_Wx), Ux = F(c, FLD_Ux), X = F(c, FLD_X);
+  CView Wx_face{Wx.p + Wx.ld, Wx.ld}, Ux_face{Ux.p + 1, Ux.ld};
+  DView qx = F(c, FLD_qx_advn_X), qz = F(c, FLD_qz_advn_X);
+  DView qxi{qx.p + 1, qx.ld}, qzi{qz.p + qz.ld, qz.ld};
+  cudaEvent_t e0, e1;
+  XC_CUDA_TRY(cudaEventCreate(&e0));
+  XC_CUDA_TRY(cudaEventCreate(&e1));
+  int st = XC_OK;
+  for (int it = -1; it < iters && st == XC_OK; ++it) {
+    if (it == 0) cudaEventRecord(e0, c->stream);
+    st = stencil_advect_flux(X.p, X.ld, false, Nz, Nx, c->p.ADVN, c->p.xBC, c->p.zBC, Ux_face, Wx_face, c->p.h,
+                             F(c, FLD_advn_X), qxi, qzi, c->stream);
+  }
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != XC_OK) return st;
+  const double cells = (double)Nz * Nx;
+  const double fpc = c->p.ADVN == XC_WENO5 ? 282.0 : (c->p.ADVN == XC_QUICK ? 38.0 : 20.0);
+  out[0] = ms / iters;
+  out[1] = 48.0 * cells;     // read f, u, w; write adv, qx, qz (8 B each per cell)
+  out[2] = fpc * cells;
+  out[3] = cells;
   return XC_OK;
 }

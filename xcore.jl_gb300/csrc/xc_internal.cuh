@@ -93,6 +93,10 @@ void xc_set_error(const char* fmt, ...);
 
 #define XC_LAUNCH_CHECK() XC_CUDA_TRY(cudaGetLastError())
 
+// number of kernels this library has launched (host side, process-wide)
+extern long long g_xc_launches;
+inline void xc_count_launch() { ++g_xc_launches; }
+
 #define XC_TRY(expr)               \
   do {                             \
     int s_ = (expr);               \
@@ -208,6 +212,7 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
 int stokes_create(xc_ctx* c);
 void stokes_destroy(xc_ctx* c);
 struct MmsData { const double *src_W, *src_U, *src_P, *W_exact, *U_exact, *P_exact; };
+int stokes_bench(xc_ctx* c, int which, int iters, double out[4]);
 int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_opts* opts,
                    xc_solver_stats* stats, const MmsData* mms);
 

@@ -226,7 +226,7 @@ int run_line_filter(const LineFilter& lf, CView in, DView out, int rows, int col
     XC_CUDA_TRY(cudaFuncSetAttribute(line_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int threads = lf.M * P >= 1024 ? 512 : 256;
   line_filter_kernel<<<(npairs + P - 1) / P, threads, smem, s>>>(in, out, rows, cols, axis, lf.M,
-                                                                 lf.logM, lf.khat, lf.tw, P);
+                                                                 lf.logM, lf.khat, lf.tw, P); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -371,7 +371,7 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
       Nz, Nx, p.Xi, p.L0h, p.l0h, p.txi0, dt, np->fL, np->fl, CF(c, FLD_V), CF(c, FLD_vx),
       CF(c, FLD_fReL), CF(c, FLD_ke), CF(c, FLD_chi), CF(c, FLD_ks), CF(c, FLD_psieo),
       CF(c, FLD_psixo), CF(c, FLD_psiso), CF(c, FLD_re), CF(c, FLD_rs), F(c, FLD_psie),
-      F(c, FLD_psix), F(c, FLD_psis));
+      F(c, FLD_psix), F(c, FLD_psis)); xc_count_launch();
   XC_LAUNCH_CHECK();
   // filtered fields in tmp[2..4], z-pass intermediate in tmp[5]
   DView flt[3] = {DView{c->tmp[2], Nz}, DView{c->tmp[3], Nz}, DView{c->tmp[4], Nz}};
@@ -390,16 +390,43 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
     XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 2, s, n));
     XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, st + 4 * q + 2, Nz, Nx, st + 4 * q + 3, s));
   }
-  rescale_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(Nz, Nx, flt[0], flt[1], flt[2], st);
+  rescale_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(Nz, Nx, flt[0], flt[1], flt[2], st); xc_count_launch();
   XC_LAUNCH_CHECK();
   stagger_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, s>>>(
       Nz, Nx, CView{flt[0].p, Nz}, CView{flt[1].p, Nz}, CView{flt[2].p, Nz}, CF(c, FLD_chiw),
       CF(c, FLD_muw), CF(c, FLD_chiu), CF(c, FLD_muu), F(c, FLD_xieu), F(c, FLD_xiew),
-      F(c, FLD_xixu), F(c, FLD_xixw), F(c, FLD_xisu), F(c, FLD_xisw));
+      F(c, FLD_xixu), F(c, FLD_xixw), F(c, FLD_xisu), F(c, FLD_xisw)); xc_count_launch();
   XC_LAUNCH_CHECK();
   speeds_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
       Nz, Nx, CF(c, FLD_xisw), CF(c, FLD_xisu), CF(c, FLD_xixw), CF(c, FLD_xixu), CF(c, FLD_xiew),
-      CF(c, FLD_xieu), F(c, FLD_xis), F(c, FLD_xix), F(c, FLD_xie));
+      CF(c, FLD_xieu), F(c, FLD_xis), F(c, FLD_xix), F(c, FLD_xie)); xc_count_launch();
   XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+// time the FFT line filter (z pass of psie) with CUDA events on the context stream
+int noise_bench_zpass(xc_ctx* c, int iters, double out[4]) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  NoisePlan* np = c->noise;
+  cudaEvent_t e0, e1;
+  XC_CUDA_TRY(cudaEventCreate(&e0));
+  XC_CUDA_TRY(cudaEventCreate(&e1));
+  int st = XC_OK;
+  for (int it = -1; it < iters && st == XC_OK; ++it) {
+    if (it == 0) cudaEventRecord(e0, c->stream);
+    st = run_line_filter(np->ze, CF(c, FLD_psie), DView{c->tmp[5], Nz}, Nz, Nx, 0, c->stream);
+  }
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != XC_OK) return st;
+  const double M = np->ze.M, logM = np->ze.logM;
+  out[0] = ms / iters;
+  out[1] = 16.0 * Nz * (double)Nx;                   // read psi, write the filtered field
+  out[2] = (double)((Nx + 1) / 2) * 2.0 * 5.0 * M * logM;   // forward + inverse complex FFT per line pair
+  out[3] = (double)Nz * Nx;
   return XC_OK;
 }

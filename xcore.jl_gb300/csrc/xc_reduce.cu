@@ -78,9 +78,9 @@ int reduce_to(xc_ctx* c, int op, CView a, CView b, const double* center, int row
               double* out, cudaStream_t s, double divisor) {
   int combine_op = (op == RED_SUMSQ || op == RED_SUMSQDIFF) ? RED_SUM : op;
   if (center) combine_op = RED_SUM;
-  partial_kernel<<<RG, RB, 0, s>>>(op, a, b, center, rows, cols, c->red_partials);
+  partial_kernel<<<RG, RB, 0, s>>>(op, a, b, center, rows, cols, c->red_partials); xc_count_launch();
   XC_LAUNCH_CHECK();
-  final_kernel<<<1, RB, 0, s>>>(combine_op, c->red_partials, RG, out, divisor);
+  final_kernel<<<1, RB, 0, s>>>(combine_op, c->red_partials, RG, out, divisor); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }

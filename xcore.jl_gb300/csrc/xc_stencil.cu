@@ -364,10 +364,11 @@ int launch_advect(const double* f, int ldf, bool halod, int Nz, int Nx, int xBC,
                   CView w, double invh, DView adv, DView qx, DView qz, cudaStream_t s) {
   // the last tile of each axis also writes the closing face (index Nz / Nx)
   dim3 grid((Nz + TZ - 1) / TZ, (Nx + TX - 1) / TX);
-  if (halod)
-    advect_tile_kernel<S, true><<<grid, NT, 0, s>>>(f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz);
-  else
-    advect_tile_kernel<S, false><<<grid, NT, 0, s>>>(f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz);
+  if (halod) {
+    advect_tile_kernel<S, true><<<grid, NT, 0, s>>>(f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz); xc_count_launch();
+  } else {
+    advect_tile_kernel<S, false><<<grid, NT, 0, s>>>(f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz); xc_count_launch();
+  }
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -409,10 +410,11 @@ static int diffus_launch(const double* f, const double* k1, const double* k2, in
                          cudaStream_t s) {
   dim3 grid((Nz + TZ - 1) / TZ, (Nx + TX - 1) / TX);
   double invh = 1.0 / h;
-  if (halod)
-    diffus_tile_kernel<true><<<grid, NT, 0, s>>>(f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz);
-  else
-    diffus_tile_kernel<false><<<grid, NT, 0, s>>>(f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz);
+  if (halod) {
+    diffus_tile_kernel<true><<<grid, NT, 0, s>>>(f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz); xc_count_launch();
+  } else {
+    diffus_tile_kernel<false><<<grid, NT, 0, s>>>(f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz); xc_count_launch();
+  }
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -425,7 +427,7 @@ int stencil_diffus_flux(const double* f, const double* k, int ld, bool halod, in
 
 int pad_face_fluxes(DView qx, DView qz, int Nz, int Nx, int xBC, int zBC, cudaStream_t s) {
   int n = (Nz > Nx ? Nz : Nx) + 1;
-  pad_fluxes_kernel<<<(n + 255) / 256, 256, 0, s>>>(qx, qz, Nz, Nx, xBC, zBC);
+  pad_fluxes_kernel<<<(n + 255) / 256, 256, 0, s>>>(qx, qz, Nz, Nx, xBC, zBC); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -457,7 +459,7 @@ int phsevo_impl(xc_ctx* c, int scheme, const double coefs[6], double dt, double 
       Nz, Nx, coefs[0], coefs[1], coefs[2], coefs[3], coefs[4], coefs[5], dt, alpha, c->p.G0,
       X, CF(c, FLD_Xo), CF(c, FLD_Xoo), M, F(c, FLD_x), F(c, FLD_m), CF(c, FLD_rho),
       CF(c, FLD_advn_X), CF(c, FLD_advn_M), F(c, FLD_advn_rho), CF(c, FLD_dffn_X),
-      CF(c, FLD_bndshape), F(c, FLD_Gx), F(c, FLD_dXdt), CF(c, FLD_dXdto), CF(c, FLD_dXdtoo));
+      CF(c, FLD_bndshape), F(c, FLD_Gx), F(c, FLD_dXdt), CF(c, FLD_dXdto), CF(c, FLD_dXdtoo)); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -473,7 +475,7 @@ extern "C" int xc_fill_ghosts(double* f, int Nz, int Nx, int halo, int zBC, int 
     return XC_BAD_ARG;
   }
   long long n = (long long)(Nz + 2 * halo) * (Nx + 2 * halo);
-  fill_ghosts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(f, Nz, Nx, halo, zBC, xBC);
+  fill_ghosts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(f, Nz, Nx, halo, zBC, xBC); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }

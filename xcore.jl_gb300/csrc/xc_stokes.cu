@@ -1,13 +1,1537 @@
-// Stokes saddle-point solve of fluidmech! (placeholder until the solver lands).
+// fluidmech! on the GPU: the staggered-grid Stokes saddle-point system of
+// src/fluidmech.jl:71-534, solved matrix-free.
+//
+// The reference assembles LL = [KV GG; DM KP] from triplets, scales it with
+// scl = 1/(sqrt|diag LL| + [0; sqrt(eta/rho)]) and factorises SCL*LL*SCL with
+// UMFPACK; one call is mathematically SOL <- LL^{-1} RR.  Here the same LL
+// (every row of fluidmech.jl:145-488, incl. the periodic W ghost columns, the
+// top/bottom U rows, the P ghost ring and the pressure pin) is applied as a
+// stencil, the right-hand side RR (fluidmech.jl:111-127, 236-246, 310-323,
+// 446-459, with the WENO5/QUICK momentum advection of the current W, U) is
+// assembled on the device, and the scaled system is solved by FGMRES with a
+// block upper-triangular preconditioner
+//     [A  B]^-1            z_p = S~^-1 r_p,   z_v = A~^-1 (r_v - B z_p)
+//     [0  S]
+// where A~^-1 is one V-cycle of a geometric multigrid for the velocity block
+// (re-discretised coarse operators from averaged eta / etaco / rho, damped
+// Jacobi smoothing, bilinear transfers) and S~^-1 one V-cycle of a
+// cell-centred multigrid for S = -DM diag(A)^-1 GG, a variable-coefficient
+// pressure Laplacian with the pin (plus an optional eta/rho mass term).
+// Mixed precision: the same Krylov/multigrid machinery in FP32 inside FP64
+// iterative refinement on the FP64 residual.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "xc_internal.cuh"
 
-struct StokesWork { int dummy; };
+namespace {
 
-int stokes_create(xc_ctx* c) { c->stokes = nullptr; return XC_OK; }
-void stokes_destroy(xc_ctx* c) { c->stokes = nullptr; }
+constexpr int kMaxLevels = 12;
+constexpr int kMaxRestart = 64;
+
+struct Geo {          // one grid level
+  int Nz, Nx, NW, NU, NP;
+  double h, invh;
+};
+
+Geo make_geo(int Nz, int Nx, double h) {
+  Geo g;
+  g.Nz = Nz; g.Nx = Nx; g.h = h; g.invh = 1.0 / h;
+  g.NW = (Nz + 1) * (Nx + 2);
+  g.NU = (Nz + 2) * (Nx + 1);
+  g.NP = (Nz + 2) * (Nx + 2);
+  return g;
+}
+
+// row-local scalars of the operator
+struct OpConst {
+  double a1, gamma, dt, g0;
+  int sds, top_cnv, bot_cnv;
+  int sailor;          // 0 in MMS mode (fluidmech.jl:218, 293)
+  int pin_p;           // flat P index (0..NP-1) of the pressure pin
+  int mms;             // 1: MMS pins (P row and U row are identity rows)
+  int pin_u;           // flat U index of the MMS velocity pin
+};
+
+__device__ __forceinline__ int icxp(int i, int Nx) { return i == 0 ? Nx - 1 : (i == Nx + 1 ? 0 : i - 1); }
+
+// ---------------------------------------------------------------------------
+// coefficient planes of the velocity block (physical, unscaled), one level.
+// W row planes: 0 diag, 1 W(j-1,i), 2 W(j+1,i), 3 W(j,i-1), 4 W(j,i+1),
+//               5 U(j,i-1), 6 U(j+1,i-1), 7 U(j,i), 8 U(j+1,i)
+// U row planes: 0 diag, 1 U(j,il), 2 U(j,ir), 3 U(j-1,i), 4 U(j+1,i),
+//               5 W(j-1,i), 6 W(j-1,i+1), 7 W(j,i), 8 W(j,i+1)
+// Also the inertia(+drunken-sailor) part of the diagonal in plane 9.
+// (fluidmech.jl:194-233, 270-307)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta,
+                                const double* __restrict__ etaco, const double* __restrict__ rho,
+                                const double* __restrict__ rhow, const double* __restrict__ rhou,
+                                T* cw, T* cu) {
+  const int Nz = g.Nz, Nx = g.Nx;
+  const double invh = g.invh, invh2 = invh * invh;
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const double c23 = 2.0 / 3.0, c13 = 1.0 / 3.0;
+  if (t < g.NW) {
+    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    double c[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (i == 0 || i == Nx + 1 || j == 0) {
+      c[0] = 1.0;
+    } else if (j == Nz) {
+      c[0] = rhow[(size_t)(i - 1) * (Nz + 1) + Nz] * invh;
+    } else {
+      double C1 = etaco[(size_t)(i - 1) * (Nz + 1) + j], C2 = etaco[(size_t)i * (Nz + 1) + j];
+      double P1 = eta[(size_t)(i - 1) * Nz + (j - 1)], P2 = eta[(size_t)(i - 1) * Nz + j];
+      double iner = k.a1 * rhow[(size_t)(i - 1) * (Nz + 1) + j] / k.dt;
+      double d = iner + (c23 * (P1 + P2) * invh2 + 0.5 * (C1 + C2) * invh2);
+      double sail = 0.0;
+      if (k.sailor) {
+        double dz = (rho[(size_t)(i - 1) * Nz + j] - rho[(size_t)(i - 1) * Nz + j - 1]) * invh;
+        sail = dz * k.g0 * k.dt;
+        d = d + sail;
+      }
+      c[0] = d;
+      c[1] = -c23 * P1 * invh2;
+      c[2] = -c23 * P2 * invh2;
+      c[3] = -0.5 * C1 * invh2;
+      c[4] = -0.5 * C2 * invh2;
+      c[5] = -(0.5 * C1 - c13 * P1) * invh2;
+      c[6] = +(0.5 * C1 - c13 * P2) * invh2;
+      c[7] = +(0.5 * C2 - c13 * P1) * invh2;
+      c[8] = -(0.5 * C2 - c13 * P2) * invh2;
+      c[9] = iner + sail;
+    }
+    for (int q = 0; q < 10; ++q) cw[(size_t)q * g.NW + t] = (T)c[q];
+    return;
+  }
+  t -= g.NW;
+  if (t < g.NU) {
+    int j = (int)(t % (Nz + 2)), i = (int)(t / (Nz + 2));
+    double c[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (j == 0 || j == Nz + 1 || (k.mms && (int)t == k.pin_u)) {
+      c[0] = 1.0;
+    } else {
+      int ia = (i == 0) ? Nx - 1 : i - 1;       // icx[i]
+      int ib = (i == Nx) ? 0 : i;               // icx[i+1]
+      double C1 = etaco[(size_t)i * (Nz + 1) + j - 1], C2 = etaco[(size_t)i * (Nz + 1) + j];
+      double P1 = eta[(size_t)ia * Nz + j - 1], P2 = eta[(size_t)ib * Nz + j - 1];
+      double iner = (k.a1 + k.gamma) * rhou[(size_t)i * Nz + j - 1] / k.dt;
+      double d = iner + (c23 * (P1 + P2) * invh2 + 0.5 * (C1 + C2) * invh2);
+      double sail = 0.0;
+      if (k.sailor) {
+        double dx = (rho[(size_t)ib * Nz + j - 1] - rho[(size_t)ia * Nz + j - 1]) * invh;
+        sail = dx * k.g0 * k.dt;
+        d = d + sail;
+      }
+      c[0] = d;
+      c[1] = -c23 * P1 * invh2;
+      c[2] = -c23 * P2 * invh2;
+      c[3] = -0.5 * C1 * invh2;
+      c[4] = -0.5 * C2 * invh2;
+      c[5] = -(0.5 * C1 - c13 * P1) * invh2;
+      c[6] = +(0.5 * C1 - c13 * P2) * invh2;
+      c[7] = +(0.5 * C2 - c13 * P1) * invh2;
+      c[8] = -(0.5 * C2 - c13 * P2) * invh2;
+      c[9] = iner + sail;
+    }
+    for (int q = 0; q < 10; ++q) cu[(size_t)q * g.NU + t] = (T)c[q];
+  }
+}
+
+// y = A x over all velocity rows of a level (ghost / boundary rows included);
+// if b != null: y = b - A x.  With FULL (fine level): adds the pressure
+// gradient GG p (fluidmech.jl:343-356).
+template <typename T, bool FULL>
+__device__ __forceinline__ T vel_row(const Geo& g, const OpConst& k, const T* __restrict__ cw,
+                                     const T* __restrict__ cu, const T* __restrict__ xw,
+                                     const T* __restrict__ xu, const T* __restrict__ xp, long long t) {
+  const int Nz = g.Nz, Nx = g.Nx;
+  const int lw = Nz + 1, lu = Nz + 2;
+  if (t < g.NW) {
+    int j = (int)(t % lw), i = (int)(t / lw);
+    if (i == 0) return xw[t] + (T)k.sds * xw[(size_t)Nx * lw + j];
+    if (i == Nx + 1) return xw[t] + (T)k.sds * xw[(size_t)1 * lw + j];
+    if (j == 0 || j == Nz) return cw[t] * xw[t];
+    const size_t NW = g.NW;
+    T s = cw[t] * xw[t];
+    s += cw[1 * NW + t] * xw[t - 1];
+    s += cw[2 * NW + t] * xw[t + 1];
+    s += cw[3 * NW + t] * xw[t - lw];
+    s += cw[4 * NW + t] * xw[t + lw];
+    s += cw[5 * NW + t] * xu[(size_t)(i - 1) * lu + j];
+    s += cw[6 * NW + t] * xu[(size_t)(i - 1) * lu + j + 1];
+    s += cw[7 * NW + t] * xu[(size_t)i * lu + j];
+    s += cw[8 * NW + t] * xu[(size_t)i * lu + j + 1];
+    if (FULL) s += (T)g.invh * (xp[(size_t)i * lu + j + 1] - xp[(size_t)i * lu + j]);
+    return s;
+  }
+  t -= g.NW;
+  int j = (int)(t % lu), i = (int)(t / lu);
+  if (j == 0) return xu[t] + (T)k.top_cnv * xu[t + 1];
+  if (j == Nz + 1) return xu[t] + (T)k.bot_cnv * xu[t - 1];
+  if (k.mms && (int)t == k.pin_u) return xu[t];
+  const size_t NU = g.NU;
+  int il = (i == 0) ? Nx - 1 : i - 1, ir = (i == Nx) ? 1 : i + 1;
+  T s = cu[t] * xu[t];
+  s += cu[1 * NU + t] * xu[(size_t)il * lu + j];
+  s += cu[2 * NU + t] * xu[(size_t)ir * lu + j];
+  s += cu[3 * NU + t] * xu[t - 1];
+  s += cu[4 * NU + t] * xu[t + 1];
+  s += cu[5 * NU + t] * xw[(size_t)i * lw + j - 1];
+  s += cu[6 * NU + t] * xw[(size_t)(i + 1) * lw + j - 1];
+  s += cu[7 * NU + t] * xw[(size_t)i * lw + j];
+  s += cu[8 * NU + t] * xw[(size_t)(i + 1) * lw + j];
+  if (FULL) s += (T)g.invh * (xp[(size_t)(i + 1) * lu + j] - xp[(size_t)i * lu + j]);
+  return s;
+}
+
+// pressure rows of LL: ghost ring, pin, rho-weighted divergence (fluidmech.jl:367-488)
+template <typename T>
+__device__ __forceinline__ T p_row(const Geo& g, const OpConst& k, const T* __restrict__ cp,
+                                   const T* __restrict__ xw, const T* __restrict__ xu,
+                                   const T* __restrict__ xp, int t) {
+  const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2, lw = Nz + 1;
+  int j = t % lp, i = t / lp;
+  if (j == 0) return xp[t] - xp[t + 1];
+  if (j == Nz + 1) return xp[t] - xp[t - 1];
+  if (i == 0) return xp[t] - xp[(size_t)Nx * lp + j];
+  if (i == Nx + 1) return xp[t] - xp[(size_t)1 * lp + j];
+  if (k.mms && t == k.pin_p) return xp[t];
+  const size_t NP = g.NP;
+  T s = cp[t] * xu[(size_t)(i - 1) * lp + j] + cp[NP + t] * xu[(size_t)i * lp + j] +
+        cp[2 * NP + t] * xw[(size_t)i * lw + j - 1] + cp[3 * NP + t] * xw[(size_t)i * lw + j];
+  if (t == k.pin_p) s += xp[t];
+  return s;
+}
+
+// DM coefficients of the interior P rows (fluidmech.jl:373-386)
+__global__ void p_coef_kernel(Geo g, const double* __restrict__ rhow, const double* __restrict__ rhou,
+                              double* cp) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.NP) return;
+  const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
+  int j = t % lp, i = t / lp;
+  double c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+  if (j >= 1 && j <= Nz && i >= 1 && i <= Nx) {
+    c0 = -rhou[(size_t)(i - 1) * Nz + j - 1] * g.invh;
+    c1 = +rhou[(size_t)i * Nz + j - 1] * g.invh;
+    c2 = -rhow[(size_t)(i - 1) * (Nz + 1) + j - 1] * g.invh;
+    c3 = +rhow[(size_t)(i - 1) * (Nz + 1) + j] * g.invh;
+  }
+  cp[t] = c0; cp[g.NP + t] = c1; cp[2 * g.NP + t] = c2; cp[3 * g.NP + t] = c3;
+}
+
+// y = S o (LL (S o v)) on the whole unknown vector; t must hold S o v.
+// If b != null: y = b - S o (LL t).
+template <typename T>
+__global__ void stokes_apply_kernel(Geo g, OpConst k, const T* __restrict__ cw,
+                                    const T* __restrict__ cu, const T* __restrict__ cp,
+                                    const T* __restrict__ scl, const T* __restrict__ tv,
+                                    const T* __restrict__ b, T* y) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  if (t >= n) return;
+  const T* xw = tv;
+  const T* xu = tv + g.NW;
+  const T* xp = tv + g.NW + g.NU;
+  T v;
+  if (t < (long long)g.NW + g.NU) v = vel_row<T, true>(g, k, cw, cu, xw, xu, xp, t);
+  else v = p_row<T>(g, k, cp, xw, xu, xp, (int)(t - g.NW - g.NU));
+  v *= scl[t];
+  y[t] = b ? b[t] - v : v;
+}
+
+template <typename T>
+__global__ void mul_kernel(long long n, const T* __restrict__ a, const T* __restrict__ b, T* out) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) out[t] = a[t] * b[t];
+}
+template <typename T>
+__global__ void div_kernel(long long n, const T* __restrict__ a, const T* __restrict__ b, T* out) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) out[t] = a[t] / b[t];
+}
+template <typename A, typename B>
+__global__ void convert_kernel(long long n, const A* __restrict__ a, B* out) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) out[t] = (B)a[t];
+}
+// x += s o dy (FP64 refinement update)
+template <typename T>
+__global__ void refine_update_kernel(long long n, const T* __restrict__ dy, const double* __restrict__ scl,
+                                     double* x) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) x[t] += scl[t] * (double)dy[t];
+}
+
+// ---------------------------------------------------------------------------
+// velocity multigrid
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void vel_residual_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
+                                    const T* __restrict__ x, const T* __restrict__ b, T* r) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)g.NW + g.NU) return;
+  r[t] = b[t] - vel_row<T, false>(g, k, cw, cu, x, x + g.NW, nullptr, t);
+}
+
+// damped Jacobi: xo = xi + w D^-1 (b - A xi); ghost / boundary rows exact
+template <typename T>
+__global__ void vel_jacobi_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
+                                  const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
+                                  int zero_init) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)g.NW + g.NU) return;
+  const int Nz = g.Nz, Nx = g.Nx;
+  bool exact;
+  T d;
+  if (t < g.NW) {
+    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    exact = (i == 0 || i == Nx + 1 || j == 0 || j == Nz);
+    d = cw[t];
+  } else {
+    long long u = t - g.NW;
+    int j = (int)(u % (Nz + 2));
+    exact = (j == 0 || j == Nz + 1) || (k.mms && (int)u == k.pin_u);
+    d = cu[u];
+  }
+  if (zero_init) {
+    xo[t] = (exact ? (T)1 : omega) * b[t] / d;
+    return;
+  }
+  T res = b[t] - vel_row<T, false>(g, k, cw, cu, xi, xi + g.NW, nullptr, t);
+  xo[t] = xi[t] + (exact ? (T)1 : omega) * res / d;
+}
+
+// restriction of the interior-row residual (full weighting / 4 of the
+// bilinear prolongation); coarse ghost / boundary rows get zero
+template <typename T>
+__global__ void vel_restrict_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)c.NW + c.NU) return;
+  const int lwf = f.Nz + 1, luf = f.Nz + 2;
+  const T* rw = r;
+  const T* ru = r + f.NW;
+  T acc = 0;
+  if (t < c.NW) {
+    int J = (int)(t % (c.Nz + 1)), Ic = (int)(t / (c.Nz + 1));
+    if (J >= 1 && J <= c.Nz - 1 && Ic >= 1 && Ic <= c.Nx) {
+      int I = Ic - 1;
+      const int ixs[4] = {2 * I - 1, 2 * I, 2 * I + 1, 2 * I + 2};
+      const T wx[4] = {(T)0.25, (T)0.75, (T)0.75, (T)0.25};
+      for (int dj = -1; dj <= 1; ++dj) {
+        T wz = dj == 0 ? (T)1 : (T)0.5;
+        int j = 2 * J + dj;
+        for (int q = 0; q < 4; ++q) {
+          int ix = ixs[q];
+          ix = ix < 0 ? ix + f.Nx : (ix >= f.Nx ? ix - f.Nx : ix);
+          acc += wz * wx[q] * rw[(size_t)(ix + 1) * lwf + j];
+        }
+      }
+      acc *= (T)0.25;
+    }
+    bc[t] = acc;
+    return;
+  }
+  t -= c.NW;
+  int Jr = (int)(t % (c.Nz + 2)), I = (int)(t / (c.Nz + 2));
+  if (Jr >= 1 && Jr <= c.Nz) {
+    int Jc = Jr - 1;
+    const int jzs[4] = {2 * Jc - 1, 2 * Jc, 2 * Jc + 1, 2 * Jc + 2};
+    const T wz[4] = {(T)0.25, (T)0.75, (T)0.75, (T)0.25};
+    for (int q = 0; q < 4; ++q) {
+      int jz = jzs[q];
+      if (jz < 0 || jz >= f.Nz) continue;
+      for (int di = -1; di <= 1; ++di) {
+        int i = 2 * I + di;
+        if (i < 0 || i > f.Nx) continue;
+        T wx = di == 0 ? (T)1 : (T)0.5;
+        acc += wz[q] * wx * ru[(size_t)i * luf + jz + 1];
+      }
+    }
+    acc *= (T)0.25;
+  }
+  bc[c.NW + t] = acc;
+}
+
+// x_f += P x_c (bilinear; ghost rows of U follow the reflection rule)
+template <typename T>
+__global__ void vel_prolong_kernel(Geo f, Geo c, OpConst k, const T* __restrict__ xc, T* xf) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)f.NW + f.NU) return;
+  const int lwc = c.Nz + 1, luc = c.Nz + 2;
+  const T* cw = xc;
+  const T* cu = xc + c.NW;
+  if (t < f.NW) {
+    int j = (int)(t % (f.Nz + 1)), i = (int)(t / (f.Nz + 1));
+    int ix = (i - 1) % f.Nx;
+    if (ix < 0) ix += f.Nx;
+    int I0 = ix / 2;
+    int In = (ix % 2 == 0) ? (I0 - 1 + c.Nx) % c.Nx : (I0 + 1) % c.Nx;
+    T v = 0;
+    int J0 = j / 2;
+    int nz = (j % 2 == 0) ? 1 : 2;
+    for (int q = 0; q < nz; ++q) {
+      int J = J0 + q;
+      T wz = nz == 1 ? (T)1 : (T)0.5;
+      v += wz * ((T)0.75 * cw[(size_t)(I0 + 1) * lwc + J] + (T)0.25 * cw[(size_t)(In + 1) * lwc + J]);
+    }
+    xf[t] += v;
+    return;
+  }
+  long long u = t - f.NW;
+  int j = (int)(u % (f.Nz + 2)), i = (int)(u / (f.Nz + 2));
+  auto interior = [&](int jj) -> T {
+    int jz = jj - 1, J0 = jz / 2;
+    int Jn = (jz % 2 == 0) ? J0 : J0 + 2;     // coarse row of the 1/4 neighbour (full layout)
+    T v = 0;
+    int nx = (i % 2 == 0) ? 1 : 2;
+    int I0 = (i % 2 == 0) ? i / 2 : (i - 1) / 2;
+    for (int q = 0; q < nx; ++q) {
+      T wx = nx == 1 ? (T)1 : (T)0.5;
+      int I = I0 + q;
+      v += wx * ((T)0.75 * cu[(size_t)I * luc + J0 + 1] + (T)0.25 * cu[(size_t)I * luc + Jn]);
+    }
+    return v;
+  };
+  T v;
+  if (j == 0) v = -(T)k.top_cnv * interior(1);
+  else if (j == f.Nz + 1) v = -(T)k.bot_cnv * interior(f.Nz);
+  else v = interior(j);
+  xf[t] += v;
+}
+
+// coarse coefficient fields: eta (avg4), etaco (injection), rho (avg4),
+// rhow / rhou (avg of the two fine faces of the coarse face)
+__global__ void coarsen_fields_kernel(int Nzc, int Nxc, const double* __restrict__ eta,
+                                      const double* __restrict__ etaco, const double* __restrict__ rho,
+                                      const double* __restrict__ rhow, const double* __restrict__ rhou,
+                                      double* etac, double* etacoc, double* rhoc, double* rhowc,
+                                      double* rhouc) {
+  int J = blockIdx.x * blockDim.x + threadIdx.x;
+  int I = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Nz = 2 * Nzc, Nx = 2 * Nxc;
+  if (J > Nzc || I > Nxc) return;
+  etacoc[(size_t)I * (Nzc + 1) + J] = etaco[(size_t)(2 * I) * (Nz + 1) + 2 * J];
+  if (I < Nxc) {
+    rhowc[(size_t)I * (Nzc + 1) + J] = 0.5 * (rhow[(size_t)(2 * I) * (Nz + 1) + 2 * J] +
+                                              rhow[(size_t)(2 * I + 1) * (Nz + 1) + 2 * J]);
+  }
+  if (J < Nzc) {
+    rhouc[(size_t)I * Nzc + J] = 0.5 * (rhou[(size_t)(2 * I) * Nz + 2 * J] + rhou[(size_t)(2 * I) * Nz + 2 * J + 1]);
+  }
+  if (J < Nzc && I < Nxc) {
+    size_t a = (size_t)(2 * I) * Nz + 2 * J, b = (size_t)(2 * I + 1) * Nz + 2 * J;
+    etac[(size_t)I * Nzc + J] = 0.25 * (eta[a] + eta[a + 1] + eta[b] + eta[b + 1]);
+    rhoc[(size_t)I * Nzc + J] = 0.25 * (rho[a] + rho[a + 1] + rho[b] + rho[b + 1]);
+  }
+}
+
+// many damped-Jacobi sweeps on the coarsest velocity level in one CTA
+template <typename T>
+__global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
+                                  T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+  const long long n = (long long)g.NW + g.NU;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
+  __syncthreads();
+  T* a = x;
+  T* o = x2;
+  for (int s = 0; s < sweeps; ++s) {
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+      bool exact;
+      T d;
+      if (t < g.NW) {
+        int j = (int)(t % (g.Nz + 1)), i = (int)(t / (g.Nz + 1));
+        exact = (i == 0 || i == g.Nx + 1 || j == 0 || j == g.Nz);
+        d = cw[t];
+      } else {
+        long long u = t - g.NW;
+        int j = (int)(u % (g.Nz + 2));
+        exact = (j == 0 || j == g.Nz + 1);
+        d = cu[u];
+      }
+      T res = b[t] - vel_row<T, false>(g, k, cw, cu, a, a + g.NW, nullptr, t);
+      o[t] = a[t] + (exact ? (T)1 : omega) * res / d;
+    }
+    __syncthreads();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != x)
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = a[t];
+}
+
+// ---------------------------------------------------------------------------
+// pressure (Schur) multigrid on interior cells: periodic x, no flux in z
+// (L p)_c = sum_faces k_f (p_c - p_n) + dpin p_pin
+// kx[j,i]: face left of cell (j,i) (periodic); kz[j,i]: face above (kz[0]=kz[Nz]=0)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T p_apply_at(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
+                                        int pin, T dpin, const T* __restrict__ p, int j, int i, T* diag) {
+  size_t c = (size_t)i * Nz + j;
+  int il = i == 0 ? Nx - 1 : i - 1, ir = i == Nx - 1 ? 0 : i + 1;
+  T kl = kx[c], kr = kx[(size_t)ir * Nz + j];
+  T kt = kz[(size_t)i * (Nz + 1) + j], kb = kz[(size_t)i * (Nz + 1) + j + 1];
+  T pc = p[c];
+  T s = kl * (pc - p[(size_t)il * Nz + j]) + kr * (pc - p[(size_t)ir * Nz + j]);
+  if (j > 0) s += kt * (pc - p[c - 1]);
+  if (j < Nz - 1) s += kb * (pc - p[c + 1]);
+  T d = kl + kr + (j > 0 ? kt : (T)0) + (j < Nz - 1 ? kb : (T)0);
+  if ((int)c == pin) { s += dpin * pc; d += dpin; }
+  *diag = d;
+  return s;
+}
+
+template <typename T>
+__global__ void p_jacobi_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
+                                T dpin, const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
+                                int zero_init) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nz * Nx) return;
+  int j = t % Nz, i = t / Nz;
+  T d;
+  if (zero_init) {
+    p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, b, j, i, &d);   // only the diagonal is used
+    xo[t] = omega * b[t] / d;
+    return;
+  }
+  T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, j, i, &d);
+  xo[t] = xi[t] + omega * (b[t] - ax) / d;
+}
+
+template <typename T>
+__global__ void p_residual_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
+                                  T dpin, const T* __restrict__ x, const T* __restrict__ b, T* r) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nz * Nx) return;
+  T d;
+  r[t] = b[t] - p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, x, t % Nz, t / Nz, &d);
+}
+
+template <typename T>
+__global__ void p_restrict_kernel(int Nzc, int Nxc, const T* __restrict__ r, T* bc) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nzc * Nxc) return;
+  int J = t % Nzc, I = t / Nzc;
+  const int Nz = 2 * Nzc;
+  size_t a = (size_t)(2 * I) * Nz + 2 * J, b = (size_t)(2 * I + 1) * Nz + 2 * J;
+  bc[t] = (T)0.25 * (r[a] + r[a + 1] + r[b] + r[b + 1]);
+}
+
+template <typename T>
+__global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* xf) {
+  const int Nz = 2 * Nzc, Nx = 2 * Nxc;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nz * Nx) return;
+  int j = t % Nz, i = t / Nz;
+  int J = j / 2, I = i / 2;
+  int Jn = (j % 2 == 0) ? (J > 0 ? J - 1 : 0) : (J < Nzc - 1 ? J + 1 : Nzc - 1);
+  int In = (i % 2 == 0) ? (I - 1 + Nxc) % Nxc : (I + 1) % Nxc;
+  T v = (T)9 * xc[(size_t)I * Nzc + J] + (T)3 * xc[(size_t)I * Nzc + Jn] + (T)3 * xc[(size_t)In * Nzc + J] +
+        xc[(size_t)In * Nzc + Jn];
+  xf[t] += v / (T)16;
+}
+
+template <typename T>
+__global__ void p_coarsen_kernel(int Nzc, int Nxc, const T* __restrict__ kx, const T* __restrict__ kz,
+                                 T* kxc, T* kzc) {
+  int J = blockIdx.x * blockDim.x + threadIdx.x;
+  int I = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Nz = 2 * Nzc;
+  if (J > Nzc || I >= Nxc) return;
+  if (J < Nzc)
+    kxc[(size_t)I * Nzc + J] = (kx[(size_t)(2 * I) * Nz + 2 * J] + kx[(size_t)(2 * I) * Nz + 2 * J + 1]) / (T)8;
+  kzc[(size_t)I * (Nzc + 1) + J] = (kz[(size_t)(2 * I) * (Nz + 1) + 2 * J] +
+                                    kz[(size_t)(2 * I + 1) * (Nz + 1) + 2 * J]) / (T)8;
+}
+
+template <typename T>
+__global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
+                                T dpin, T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+  const int n = Nz * Nx;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
+  __syncthreads();
+  T* a = x;
+  T* o = x2;
+  for (int s = 0; s < sweeps; ++s) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      T d;
+      T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, a, t % Nz, t / Nz, &d);
+      o[t] = a[t] + omega * (b[t] - ax) / d;
+    }
+    __syncthreads();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != x)
+    for (int t = threadIdx.x; t < n; t += blockDim.x) x[t] = a[t];
+}
+
+// fine-level pressure coefficients from the velocity diagonal (plane 0: full,
+// plane 9: inertia only) -- k = rho_face / (h^2 A_ff)
+template <typename T>
+__global__ void p_kcoef_kernel(Geo g, const double* __restrict__ rhow, const double* __restrict__ rhou,
+                               const T* __restrict__ cw, const T* __restrict__ cu, int plane, T* kx, T* kz,
+                               T* kr) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, Nx = g.Nx;
+  const double ih2 = g.invh * g.invh;
+  if (t < Nz * Nx) {
+    int j = t % Nz, i = t / Nz;
+    // face left of cell (j,i) is U(j+1, i)
+    double a = (double)cu[(size_t)plane * g.NU + (size_t)i * (Nz + 2) + j + 1];
+    kx[t] = (T)(rhou[(size_t)i * Nz + j] * ih2 / a);
+    if (i == Nx - 1) {    // right face of the last column is U(j+1, Nx)
+      double ar = (double)cu[(size_t)plane * g.NU + (size_t)Nx * (Nz + 2) + j + 1];
+      kr[j] = (T)(rhou[(size_t)Nx * Nz + j] * ih2 / ar);
+    }
+  }
+  if (t < (Nz + 1) * Nx) {
+    int j = t % (Nz + 1), i = t / (Nz + 1);
+    T v = 0;
+    if (j >= 1 && j <= Nz - 1) {
+      double a = (double)cw[(size_t)plane * g.NW + (size_t)(i + 1) * (Nz + 1) + j];
+      v = (T)(rhow[(size_t)i * (Nz + 1) + j] * ih2 / a);
+    }
+    kz[t] = v;
+  }
+}
+
+// pressure part of the preconditioner, before / after the interior solve:
+// ghost elimination of the residual (P ghost rows P_g - P_n = r_g) and the
+// ghost values of the result
+template <typename T>
+__global__ void p_gather_kernel(Geo g, const T* __restrict__ kx, const T* __restrict__ kr,
+                                const T* __restrict__ rp, T* rin) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
+  if (t >= Nz * Nx) return;
+  int j = t % Nz, i = t / Nz;
+  T v = rp[(size_t)(i + 1) * lp + j + 1];
+  if (i == 0) v += kx[j] * rp[j + 1];
+  if (i == Nx - 1) v += kr[j] * rp[(size_t)(Nx + 1) * lp + j + 1];
+  rin[t] = v;
+}
+
+template <typename T>
+__global__ void p_scatter_kernel(Geo g, const T* __restrict__ z, const T* __restrict__ rp,
+                                 const T* __restrict__ etarho, T cmass, T* zp) {
+  // interior cells: z + cmass * (eta/rho) * r
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, lp = Nz + 2;
+  if (t >= Nz * g.Nx) return;
+  int j = t % Nz, i = t / Nz;
+  size_t o = (size_t)(i + 1) * lp + j + 1;
+  zp[o] = z[t] + cmass * etarho[t] * rp[o];
+}
+// ghost columns then ghost rows: P_g = r_g + P_neighbour (fluidmech.jl:403-417)
+template <typename T>
+__global__ void p_scatter_cols_kernel(Geo g, const T* __restrict__ rp, T* zp) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
+  if (j < 1 || j > Nz) return;
+  zp[j] = rp[j] + zp[(size_t)Nx * lp + j];
+  zp[(size_t)(Nx + 1) * lp + j] = rp[(size_t)(Nx + 1) * lp + j] + zp[(size_t)lp + j];
+}
+template <typename T>
+__global__ void p_scatter_rows_kernel(Geo g, const T* __restrict__ rp, T* zp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, lp = Nz + 2;
+  if (i >= g.Nx + 2) return;
+  size_t o = (size_t)i * lp;
+  zp[o] = rp[o] + zp[o + 1];
+  zp[o + Nz + 1] = rp[o + Nz + 1] + zp[o + Nz];
+}
+
+// r_v' = r_v - GG z_p on interior velocity rows (fluidmech.jl:343-356)
+template <typename T>
+__global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, T* rv) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
+  if (t < g.NW) {
+    int j = (int)(t % lw), i = (int)(t / lw);
+    if (j >= 1 && j <= Nz - 1 && i >= 1 && i <= Nx)
+      rv[t] -= (T)g.invh * (zp[(size_t)i * lu + j + 1] - zp[(size_t)i * lu + j]);
+    return;
+  }
+  long long u = t - g.NW;
+  if (u >= g.NU) return;
+  int j = (int)(u % lu), i = (int)(u / lu);
+  if (j >= 1 && j <= Nz) rv[t] -= (T)g.invh * (zp[(size_t)(i + 1) * lu + j] - zp[(size_t)i * lu + j]);
+}
+
+// ---------------------------------------------------------------------------
+// Krylov vector kernels
+// ---------------------------------------------------------------------------
+constexpr int KB = 256;
+constexpr int KG = 2 * kNumSMs;
+
+// partial dot products of w with V[0..m) -> part[blk * m + k]
+template <typename T>
+__global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
+                                                      const T* __restrict__ w, double* part) {
+  __shared__ double sh[KB];
+  for (int k = 0; k < m; ++k) {
+    double acc = 0;
+    const T* v = V + (size_t)k * ldv;
+    for (long long t = blockIdx.x * (long long)KB + threadIdx.x; t < n; t += (long long)KG * KB)
+      acc += (double)v[t] * (double)w[t];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = KB / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(size_t)blockIdx.x * m + k] = sh[0];
+    __syncthreads();
+  }
+}
+__global__ void multidot_final_kernel(int m, const double* __restrict__ part, double* out) {
+  int k = blockIdx.x;
+  __shared__ double sh[KB];
+  double acc = 0;
+  for (int b = threadIdx.x; b < KG; b += KB) acc += part[(size_t)b * m + k];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = KB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[k] = sh[0];
+}
+// w -= sum_k h[k] V[k]
+template <typename T>
+__global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
+                                 const double* __restrict__ h, T* w) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double s = (double)w[t];
+  for (int k = 0; k < m; ++k) s -= h[k] * (double)V[(size_t)k * ldv + t];
+  w[t] = (T)s;
+}
+// x += sum_k y[k] Z[k]
+template <typename T>
+__global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long long ldz,
+                               const double* __restrict__ y, T* x) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double s = (double)x[t];
+  for (int k = 0; k < m; ++k) s += y[k] * (double)Z[(size_t)k * ldz + t];
+  x[t] = (T)s;
+}
+template <typename T>
+__global__ void scale_kernel(long long n, const double* __restrict__ alpha_inv, const T* __restrict__ w,
+                             T* v) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) v[t] = (T)((double)w[t] / *alpha_inv);
+}
+__global__ void sqrt_kernel(double* a) { *a = sqrt(*a); }
+
+// ---------------------------------------------------------------------------
+// RHS assembly
+// ---------------------------------------------------------------------------
+// momentum-advection inputs (fluidmech.jl:236-240, 310-314)
+__global__ void mom_prep_kernel(int Nz, int Nx, CView W, CView U, CView rhow, CView rhou, double* fz,
+                                double* uz, double* wz, double* fx, double* ux, double* wxm) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  // z-momentum grid (Nz-1, Nx): f (Nz-1, Nx), u (Nz-1, Nx+1), w (Nz, Nx)
+  if (j < Nz - 1 && i < Nx) fz[(size_t)i * (Nz - 1) + j] = AT(rhow, j + 1, i) * AT(W, j + 1, i + 1);
+  if (j < Nz - 1 && i <= Nx) uz[(size_t)i * (Nz - 1) + j] = (AT(U, j + 1, i) + AT(U, j + 2, i)) / 2.0;
+  if (j < Nz && i < Nx) wz[(size_t)i * Nz + j] = (AT(W, j, i + 1) + AT(W, j + 1, i + 1)) / 2.0;
+  // x-momentum grid (Nz, Nx+1): f (Nz, Nx+1), u (Nz, Nx+2) with ifx, w (Nz+1, Nx+1)
+  if (j < Nz && i <= Nx) fx[(size_t)i * Nz + j] = AT(rhou, j, i) * AT(U, j + 1, i);
+  if (j < Nz && i <= Nx + 1) {
+    int a = (i == 0) ? Nx - 1 : i - 1;          // ifx[i]
+    int b = (i == Nx + 1) ? 1 : i;              // ifx[i+1]
+    ux[(size_t)i * Nz + j] = (AT(U, j + 1, a) + AT(U, j + 1, b)) / 2.0;
+  }
+  if (j <= Nz && i <= Nx) wxm[(size_t)i * (Nz + 1) + j] = (AT(W, j, i) + AT(W, j, i + 1)) / 2.0;
+}
+
+struct RhsArgs {
+  double a1, a2, a3, dt, g0, D, h, oc;
+  int mms;
+  int pin_p, pin_u;
+};
+
+__global__ void rhs_kernel(Geo g, RhsArgs a, CView Drho, CView rhoWo, CView rhoWoo, CView rhoUo, CView rhoUoo,
+                           CView MFS, const double* __restrict__ advz, const double* __restrict__ advx,
+                           const double* __restrict__ mfs_mean, const double* __restrict__ src_w,
+                           const double* __restrict__ src_u, const double* __restrict__ src_p,
+                           double pin_p_val, double pin_u_val, double* RR) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int Nz = g.Nz, Nx = g.Nx;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  if (t >= n) return;
+  double v = 0.0;
+  if (t < g.NW) {
+    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    if (i >= 1 && i <= Nx) {
+      if (j == Nz) {
+        double mfbg = (*mfs_mean) * a.D / a.h;
+        v = a.oc * AT(MFS, Nz - 1, i - 1) + (1.0 - a.oc) * mfbg;
+      } else if (j >= 1) {
+        v = (AT(Drho, j, i - 1) * a.g0 + (a.a2 * AT(rhoWo, j, i - 1) + a.a3 * AT(rhoWoo, j, i - 1)) / a.dt) -
+            advz[(size_t)(i - 1) * (Nz - 1) + j - 1];
+        if (a.mms) v = v + src_w[t];
+      }
+    }
+  } else if (t < (long long)g.NW + g.NU) {
+    long long u = t - g.NW;
+    int j = (int)(u % (Nz + 2)), i = (int)(u / (Nz + 2));
+    if (j >= 1 && j <= Nz) {
+      double ad;
+      if (i == 0 || i == Nx) ad = (advx[(size_t)j - 1] + advx[(size_t)Nx * Nz + j - 1]) / 2.0;
+      else ad = advx[(size_t)i * Nz + j - 1];
+      v = (a.a2 * AT(rhoUo, j - 1, i) + a.a3 * AT(rhoUoo, j - 1, i)) / a.dt - ad;
+      if (a.mms) v = v + src_u[u];
+      if (a.mms && (int)u == a.pin_u) v = pin_u_val;
+    }
+  } else {
+    int p = (int)(t - g.NW - g.NU);
+    int j = p % (Nz + 2), i = p / (Nz + 2);
+    if (j >= 1 && j <= Nz && i >= 1 && i <= Nx) {
+      v = AT(MFS, j - 1, i - 1);
+      if (a.mms) v = v + src_p[p];
+    }
+    if (a.mms && p == a.pin_p) v = pin_p_val;
+  }
+  RR[t] = v;
+}
+
+// MFS update (fluidmech.jl:115-126); explicit round-to-nearest intrinsics keep
+// every product and sum separately rounded (no FMA contraction) so the state
+// field MFS matches the reference arithmetic bit for bit
+__global__ void mfs_kernel(int Nz, int Nx, double a1, double a2, double a3, double b1, double b2, double b3,
+                           double dt, double alpha, CView rho, CView rhoo, CView rhooo, CView advn_rho,
+                           DView drhodt, CView drhodto, CView drhodtoo, DView MFS) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j >= Nz || i >= Nx) return;
+  double d = -AT(advn_rho, j, i);
+  AT(drhodt, j, i) = d;
+  double lhs = __dsub_rn(__dsub_rn(__dmul_rn(a1, AT(rho, j, i)), __dmul_rn(a2, AT(rhoo, j, i))),
+                         __dmul_rn(a3, AT(rhooo, j, i)));
+  double rhs = __dadd_rn(__dadd_rn(__dmul_rn(b1, d), __dmul_rn(b2, AT(drhodto, j, i))),
+                         __dmul_rn(b3, AT(drhodtoo, j, i)));
+  double res = __dsub_rn(__ddiv_rn(lhs, dt), rhs);
+  AT(MFS, j, i) = __dsub_rn(AT(MFS, j, i), __dmul_rn(alpha, res));
+}
+
+// scl = 1 / (sqrt|diag LL| + extra) (fluidmech.jl:496-501)
+__global__ void scl_kernel(Geo g, OpConst k, const double* __restrict__ cw, const double* __restrict__ cu,
+                           CView rho, CView eta, double* scl, double* etarho) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  if (t >= n) return;
+  double d, extra = 0.0;
+  if (t < g.NW) d = cw[t];
+  else if (t < (long long)g.NW + g.NU) d = cu[t - g.NW];
+  else {
+    int p = (int)(t - g.NW - g.NU);
+    int j = p % (g.Nz + 2), i = p / (g.Nz + 2);
+    bool interior = j >= 1 && j <= g.Nz && i >= 1 && i <= g.Nx;
+    d = interior ? 0.0 : 1.0;
+    if (p == k.pin_p) d = 1.0;
+    double sp = interior ? AT(rho, j - 1, i - 1) / AT(eta, j - 1, i - 1) : 1.0;
+    extra = sqrt(1.0 / sp);
+    if (interior) etarho[(size_t)(i - 1) * g.Nz + j - 1] = 1.0 / sp;
+  }
+  scl[t] = 1.0 / (sqrt(fabs(d)) + extra);
+}
+
+// write the solution back (x is the physical unknown vector)
+__global__ void unpack_kernel(Geo g, const double* __restrict__ x, DView W, DView U, DView P) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < g.NW) { W.p[t] = x[t]; return; }
+  t -= g.NW;
+  if (t < g.NU) { U.p[t] = x[g.NW + t]; return; }
+  t -= g.NU;
+  if (t < g.NP) P.p[t] = x[g.NW + g.NU + t];
+}
+__global__ void pack_kernel(Geo g, CView W, CView U, CView P, double* x) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < g.NW) { x[t] = W.p[t]; return; }
+  t -= g.NW;
+  if (t < g.NU) { x[g.NW + t] = U.p[t]; return; }
+  t -= g.NU;
+  if (t < g.NP) x[g.NW + g.NU + t] = P.p[t];
+}
+
+inline unsigned nblk(long long n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host-side solver state
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Hier {
+  int nv, np_lv;               // velocity and pressure level counts
+  Geo vg[kMaxLevels];
+  T* cw[kMaxLevels];
+  T* cu[kMaxLevels];
+  T* vx[kMaxLevels];
+  T* vx2[kMaxLevels];
+  T* vb[kMaxLevels];
+  T* vr[kMaxLevels];
+  int pNz[kMaxLevels], pNx[kMaxLevels], ppin[kMaxLevels];
+  T pdpin[kMaxLevels];
+  T* kx[kMaxLevels];
+  T* kz[kMaxLevels];
+  T* px[kMaxLevels];
+  T* px2[kMaxLevels];
+  T* pb[kMaxLevels];
+  T* pr[kMaxLevels];
+  T* kr;          // right-face coefficient of the last column (fine level)
+  T* cp;          // DM coefficient planes (fine level)
+  T* scl;         // scaling vector
+  T* etarho;      // eta/rho on interior cells
+  // Krylov
+  int m;
+  T* V;
+  T* Z;
+  T* w;
+  T* t;
+  T* y;           // current iterate (scaled unknowns)
+  T* rv;          // preconditioner scratch (velocity part, physical)
+  T* rp;          // preconditioner scratch (pressure, physical full layout)
+  T* rin;         // interior pressure rhs
+};
+
+struct StokesWork {
+  Geo g;
+  bool ok;
+  Hier<double> d;
+  Hier<float> f;
+  bool f_alloc;
+  // coarse coefficient fields (double), per velocity level >= 1
+  double *eta[kMaxLevels], *etaco[kMaxLevels], *rho[kMaxLevels], *rhow[kMaxLevels], *rhou[kMaxLevels];
+  OpConst last_k;   // operator constants of the last solve (instrumentation)
+  bool have_k;
+  double* RR;
+  double* x;      // physical solution (double)
+  double* r;      // scaled residual (double)
+  double* part;   // multidot partials
+  double* hdev;   // device small vectors (2 * kMaxRestart + 8)
+  double* hhost;  // pinned host mirror
+  // momentum advection scratch
+  double *fz, *uz, *wz, *fx, *ux, *wx, *advz, *advx;
+  double *srcw, *srcu, *srcp;
+  cudaEvent_t ev0, ev1;
+};
+
+namespace {
+
+template <typename T>
+int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
+  const Geo& g = w->g;
+  H.m = m;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  // velocity levels
+  int Nz = g.Nz, Nx = g.Nx;
+  double h = g.h;
+  H.nv = 0;
+  while (H.nv < kMaxLevels) {
+    Geo lg = make_geo(Nz, Nx, h);
+    H.vg[H.nv] = lg;
+    long long nvv = (long long)lg.NW + lg.NU;
+    XC_CUDA_TRY(cudaMalloc(&H.cw[H.nv], sizeof(T) * 10 * lg.NW));
+    XC_CUDA_TRY(cudaMalloc(&H.cu[H.nv], sizeof(T) * 10 * lg.NU));
+    XC_CUDA_TRY(cudaMalloc(&H.vx[H.nv], sizeof(T) * nvv));
+    XC_CUDA_TRY(cudaMalloc(&H.vx2[H.nv], sizeof(T) * nvv));
+    XC_CUDA_TRY(cudaMalloc(&H.vb[H.nv], sizeof(T) * nvv));
+    XC_CUDA_TRY(cudaMalloc(&H.vr[H.nv], sizeof(T) * nvv));
+    H.nv++;
+    if (Nz % 2 || Nx % 2 || Nz / 2 < 4 || Nx / 2 < 4 || (long long)Nz * Nx <= 256) break;
+    Nz /= 2; Nx /= 2; h *= 2;
+  }
+  // pressure levels
+  Nz = g.Nz; Nx = g.Nx;
+  int pz = (int)std::nearbyint(g.Nz / 2.0) - 2, px = (int)std::nearbyint(g.Nx / 2.0) - 2;
+  H.np_lv = 0;
+  while (H.np_lv < kMaxLevels) {
+    int L = H.np_lv;
+    H.pNz[L] = Nz; H.pNx[L] = Nx; H.ppin[L] = px * Nz + pz;
+    XC_CUDA_TRY(cudaMalloc(&H.kx[L], sizeof(T) * Nz * Nx));
+    XC_CUDA_TRY(cudaMalloc(&H.kz[L], sizeof(T) * (Nz + 1) * Nx));
+    XC_CUDA_TRY(cudaMalloc(&H.px[L], sizeof(T) * Nz * Nx));
+    XC_CUDA_TRY(cudaMalloc(&H.px2[L], sizeof(T) * Nz * Nx));
+    XC_CUDA_TRY(cudaMalloc(&H.pb[L], sizeof(T) * Nz * Nx));
+    XC_CUDA_TRY(cudaMalloc(&H.pr[L], sizeof(T) * Nz * Nx));
+    H.np_lv++;
+    if (Nz % 2 || Nx % 2 || Nz / 2 < 2 || Nx / 2 < 2 || (long long)Nz * Nx <= 64) break;
+    Nz /= 2; Nx /= 2; pz /= 2; px /= 2;
+  }
+  XC_CUDA_TRY(cudaMalloc(&H.kr, sizeof(T) * g.Nz));
+  XC_CUDA_TRY(cudaMalloc(&H.cp, sizeof(T) * 4 * g.NP));
+  XC_CUDA_TRY(cudaMalloc(&H.scl, sizeof(T) * n));
+  XC_CUDA_TRY(cudaMalloc(&H.etarho, sizeof(T) * g.Nz * g.Nx));
+  XC_CUDA_TRY(cudaMalloc(&H.V, sizeof(T) * n * (m + 1)));
+  XC_CUDA_TRY(cudaMalloc(&H.Z, sizeof(T) * n * m));
+  XC_CUDA_TRY(cudaMalloc(&H.w, sizeof(T) * n));
+  XC_CUDA_TRY(cudaMalloc(&H.t, sizeof(T) * n));
+  XC_CUDA_TRY(cudaMalloc(&H.y, sizeof(T) * n));
+  XC_CUDA_TRY(cudaMalloc(&H.rv, sizeof(T) * (g.NW + g.NU)));
+  XC_CUDA_TRY(cudaMalloc(&H.rp, sizeof(T) * g.NP));
+  XC_CUDA_TRY(cudaMalloc(&H.rin, sizeof(T) * g.Nz * g.Nx));
+  return XC_OK;
+}
+
+template <typename T>
+void free_hier(Hier<T>& H) {
+  for (int l = 0; l < H.nv; ++l) {
+    cudaFree(H.cw[l]); cudaFree(H.cu[l]); cudaFree(H.vx[l]); cudaFree(H.vx2[l]); cudaFree(H.vb[l]); cudaFree(H.vr[l]);
+  }
+  for (int l = 0; l < H.np_lv; ++l) {
+    cudaFree(H.kx[l]); cudaFree(H.kz[l]); cudaFree(H.px[l]); cudaFree(H.px2[l]); cudaFree(H.pb[l]); cudaFree(H.pr[l]);
+  }
+  cudaFree(H.kr); cudaFree(H.cp); cudaFree(H.scl); cudaFree(H.etarho); cudaFree(H.V); cudaFree(H.Z);
+  cudaFree(H.w); cudaFree(H.t); cudaFree(H.y); cudaFree(H.rv); cudaFree(H.rp); cudaFree(H.rin);
+  H.nv = H.np_lv = 0;
+}
+
+struct SolveCfg {
+  double omega_v = 0.7, omega_p = 0.8;
+  int nu = 2;
+  int coarse_sweeps = 200;
+  double cmass = 0.0;     // eta/rho mass term in the Schur approximation
+  int kplane = 0;         // 0: full velocity diagonal, 9: inertia-only
+};
+
+// ---- velocity V-cycle on level l: solve A x = vb[l] approximately (x := vx[l])
+template <typename T>
+int vcycle_vel(Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int l, cudaStream_t s) {
+  const Geo& g = H.vg[l];
+  const long long n = (long long)g.NW + g.NU;
+  const T om = (T)cfg.omega_v;
+  if (l == H.nv - 1) {
+    vel_coarse_kernel<T><<<1, 1024, 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vx2[l], H.vb[l],
+                                            cfg.coarse_sweeps, om); xc_count_launch();
+    XC_LAUNCH_CHECK();
+    return XC_OK;
+  }
+  // pre-smoothing (first sweep from zero)
+  vel_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vb[l], H.vx[l], om, 1); xc_count_launch();
+  T* a = H.vx[l];
+  T* o = H.vx2[l];
+  for (int q = 1; q < cfg.nu; ++q) {
+    vel_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], a, H.vb[l], o, om, 0); xc_count_launch();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+  vel_residual_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vb[l], H.vr[l]); xc_count_launch();
+  const Geo& c = H.vg[l + 1];
+  vel_restrict_kernel<T><<<nblk((long long)c.NW + c.NU), 256, 0, s>>>(g, c, H.vr[l], H.vb[l + 1]); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_TRY(vcycle_vel<T>(H, k, cfg, l + 1, s));
+  vel_prolong_kernel<T><<<nblk(n), 256, 0, s>>>(g, c, k, H.vx[l + 1], H.vx[l]); xc_count_launch();
+  a = H.vx[l];
+  o = H.vx2[l];
+  for (int q = 0; q < cfg.nu; ++q) {
+    vel_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], a, H.vb[l], o, om, 0); xc_count_launch();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+template <typename T>
+int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
+  const int Nz = H.pNz[l], Nx = H.pNx[l], n = Nz * Nx;
+  const T om = (T)cfg.omega_p;
+  if (l == H.np_lv - 1) {
+    p_coarse_kernel<T><<<1, 1024, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.px2[l],
+                                          H.pb[l], cfg.coarse_sweeps, om); xc_count_launch();
+    XC_LAUNCH_CHECK();
+    return XC_OK;
+  }
+  p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
+                                             H.px[l], om, 1); xc_count_launch();
+  T* a = H.px[l];
+  T* o = H.px2[l];
+  for (int q = 1; q < cfg.nu; ++q) {
+    p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                               om, 0); xc_count_launch();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != H.px[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.px[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+  p_residual_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
+                                               H.pr[l]); xc_count_launch();
+  const int Nzc = H.pNz[l + 1], Nxc = H.pNx[l + 1];
+  p_restrict_kernel<T><<<nblk(Nzc * Nxc), 256, 0, s>>>(Nzc, Nxc, H.pr[l], H.pb[l + 1]); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_TRY(vcycle_p<T>(H, cfg, l + 1, s));
+  p_prolong_kernel<T><<<nblk(n), 256, 0, s>>>(Nzc, Nxc, H.px[l + 1], H.px[l]); xc_count_launch();
+  a = H.px[l];
+  o = H.px2[l];
+  for (int q = 0; q < cfg.nu; ++q) {
+    p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                               om, 0); xc_count_launch();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != H.px[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.px[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+// out = M^-1 v for the scaled system: out = S^-1 M_phys (S^-1 v)
+template <typename T>
+int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* v, T* out,
+            cudaStream_t s) {
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  const long long nvv = (long long)g.NW + g.NU;
+  // physical residual r = S^-1 v -> velocity part into vb[0], pressure into rp
+  div_kernel<T><<<nblk(nvv), 256, 0, s>>>(nvv, v, H.scl, H.vb[0]); xc_count_launch();
+  div_kernel<T><<<nblk(g.NP), 256, 0, s>>>(g.NP, v + nvv, H.scl + nvv, H.rp); xc_count_launch();
+  // pressure: interior solve with ghost elimination
+  p_gather_kernel<T><<<nblk(g.Nz * g.Nx), 256, 0, s>>>(g, H.kx[0], H.kr, H.rp, H.pb[0]); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_TRY(vcycle_p<T>(H, cfg, 0, s));
+  T* zp = out + nvv;   // physical z_p written directly into out, rescaled below
+  p_scatter_kernel<T><<<nblk((long long)g.Nz * g.Nx), 256, 0, s>>>(g, H.px[0], H.rp, H.etarho, (T)cfg.cmass, zp); xc_count_launch();
+  p_scatter_cols_kernel<T><<<nblk(g.Nz + 1), 256, 0, s>>>(g, H.rp, zp); xc_count_launch();
+  p_scatter_rows_kernel<T><<<nblk(g.Nx + 2), 256, 0, s>>>(g, H.rp, zp); xc_count_launch();
+  // velocity: rhs r_v - GG z_p, one V-cycle
+  sub_grad_kernel<T><<<nblk(nvv), 256, 0, s>>>(g, zp, H.vb[0]); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_TRY(vcycle_vel<T>(H, k, cfg, 0, s));
+  div_kernel<T><<<nblk(nvv), 256, 0, s>>>(nvv, H.vx[0], H.scl, out); xc_count_launch();
+  div_kernel<T><<<nblk(g.NP), 256, 0, s>>>(g.NP, zp, H.scl + nvv, zp); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  (void)n;
+  return XC_OK;
+}
+
+// y_out = S o LL (S o v)  (or b - that when b != null)
+template <typename T>
+int apply_scaled(StokesWork* w, Hier<T>& H, const OpConst& k, const T* v, const T* b, T* y, cudaStream_t s) {
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  mul_kernel<T><<<nblk(n), 256, 0, s>>>(n, v, H.scl, H.t); xc_count_launch();
+  stokes_apply_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[0], H.cu[0], H.cp, H.scl, H.t, b, y); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+// ||v||^2 -> hdev[slot] (device), deterministic
+template <typename T>
+int dot_self(StokesWork* w, Hier<T>& H, const T* v, long long n, int slot, cudaStream_t s) {
+  multidot_kernel<T><<<KG, KB, 0, s>>>(n, 1, v, n, v, w->part); xc_count_launch();
+  multidot_final_kernel<<<1, KB, 0, s>>>(1, w->part, w->hdev + slot); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+// FGMRES(m) on S LL S y = rhs (rhs already in H.w on entry is NOT assumed):
+// solves from the initial guess in H.y; rhs = rhs_dev (scaled).
+// Returns iterations used; sets *relres = ||rhs - A y|| / ||rhs||.
+template <typename T>
+int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* rhs, double rtol,
+           int maxit, int* its_out, double* relres_out, cudaStream_t s) {
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  const int m = H.m;
+  double* hh = w->hhost;
+  XC_TRY(dot_self<T>(w, H, rhs, n, 0, s));
+  XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  const double bnorm = std::sqrt(hh[0]) > 0 ? std::sqrt(hh[0]) : 1.0;
+  int its = 0;
+  double relres = 1.0;
+  std::vector<double> Hm((size_t)(m + 1) * m), cs(m), sn(m), gv(m + 1), yv(m);
+  while (true) {
+    // r = rhs - A y  -> V[0]
+    XC_TRY(apply_scaled<T>(w, H, k, H.y, rhs, H.V, s));
+    XC_TRY(dot_self<T>(w, H, H.V, n, 0, s));
+    XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    XC_CUDA_TRY(cudaStreamSynchronize(s));
+    double beta = std::sqrt(hh[0]);
+    relres = beta / bnorm;
+    if (!(relres > rtol) || its >= maxit) break;
+    if (!std::isfinite(beta)) { *its_out = its; *relres_out = relres; xc_set_error("fgmres: non-finite residual"); return XC_NAN; }
+    hh[0] = beta;
+    XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 1, hh, sizeof(double), cudaMemcpyHostToDevice, s));
+    scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 1, H.V, H.V); xc_count_launch();
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+    int kk = 0;
+    for (; kk < m && its < maxit; ++kk) {
+      T* vk = H.V + (size_t)kk * n;
+      T* zk = H.Z + (size_t)kk * n;
+      XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
+      T* wv = H.V + (size_t)(kk + 1) * n;
+      XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
+      // classical Gram-Schmidt, two passes
+      double* hd = w->hdev + 8;
+      for (int pass = 0; pass < 2; ++pass) {
+        multidot_kernel<T><<<KG, KB, 0, s>>>(n, kk + 1, H.V, n, wv, w->part); xc_count_launch();
+        multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, w->part, hd + pass * kMaxRestart); xc_count_launch();
+        multiaxpy_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv); xc_count_launch();
+      }
+      XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
+      XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
+      XC_CUDA_TRY(cudaStreamSynchronize(s));
+      XC_LAUNCH_CHECK();
+      for (int i = 0; i <= kk; ++i) Hm[(size_t)kk * (m + 1) + i] = hh[8 + i] + hh[8 + kMaxRestart + i];
+      double hn = std::sqrt(hh[2]);
+      Hm[(size_t)kk * (m + 1) + kk + 1] = hn;
+      hh[1] = hn > 0 ? hn : 1.0;
+      XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 1, hh + 1, sizeof(double), cudaMemcpyHostToDevice, s));
+      scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 1, wv, wv); xc_count_launch();
+      // Givens rotations on column kk
+      double* col = &Hm[(size_t)kk * (m + 1)];
+      for (int i = 0; i < kk; ++i) {
+        double a = col[i], b = col[i + 1];
+        col[i] = cs[i] * a + sn[i] * b;
+        col[i + 1] = -sn[i] * a + cs[i] * b;
+      }
+      double a = col[kk], b = col[kk + 1];
+      double r = std::hypot(a, b);
+      cs[kk] = r > 0 ? a / r : 1.0;
+      sn[kk] = r > 0 ? b / r : 0.0;
+      col[kk] = r;
+      col[kk + 1] = 0.0;
+      gv[kk + 1] = -sn[kk] * gv[kk];
+      gv[kk] = cs[kk] * gv[kk];
+      ++its;
+      relres = std::fabs(gv[kk + 1]) / bnorm;
+      if (!std::isfinite(relres)) { xc_set_error("fgmres: breakdown"); return XC_NAN; }
+      if (relres <= rtol * 0.5 || hn == 0.0) { ++kk; break; }
+    }
+    // back substitution and update y += Z yv
+    for (int i = kk - 1; i >= 0; --i) {
+      double sacc = gv[i];
+      for (int j = i + 1; j < kk; ++j) sacc -= Hm[(size_t)j * (m + 1) + i] * yv[j];
+      yv[i] = sacc / Hm[(size_t)i * (m + 1) + i];
+    }
+    XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 8, yv.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
+    combine_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
+    XC_LAUNCH_CHECK();
+  }
+  *its_out = its;
+  *relres_out = relres;
+  return XC_OK;
+}
+
+// build the operator coefficients and both multigrid hierarchies for one solve
+template <typename T>
+int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, xc_ctx* c, cudaStream_t s) {
+  for (int l = 0; l < H.nv; ++l) {
+    const Geo& lg = H.vg[l];
+    const double* eta = l ? w->eta[l] : (const double*)c->field[FLD_eta];
+    const double* etaco = l ? w->etaco[l] : (const double*)c->field[FLD_etaco];
+    const double* rho = l ? w->rho[l] : (const double*)c->field[FLD_rho];
+    const double* rhow = l ? w->rhow[l] : (const double*)c->field[FLD_rhow];
+    const double* rhou = l ? w->rhou[l] : (const double*)c->field[FLD_rhou];
+    OpConst kl = k;
+    if (l) kl.mms = 0;
+    vel_coef_kernel<T><<<nblk((long long)lg.NW + lg.NU), 256, 0, s>>>(lg, kl, eta, etaco, rho, rhow, rhou,
+                                                                      H.cw[l], H.cu[l]); xc_count_launch();
+    XC_LAUNCH_CHECK();
+  }
+  // DM planes, scaling, eta/rho (double), converted for FP32
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  double* cpd = w->d.cp;
+  p_coef_kernel<<<nblk(g.NP), 256, 0, s>>>(g, (const double*)c->field[FLD_rhow], (const double*)c->field[FLD_rhou],
+                                           cpd); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  if ((void*)&H != (void*)&w->d) {
+    convert_kernel<double, T><<<nblk(4LL * g.NP), 256, 0, s>>>(4LL * g.NP, cpd, H.cp); xc_count_launch();
+    convert_kernel<double, T><<<nblk(n), 256, 0, s>>>(n, w->d.scl, H.scl); xc_count_launch();
+    convert_kernel<double, T><<<nblk((long long)g.Nz * g.Nx), 256, 0, s>>>((long long)g.Nz * g.Nx, w->d.etarho,
+                                                                          H.etarho); xc_count_launch();
+  }
+  // pressure hierarchy
+  p_kcoef_kernel<T><<<nblk((long long)(g.Nz + 1) * g.Nx), 256, 0, s>>>(
+      g, (const double*)c->field[FLD_rhow], (const double*)c->field[FLD_rhou], H.cw[0], H.cu[0], cfg.kplane,
+      H.kx[0], H.kz[0], H.kr); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  H.pdpin[0] = (T)1.0;
+  for (int l = 1; l < H.np_lv; ++l) {
+    dim3 blk(32, 8);
+    p_coarsen_kernel<T><<<grid2d(H.pNz[l] + 1, H.pNx[l], blk), blk, 0, s>>>(H.pNz[l], H.pNx[l], H.kx[l - 1],
+                                                                            H.kz[l - 1], H.kx[l], H.kz[l]); xc_count_launch();
+    H.pdpin[l] = H.pdpin[l - 1] / (T)4;
+    XC_LAUNCH_CHECK();
+  }
+  return XC_OK;
+}
+
+}  // namespace
+
+int stokes_create(xc_ctx* c) {
+  c->stokes = nullptr;
+  if (c->Nz < 4 || c->Nx < 4) return XC_OK;   // no solver for tiny grids
+  StokesWork* w = new StokesWork();
+  std::memset((void*)w, 0, sizeof(StokesWork));
+  c->stokes = w;
+  w->g = make_geo(c->Nz, c->Nx, c->p.h);
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  XC_TRY(alloc_hier<double>(w, w->d, 30));
+  for (int l = 1; l < w->d.nv; ++l) {
+    const Geo& lg = w->d.vg[l];
+    XC_CUDA_TRY(cudaMalloc(&w->eta[l], sizeof(double) * lg.Nz * lg.Nx));
+    XC_CUDA_TRY(cudaMalloc(&w->etaco[l], sizeof(double) * (lg.Nz + 1) * (lg.Nx + 1)));
+    XC_CUDA_TRY(cudaMalloc(&w->rho[l], sizeof(double) * lg.Nz * lg.Nx));
+    XC_CUDA_TRY(cudaMalloc(&w->rhow[l], sizeof(double) * (lg.Nz + 1) * lg.Nx));
+    XC_CUDA_TRY(cudaMalloc(&w->rhou[l], sizeof(double) * lg.Nz * (lg.Nx + 1)));
+  }
+  XC_CUDA_TRY(cudaMalloc(&w->RR, sizeof(double) * n));
+  XC_CUDA_TRY(cudaMalloc(&w->x, sizeof(double) * n));
+  XC_CUDA_TRY(cudaMalloc(&w->r, sizeof(double) * n));
+  XC_CUDA_TRY(cudaMalloc(&w->part, sizeof(double) * KG * (kMaxRestart + 1)));
+  XC_CUDA_TRY(cudaMalloc(&w->hdev, sizeof(double) * (8 + 2 * kMaxRestart)));
+  XC_CUDA_TRY(cudaMallocHost(&w->hhost, sizeof(double) * (8 + 2 * kMaxRestart + kMaxRestart)));
+  const int Nz = g.Nz, Nx = g.Nx;
+  XC_CUDA_TRY(cudaMalloc(&w->fz, sizeof(double) * (Nz - 1) * Nx));
+  XC_CUDA_TRY(cudaMalloc(&w->uz, sizeof(double) * (Nz - 1) * (Nx + 1)));
+  XC_CUDA_TRY(cudaMalloc(&w->wz, sizeof(double) * Nz * Nx));
+  XC_CUDA_TRY(cudaMalloc(&w->fx, sizeof(double) * Nz * (Nx + 1)));
+  XC_CUDA_TRY(cudaMalloc(&w->ux, sizeof(double) * Nz * (Nx + 2)));
+  XC_CUDA_TRY(cudaMalloc(&w->wx, sizeof(double) * (Nz + 1) * (Nx + 1)));
+  XC_CUDA_TRY(cudaMalloc(&w->advz, sizeof(double) * (Nz - 1) * Nx));
+  XC_CUDA_TRY(cudaMalloc(&w->advx, sizeof(double) * Nz * (Nx + 1)));
+  XC_CUDA_TRY(cudaEventCreate(&w->ev0));
+  XC_CUDA_TRY(cudaEventCreate(&w->ev1));
+  w->ok = true;
+  return XC_OK;
+}
+
+void stokes_destroy(xc_ctx* c) {
+  StokesWork* w = c->stokes;
+  if (!w) return;
+  free_hier<double>(w->d);
+  if (w->f_alloc) free_hier<float>(w->f);
+  for (int l = 1; l < kMaxLevels; ++l) {
+    cudaFree(w->eta[l]); cudaFree(w->etaco[l]); cudaFree(w->rho[l]); cudaFree(w->rhow[l]); cudaFree(w->rhou[l]);
+  }
+  cudaFree(w->RR); cudaFree(w->x); cudaFree(w->r); cudaFree(w->part); cudaFree(w->hdev);
+  cudaFreeHost(w->hhost);
+  cudaFree(w->fz); cudaFree(w->uz); cudaFree(w->wz); cudaFree(w->fx); cudaFree(w->ux); cudaFree(w->wx);
+  cudaFree(w->advz); cudaFree(w->advx); cudaFree(w->srcw); cudaFree(w->srcu); cudaFree(w->srcp);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+  c->stokes = nullptr;
+}
+
 int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_opts* opts,
                    xc_solver_stats* stats, const MmsData* mms) {
-  (void)c; (void)coefs; (void)dt; (void)opts; (void)stats; (void)mms;
-  xc_set_error("fluidmech: Stokes solver not built");
-  return XC_BAD_ARG;
+  StokesWork* w = c->stokes;
+  if (!w || !w->ok) { xc_set_error("fluidmech: grid too small for the Stokes solver (need Nz, Nx >= 4)"); return XC_BAD_ARG; }
+  if (c->p.open_cnv) { xc_set_error("fluidmech: open_cnv = true is not supported"); return XC_BAD_ARG; }
+  xc_solver_opts o;
+  if (opts) o = *opts;
+  else { o.kind = XC_SOLVER_FGMRES_FP64; o.rtol = 1e-10; o.maxit = 500; o.restart = 30; o.inner_rtol = 1e-4; o.inner_maxit = 60; }
+  if (o.restart < 2) o.restart = 30;
+  if (o.restart > 30) o.restart = 30;
+  const Geo& g = w->g;
+  const int Nz = g.Nz, Nx = g.Nx;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  cudaStream_t s = c->stream;
+  const xc_params& p = c->p;
+  XC_CUDA_TRY(cudaEventRecord(w->ev0, s));
+  dim3 blk(32, 8);
+  // MFS update + mean (fluidmech.jl:115-127)
+  if (!mms) {
+    mfs_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(Nz, Nx, coefs[0], coefs[1], coefs[2], coefs[3], coefs[4], coefs[5],
+                                                   dt, p.alpha, CF(c, FLD_rho), CF(c, FLD_rhoo), CF(c, FLD_rhooo),
+                                                   CF(c, FLD_advn_rho), F(c, FLD_drhodt), CF(c, FLD_drhodto),
+                                                   CF(c, FLD_drhodtoo), F(c, FLD_MFS)); xc_count_launch();
+    XC_LAUNCH_CHECK();
+  }
+  XC_TRY(reduce_to(c, RED_SUM, CF(c, FLD_MFS), CView{nullptr, 0}, nullptr, Nz, Nx, c->dscal + SC_MFS_MEAN, s,
+                   (double)Nz * (double)Nx));
+  // momentum advection of the current W, U (fluidmech.jl:236-240, 310-318)
+  mom_prep_kernel<<<grid2d(Nz + 1, Nx + 2, blk), blk, 0, s>>>(Nz, Nx, CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_rhow),
+                                                              CF(c, FLD_rhou), w->fz, w->uz, w->wz, w->fx, w->ux,
+                                                              w->wx); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_TRY(stencil_advect_flux(w->fz, Nz - 1, false, Nz - 1, Nx, p.ADVN, p.xBC, p.zBC, CView{w->uz, Nz - 1},
+                             CView{w->wz, Nz}, p.h, DView{w->advz, Nz - 1}, DView{nullptr, 0}, DView{nullptr, 0}, s));
+  XC_TRY(stencil_advect_flux(w->fx, Nz, false, Nz, Nx + 1, p.ADVN, p.xBC, p.zBC, CView{w->ux, Nz},
+                             CView{w->wx, Nz + 1}, p.h, DView{w->advx, Nz}, DView{nullptr, 0}, DView{nullptr, 0}, s));
+  // operator constants
+  OpConst k;
+  k.a1 = coefs[0]; k.gamma = p.gamma; k.dt = dt; k.g0 = p.g0;
+  k.sds = p.sds; k.top_cnv = p.top_cnv; k.bot_cnv = p.bot_cnv;
+  k.sailor = mms ? 0 : 1;
+  k.mms = mms ? 1 : 0;
+  int pin_z, pin_x;
+  double pin_p_val = 0, pin_u_val = 0;
+  k.pin_u = -1;
+  if (mms) {
+    pin_z = (int)std::nearbyint((Nz + 2) * 3.0 / 8.0) - 1;
+    pin_x = (int)std::nearbyint((Nx + 2) / 2.0) - 1;
+    int uz_ = (int)std::nearbyint((Nz + 2) / 2.0) - 1, ux_ = (int)std::nearbyint((Nx + 2) / 2.0) - 1;
+    k.pin_u = ux_ * (Nz + 2) + uz_;
+    pin_p_val = mms->P_exact[(size_t)pin_x * (Nz + 2) + pin_z];
+    pin_u_val = mms->U_exact[(size_t)ux_ * (Nz + 2) + uz_];
+  } else {
+    pin_z = (int)std::nearbyint(Nz / 2.0) - 1;
+    pin_x = (int)std::nearbyint(Nx / 2.0) - 1;
+  }
+  k.pin_p = pin_x * (Nz + 2) + pin_z;
+  // RHS
+  if (mms) {
+    if (!w->srcw) {
+      XC_CUDA_TRY(cudaMalloc(&w->srcw, sizeof(double) * g.NW));
+      XC_CUDA_TRY(cudaMalloc(&w->srcu, sizeof(double) * g.NU));
+      XC_CUDA_TRY(cudaMalloc(&w->srcp, sizeof(double) * g.NP));
+    }
+    XC_CUDA_TRY(cudaMemcpyAsync(w->srcw, mms->src_W, sizeof(double) * g.NW, cudaMemcpyHostToDevice, s));
+    XC_CUDA_TRY(cudaMemcpyAsync(w->srcu, mms->src_U, sizeof(double) * g.NU, cudaMemcpyHostToDevice, s));
+    XC_CUDA_TRY(cudaMemcpyAsync(w->srcp, mms->src_P, sizeof(double) * g.NP, cudaMemcpyHostToDevice, s));
+  }
+  RhsArgs ra{coefs[0], coefs[1], coefs[2], dt, p.g0, p.D, p.h, 0.0, mms ? 1 : 0, k.pin_p, k.pin_u};
+  rhs_kernel<<<nblk(n), 256, 0, s>>>(g, ra, CF(c, FLD_Drho), CF(c, FLD_rhoWo), CF(c, FLD_rhoWoo), CF(c, FLD_rhoUo),
+                                     CF(c, FLD_rhoUoo), CF(c, FLD_MFS), w->advz, w->advx, c->dscal + SC_MFS_MEAN,
+                                     w->srcw, w->srcu, w->srcp, pin_p_val, pin_u_val, w->RR); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  // coarse coefficient fields
+  for (int l = 1; l < w->d.nv; ++l) {
+    const Geo& lg = w->d.vg[l];
+    const double* eta = l > 1 ? w->eta[l - 1] : (const double*)c->field[FLD_eta];
+    const double* etaco = l > 1 ? w->etaco[l - 1] : (const double*)c->field[FLD_etaco];
+    const double* rho = l > 1 ? w->rho[l - 1] : (const double*)c->field[FLD_rho];
+    const double* rhow = l > 1 ? w->rhow[l - 1] : (const double*)c->field[FLD_rhow];
+    const double* rhou = l > 1 ? w->rhou[l - 1] : (const double*)c->field[FLD_rhou];
+    coarsen_fields_kernel<<<grid2d(lg.Nz + 1, lg.Nx + 1, blk), blk, 0, s>>>(
+        lg.Nz, lg.Nx, eta, etaco, rho, rhow, rhou, w->eta[l], w->etaco[l], w->rho[l], w->rhow[l], w->rhou[l]); xc_count_launch();
+    XC_LAUNCH_CHECK();
+  }
+  SolveCfg cfg;
+  w->last_k = k;
+  w->have_k = true;
+  XC_TRY(setup_hier<double>(w, w->d, k, cfg, c, s));
+  scl_kernel<<<nblk(n), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], CF(c, FLD_rho), CF(c, FLD_eta), w->d.scl,
+                                     w->d.etarho); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  // initial guess: the current W, U, P
+  pack_kernel<<<nblk(n), 256, 0, s>>>(g, CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_P), w->x); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  int its = 0, refinements = 0;
+  double relres = 1.0;
+  int status = XC_OK;
+  // scaled rhs S RR -> r (double)
+  mul_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->RR, w->d.scl, w->r); xc_count_launch();
+  if (o.kind == XC_SOLVER_MIXED) {
+    if (!w->f_alloc) { XC_TRY(alloc_hier<float>(w, w->f, 30)); w->f_alloc = true; }
+    XC_TRY(setup_hier<float>(w, w->f, k, cfg, c, s));
+    // FP64 norm of the scaled rhs
+    XC_TRY(dot_self<double>(w, w->d, w->r, n, 3, s));
+    XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+    XC_CUDA_TRY(cudaStreamSynchronize(s));
+    const double bn = std::sqrt(w->hhost[3]) > 0 ? std::sqrt(w->hhost[3]) : 1.0;
+    // the FP64 operator reuses d.V[0] as residual storage
+    double* res = w->d.V;
+    double* yd = w->d.y;
+    for (int outer = 0; outer < 50; ++outer) {
+      // yd = x / scl; res = S RR - S LL S yd (FP64)
+      div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, yd); xc_count_launch();
+      XC_TRY(apply_scaled<double>(w, w->d, k, yd, w->r, res, s));
+      XC_TRY(dot_self<double>(w, w->d, res, n, 3, s));
+      XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+      XC_CUDA_TRY(cudaStreamSynchronize(s));
+      relres = std::sqrt(w->hhost[3]) / bn;
+      if (!std::isfinite(relres)) { xc_set_error("mixed solver: non-finite residual"); status = XC_NAN; break; }
+      if (relres <= o.rtol || its >= o.maxit) break;
+      ++refinements;
+      // inner FP32 solve of S LL S dy = res
+      convert_kernel<double, float><<<nblk(n), 256, 0, s>>>(n, res, w->f.w); xc_count_launch();
+      XC_CUDA_TRY(cudaMemsetAsync(w->f.y, 0, sizeof(float) * n, s));
+      // the inner rhs must not alias the Krylov buffers: keep it in f.rv..? use a dedicated copy in f.t? use f.w
+      float* frhs = w->f.w;
+      int iits = 0;
+      double irr = 1.0;
+      // fgmres uses H.w only through its rhs pointer; H.t is scratch for apply
+      XC_TRY(fgmres<float>(w, w->f, k, cfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s));
+      its += iits;
+      refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
+      XC_LAUNCH_CHECK();
+    }
+  } else {
+    div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, w->d.y); xc_count_launch();
+    status = fgmres<double>(w, w->d, k, cfg, w->r, o.rtol, o.maxit, &its, &relres, s);
+    mul_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->d.y, w->d.scl, w->x); xc_count_launch();
+    // true FP64 residual of the final iterate
+    if (status == XC_OK) {
+      XC_TRY(apply_scaled<double>(w, w->d, k, w->d.y, w->r, w->d.V, s));
+      XC_TRY(dot_self<double>(w, w->d, w->d.V, n, 3, s));
+      XC_TRY(dot_self<double>(w, w->d, w->r, n, 4, s));
+      XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
+      XC_CUDA_TRY(cudaStreamSynchronize(s));
+      relres = std::sqrt(w->hhost[3]) / (std::sqrt(w->hhost[4]) > 0 ? std::sqrt(w->hhost[4]) : 1.0);
+    }
+  }
+  unpack_kernel<<<nblk(n), 256, 0, s>>>(g, w->x, F(c, FLD_W), F(c, FLD_U), F(c, FLD_P)); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_CUDA_TRY(cudaEventRecord(w->ev1, s));
+  XC_CUDA_TRY(cudaEventSynchronize(w->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+  if (stats) {
+    stats->iterations = its;
+    stats->refinements = refinements;
+    stats->rel_residual = relres;
+    stats->converged = relres <= o.rtol;
+    stats->seconds = ms * 1e-3;
+  }
+  if (status != XC_OK) return status;
+  if (!(relres <= o.rtol)) {
+    xc_set_error("fluidmech: not converged, relative residual %.3e after %d iterations", relres, its);
+    return XC_NOT_CONVERGED;
+  }
+  return XC_OK;
+}
+
+// CUDA-event timing of one solver kernel on the last solve's operator
+int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
+  StokesWork* w = c->stokes;
+  if (!w || !w->have_k || (which == 2 && !w->f_alloc)) {
+    xc_set_error("xc_bench_kernel: run xc_fluidmech (mixed for kernel 2) first");
+    return XC_BAD_ARG;
+  }
+  const Geo& g = w->g;
+  const OpConst& k = w->last_k;
+  cudaStream_t s = c->stream;
+  const long long n = (long long)g.NW + g.NU + g.NP, nvv = (long long)g.NW + g.NU;
+  cudaEvent_t e0, e1;
+  XC_CUDA_TRY(cudaEventCreate(&e0));
+  XC_CUDA_TRY(cudaEventCreate(&e1));
+  for (int it = -1; it < iters; ++it) {
+    if (it == 0) cudaEventRecord(e0, s);
+    if (which == 1) {
+      stokes_apply_kernel<double><<<nblk(n), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], w->d.cp, w->d.scl, w->d.t,
+                                                          nullptr, w->d.w); xc_count_launch();
+    } else if (which == 2) {
+      vel_jacobi_kernel<float><<<nblk(nvv), 256, 0, s>>>(g, k, w->f.cw[0], w->f.cu[0], w->f.vx[0], w->f.vb[0],
+                                                         w->f.vx2[0], 0.7f, 0); xc_count_launch();
+    } else {
+      vel_jacobi_kernel<double><<<nblk(nvv), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], w->d.vx[0], w->d.vb[0],
+                                                          w->d.vx2[0], 0.7, 0); xc_count_launch();
+    }
+  }
+  cudaEventRecord(e1, s);
+  XC_CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  XC_LAUNCH_CHECK();
+  const double cells = (double)g.Nz * g.Nx;
+  out[0] = ms / iters;
+  // algorithmic bytes: read the unknowns and the operator's material fields
+  // (eta, etaco, rho, rhow, rhou), write the result; FP64 88 B/cell, FP32 44 B/cell
+  out[1] = (which == 2 ? 44.0 : 88.0) * cells;
+  out[2] = 52.0 * cells;            // 2 flops per stencil entry, ~26 entries per cell
+  out[3] = cells;
+  return XC_OK;
 }

@@ -351,52 +351,52 @@ int update_impl(xc_ctx* c) {
          1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0};
   volfrac_rheology_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
       Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
-      F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix));
+      F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix)); xc_count_launch();
   XC_LAUNCH_CHECK();
   interp_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, s>>>(
       Nz, Nx, p.xBC, p.zBC, p.rhom0, p.rhox0, CF(c, FLD_rho), CF(c, FLD_chi), CF(c, FLD_mu),
       CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rhow), F(c, FLD_rhou), F(c, FLD_Drhom),
       F(c, FLD_Drhox), F(c, FLD_chiw), F(c, FLD_muw), F(c, FLD_chiu), F(c, FLD_muu),
-      F(c, FLD_x_w), F(c, FLD_m_w), F(c, FLD_x_u), F(c, FLD_m_u));
+      F(c, FLD_x_w), F(c, FLD_m_w), F(c, FLD_x_u), F(c, FLD_m_u)); xc_count_launch();
   XC_LAUNCH_CHECK();
   double* rhoref = c->tmp[6];
   double* plcol = c->tmp[6] + (Nz + 8);
-  rowmean_scan_kernel<<<1, 1024, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), p.g0, p.h, p.Ptop, rhoref, plcol);
+  rowmean_scan_kernel<<<1, 1024, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
   XC_LAUNCH_CHECK();
   drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, s>>>(
       Nz, Nx, p.Ptop, rhoref, plcol, CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
-      F(c, FLD_Pt));
+      F(c, FLD_Pt)); xc_count_launch();
   XC_LAUNCH_CHECK();
   const double invh = 1.0 / p.h;
   kinematics_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
       Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
       F(c, FLD_exx), F(c, FLD_ezz), F(c, FLD_Div_V), F(c, FLD_eII), F(c, FLD_V), F(c, FLD_vx),
-      F(c, FLD_vm));
+      F(c, FLD_vm)); xc_count_launch();
   XC_LAUNCH_CHECK();
   DView etai{c->tmp[0], Nz}, etasi{c->tmp[1], Nz};
   viscblend_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
       Nz, Nx, p.L0, CF(c, FLD_etamix), CF(c, FLD_eII), CF(c, FLD_rho), CF(c, FLD_V), etai,
-      F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL));
+      F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL)); xc_count_launch();
   XC_LAUNCH_CHECK();
   XC_TRY(reduce_view(c, RED_MIN, CView{etai.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETA));
   blend_segvisc_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
       Nz, Nx, c->dscal + SC_EMAX_ETA, p.etacntr, p.D0, p.l0, CView{etai.p, Nz}, F(c, FLD_eta),
       CF(c, FLD_V), CF(c, FLD_rho), F(c, FLD_ReD), CF(c, FLD_vx), CF(c, FLD_etamix),
       CF(c, FLD_ke), CF(c, FLD_fReL), F(c, FLD_Rel), F(c, FLD_fRel), F(c, FLD_ks),
-      F(c, FLD_etat), etasi, F(c, FLD_kx), F(c, FLD_Rc));
+      F(c, FLD_etat), etasi, F(c, FLD_kx), F(c, FLD_Rc)); xc_count_launch();
   XC_LAUNCH_CHECK();
   XC_TRY(reduce_view(c, RED_MIN, CView{etasi.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETAS));
   etas_blend_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
       Nz, Nx, c->dscal + SC_EMAX_ETAS, p.etacntr, p.d0, CView{etasi.p, Nz}, F(c, FLD_etas),
-      CF(c, FLD_vx), CF(c, FLD_rho), F(c, FLD_Red));
+      CF(c, FLD_vx), CF(c, FLD_rho), F(c, FLD_Red)); xc_count_launch();
   XC_LAUNCH_CHECK();
   corner_eta_etasw_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
-      Nz, Nx, p.zBC, CF(c, FLD_eta), F(c, FLD_etaco), CF(c, FLD_etas), F(c, FLD_etasw));
+      Nz, Nx, p.zBC, CF(c, FLD_eta), F(c, FLD_etaco), CF(c, FLD_etas), F(c, FLD_etasw)); xc_count_launch();
   XC_LAUNCH_CHECK();
   stress_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
       Nz, Nx, p.D0, CF(c, FLD_etaco), CF(c, FLD_exz), F(c, FLD_txz), CF(c, FLD_eta),
       CF(c, FLD_exx), CF(c, FLD_ezz), F(c, FLD_txx), F(c, FLD_tzz), F(c, FLD_tII), CF(c, FLD_V),
-      CF(c, FLD_kx), F(c, FLD_Ra));
+      CF(c, FLD_kx), F(c, FLD_Ra)); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -409,7 +409,7 @@ int phase_velocities_impl(xc_ctx* c) {
       CF(c, FLD_bndtaperw), CF(c, FLD_x_w), CF(c, FLD_m_w), CF(c, FLD_x_u), CF(c, FLD_m_u),
       CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_xisw), CF(c, FLD_xixw), CF(c, FLD_xiew),
       CF(c, FLD_xisu), CF(c, FLD_xixu), CF(c, FLD_xieu), F(c, FLD_wx), F(c, FLD_wm),
-      F(c, FLD_Wx), F(c, FLD_Wm), F(c, FLD_Ux), F(c, FLD_Um));
+      F(c, FLD_Wx), F(c, FLD_Wm), F(c, FLD_Ux), F(c, FLD_Um)); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -422,7 +422,7 @@ int store_previous_impl(xc_ctx* c) {
       F(c, FLD_dXdt), F(c, FLD_dXdto), F(c, FLD_dXdtoo), F(c, FLD_rho), F(c, FLD_rhoo),
       F(c, FLD_rhooo), F(c, FLD_drhodt), F(c, FLD_drhodto), F(c, FLD_drhodtoo), CF(c, FLD_rhow),
       CF(c, FLD_W), F(c, FLD_rhoWo), F(c, FLD_rhoWoo), CF(c, FLD_rhou), CF(c, FLD_U),
-      F(c, FLD_rhoUo), F(c, FLD_rhoUoo));
+      F(c, FLD_rhoUo), F(c, FLD_rhoUoo)); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }

@@ -1,0 +1,158 @@
+# XcoreGPU.jl -- Julia binding of libxcore_gb300.so (include/xcore_gb300.h).
+#
+# Drop-in for the per-timestep functions of xcore.jl: the functions below keep
+# the reference's names and keyword arguments and forward to the GB300 library
+# through ccall.  The state lives on the GPU inside a context; `upload!` /
+# `download!` move a reference FluidState / PhaseState / NoiseState field by
+# field (same names, same column-major sizes, Float64, Bool for hasx/hasm).
+#
+# Usage (after `initialize!` on the host, or with `initialize_gpu!`):
+#     gpu = XcoreGPU.Context(par, grid, scales)
+#     XcoreGPU.upload!(gpu, phase, fluid, ns)
+#     for step in 1:nsteps
+#         XcoreGPU.step!(gpu, step, dt, randn(rng, Nz, Nx), randn(rng, Nz, Nx))
+#     end
+#     XcoreGPU.download!(gpu, phase, fluid, ns)
+module XcoreGPU
+
+const LIB = joinpath(@__DIR__, "..", "_build", "libxcore_gb300.so")
+
+const SCHEMES = Dict(:centr => 0, :upwd1 => 1, :quick => 2, :fromm => 3, :weno3 => 4, :weno5 => 5, :tvdim => 6)
+const BCS = Dict(:periodic => 0, :closed => 1)
+const TINTS = Dict(:be1im => 0, :bd2im => 1, :cn2si => 2, :bd2si => 3)
+
+# mirrors xc_params (field order and types must match the C struct)
+struct XcParams
+    Nz::Cint; Nx::Cint; h::Cdouble; D::Cdouble
+    rhom0::Cdouble; rhox0::Cdouble; d0::Cdouble; g0::Cdouble; etam0::Cdouble; etax0::Cdouble
+    AA::NTuple{4,Cdouble}; BB::NTuple{4,Cdouble}; CC::NTuple{4,Cdouble}
+    Xi::Cdouble; Ptop::Cdouble; alpha::Cdouble; gamma::Cdouble; CFL::Cdouble; dtmax::Cdouble
+    etacntr::Cdouble; open_sgr::Cint
+    L0::Cdouble; l0::Cdouble; L0h::Cdouble; l0h::Cdouble; D0::Cdouble; txi0::Cdouble
+    G0::Cdouble; bnd_w::Cdouble; dt0::Cdouble
+    ADVN::Cint; TINT::Cint; xBC::Cint; zBC::Cint
+    sds::Cint; top_cnv::Cint; bot_cnv::Cint; open_cnv::Cint
+end
+
+struct SolverOpts
+    kind::Cint; rtol::Cdouble; maxit::Cint; restart::Cint; inner_rtol::Cdouble; inner_maxit::Cint
+end
+
+struct SolverStats
+    iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
+end
+
+mutable struct Context
+    h::Ptr{Cvoid}
+    Nz::Int
+    Nx::Int
+end
+
+check(st) = st == 0 ? nothing :
+    error("xcore_gb300 status $st: " * unsafe_string(ccall((:xc_last_error, LIB), Cstring, ())))
+
+row(m) = (Cdouble(m[1, 1]), Cdouble(m[1, 2]), Cdouble(m[2, 1]), Cdouble(m[2, 2]))
+
+function Context(par, grid, scales; xBC = :periodic, zBC = :closed, sds = -1, top_cnv = 1, bot_cnv = 1,
+                 open_cnv = false)
+    p = XcParams(grid.Nz, grid.Nx, grid.h, par.D, par.rhom0, par.rhox0, par.d0, par.g0, par.etam0, par.etax0,
+                 row(par.AA), row(par.BB), row(par.CC), par.Xi, par.Ptop, par.alpha, par.gamma, par.CFL,
+                 par.dtmax, par.etacntr, par.open_sgr,
+                 scales.L0, scales.l0, scales.L0h, scales.l0h, scales.D0, scales.txi0, scales.G0, scales.bnd_w,
+                 scales.dt0, SCHEMES[par.ADVN], TINTS[par.TINT], BCS[xBC], BCS[zBC], sds, top_cnv, bot_cnv,
+                 open_cnv)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:xc_ctx_create, LIB), Cint, (Ref{XcParams}, Ref{Ptr{Cvoid}}), p, h))
+    ctx = Context(h[], grid.Nz, grid.Nx)
+    finalizer(c -> ccall((:xc_ctx_destroy, LIB), Cint, (Ptr{Cvoid},), c.h), ctx)
+    return ctx
+end
+
+fieldid(name::Symbol) = ccall((:xc_field_id, LIB), Cint, (Cstring,), String(name))
+
+function upload!(ctx::Context, name::Symbol, a::AbstractMatrix)
+    id = fieldid(name)
+    id < 0 && return
+    host = eltype(a) == Bool ? Matrix{UInt8}(a) : Matrix{Float64}(a)
+    check(ccall((:xc_field_upload, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), ctx.h, id, host))
+end
+
+function download!(ctx::Context, name::Symbol, a::AbstractMatrix)
+    id = fieldid(name)
+    id < 0 && return
+    if eltype(a) == Bool
+        tmp = Matrix{UInt8}(undef, size(a))
+        check(ccall((:xc_field_download, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), ctx.h, id, tmp))
+        a .= tmp .!= 0
+    else
+        check(ccall((:xc_field_download, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), ctx.h, id, a))
+    end
+    return a
+end
+
+# every matrix field of the reference structs that the library also holds
+function foreach_field(f, structs...)
+    for s in structs, name in fieldnames(typeof(s))
+        v = getfield(s, name)
+        v isa AbstractMatrix && fieldid(name) >= 0 && f(name, v)
+    end
+end
+
+upload!(ctx::Context, structs...) = foreach_field((n, v) -> upload!(ctx, n, v), structs...)
+download!(ctx::Context, structs...) = foreach_field((n, v) -> download!(ctx, n, v), structs...)
+
+coefs(a1, a2, a3, b1, b2, b3) = Cdouble[a1, a2, a3, b1, b2, b3]
+
+# ---- the reference's functions ------------------------------------------------------
+store_previous!(ctx::Context) = check(ccall((:xc_store_previous, LIB), Cint, (Ptr{Cvoid},), ctx.h))
+store_noise!(ctx::Context) = check(ccall((:xc_store_noise, LIB), Cint, (Ptr{Cvoid},), ctx.h))
+snapshot!(ctx::Context) = check(ccall((:xc_snapshot, LIB), Cint, (Ptr{Cvoid},), ctx.h))
+
+function phsevo!(ctx::Context; ADVN::Symbol = :weno5, a1, a2, a3, b1, b2, b3, dt, alpha)
+    check(ccall((:xc_phsevo, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cdouble, Cdouble),
+                ctx.h, SCHEMES[ADVN], coefs(a1, a2, a3, b1, b2, b3), dt, alpha))
+end
+
+function fluidmech!(ctx::Context; dt, a1 = 1.0, a2 = 1.0, a3 = 0.0, b1 = 1.0, b2 = 0.0, b3 = 0.0,
+                    solver::Symbol = :fgmres64, rtol = 1e-10, maxit = 500)
+    o = SolverOpts(solver === :mixed ? 1 : 0, rtol, maxit, 30, 1e-3, 40)
+    s = Ref{SolverStats}()
+    check(ccall((:xc_fluidmech, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cdouble, Ref{SolverOpts}, Ref{SolverStats}),
+                ctx.h, coefs(a1, a2, a3, b1, b2, b3), dt, o, s))
+    return s[]
+end
+
+function noise!(ctx::Context, dt; first_iter::Bool = true, re = nothing, rs = nothing)
+    pre = re === nothing ? C_NULL : pointer(Matrix{Float64}(re))
+    prs = rs === nothing ? C_NULL : pointer(Matrix{Float64}(rs))
+    check(ccall((:xc_noise, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}),
+                ctx.h, dt, first_iter, pre, prs))
+end
+
+update_phase_velocities!(ctx::Context) =
+    check(ccall((:xc_update_phase_velocities, LIB), Cint, (Ptr{Cvoid},), ctx.h))
+update!(ctx::Context) = check(ccall((:xc_update, LIB), Cint, (Ptr{Cvoid},), ctx.h))
+
+function update_dt(ctx::Context, dt_prev)
+    out = Ref{Cdouble}()
+    check(ccall((:xc_update_dt, LIB), Cint, (Ptr{Cvoid}, Cdouble, Ref{Cdouble}), ctx.h, dt_prev, out))
+    return out[]
+end
+
+function compute_resnorm(ctx::Context, dt)
+    out = zeros(Cdouble, 3)
+    check(ccall((:xc_resnorm, LIB), Cint, (Ptr{Cvoid}, Cdouble, Ptr{Cdouble}), ctx.h, dt, out))
+    return (out[1], out[2], out[3])
+end
+
+# one outer step of run! with `sweeps` Picard sweeps; returns the next dt
+function step!(ctx::Context, step::Integer, dt, re, rs; sweeps = 3, solver::Symbol = :mixed, rtol = 1e-9)
+    o = SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 1e-3, 40)
+    st = Ref{NTuple{19,UInt64}}()   # xc_step_stats storage (152 bytes; dt_next is the last word)
+    check(ccall((:xc_step, LIB), Cint,
+                (Ptr{Cvoid}, Cint, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts}, Ptr{Cvoid}),
+                ctx.h, step, dt, sweeps, Matrix{Float64}(re), Matrix{Float64}(rs), o, st))
+    return reinterpret(Float64, collect(st[]))[end]
+end
+
+end # module
