@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--roofline-kernel", type=int, default=2)
+    ap.add_argument("--profile-kernel", type=int, default=None,
+                    help="initialise, run the warm-up steps, then launch only this kernel (xc_bench_kernel "
+                         "index) 3 times inside the NVTX range 'xc_profile' and exit (for ncu)")
     return ap.parse_args()
 
 
@@ -209,6 +212,14 @@ def main():
         info = st.step(step, dt, draws[k][0], draws[k][1], sweeps=a.sweeps, **sopt)
         dt = info["dt_next"]
         k += 1
+    if a.profile_kernel is not None:
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("xc_profile")
+        st.bench_kernel(a.profile_kernel, iters=2)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        print(json.dumps({"profiled_kernel": a.profile_kernel, "N": N}), flush=True)
+        return
     stream = torch.cuda.ExternalStream(st.stream_handle())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
