@@ -203,7 +203,7 @@ def main():
             pair.append(t.numpy().T)   # F-contiguous [z, x] view of the pinned buffer
         draws.append(pair)
     st.initialize(x0, draws[0][0], draws[0][1])
-    sopt = dict(solver=a.solver, rtol=a.rtol, maxit=400, inner_rtol=1e-3, inner_maxit=40)
+    sopt = dict(solver=a.solver, rtol=a.rtol, maxit=400, inner_rtol=1e-2, inner_maxit=30)
     dt = st.scales["dt0"]
     step = 0
     k = 1

@@ -89,6 +89,16 @@ typedef struct xc_solver_opts {
   int restart;       /* FGMRES restart length */
   double inner_rtol; /* mixed: relative reduction per FP32 inner solve */
   int inner_maxit;   /* mixed: FP32 FGMRES iterations per refinement pass */
+  /* preconditioner knobs (0 selects the default) */
+  int smooth_sweeps;       /* Jacobi sweeps before and after each coarse correction (2) */
+  double omega_velocity;   /* damping of the velocity Jacobi smoother (0.7) */
+  double schur_mass;       /* weight c of the c*eta/rho term added to the Schur inverse (0.5) */
+  int schur_full_diagonal; /* 1: pressure Laplacian from the full velocity diagonal, no mass term */
+  int coarse_cells;        /* a velocity level of at most this many cells is the coarsest, a pressure
+                              level of a quarter of it (16; 256 for MMS) */
+  int coarse_sweeps;       /* Jacobi sweeps there (4 (Nz + Nx), at least 32; 200 for MMS) */
+  int small_cells;         /* levels of at most this many cells run their V-cycle in one CTA
+                              (4096; -1: none) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {
@@ -179,6 +189,12 @@ int xc_resnorm(xc_ctx* ctx, double dt, double out[3]);
    out = {sumB, sumM, sumX, sumGx, top_aX, bot_aX, top_aM, bot_aM,
           top_dX, bot_dX, top_dM, bot_dM} */
 int xc_conservation_sums(xc_ctx* ctx, double out[12]);
+/* Field statistics of record_history!                  src/history.jl:183-222
+   out[0..3]   x: min, mean, max, std (corrected)
+   out[4..21]  V, vx, vm, xie, xix, xis: min, rms, max each
+   out[22..57] Ra, Rc, ReD, Red, ks, ke, kx, eta, etamix, etae, etas, etat:
+               min, geomean (exp(mean(log(max(a, eps))))), max each */
+int xc_history_stats(xc_ctx* ctx, double out[58]);
 /* Fresh-start initialize! (src/run.jl:71-140) with the initial crystal
    fraction x (host (Nz,Nx)) in place of the MersenneTwister perturbation
    (run.jl:98-108) and the first white-noise draw re/rs. */

@@ -1241,6 +1241,22 @@ def conservation_sums(st: State, grid: Grid) -> dict:
     return out
 
 
+def history_stats(st: State) -> dict:
+    """Field statistics pushed by record_history! (src/history.jl:183-222), with
+    _rms = sqrt(mean(x^2)) and _geomean = exp(mean(log(max(x, eps)))) (history.jl:8-9)."""
+    out = {"x_min": float(st.x.min()), "x_mean": float(st.x.mean()), "x_max": float(st.x.max()),
+           "x_std": std1(st.x)}
+    for f in ("V", "vx", "vm", "xie", "xix", "xis"):
+        a = getattr(st, f)
+        out[f + "_min"], out[f + "_rms"], out[f + "_max"] = float(a.min()), math.sqrt(float((a * a).mean())), float(a.max())
+    for f in ("Ra", "Rc", "ReD", "Red", "ks", "ke", "kx", "eta", "etamix", "etae", "etas", "etat"):
+        a = getattr(st, f)
+        out[f + "_min"] = float(a.min())
+        out[f + "_gm"] = math.exp(float(np.log(np.maximum(a, EPS)).mean()))
+        out[f + "_max"] = float(a.max())
+    return out
+
+
 # ---------------------------------------------------------------------------
 # initialize! and run!  (src/run.jl:24-140, 167-277)
 # ---------------------------------------------------------------------------

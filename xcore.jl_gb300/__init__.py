@@ -70,7 +70,18 @@ class _Params(ctypes.Structure):
 
 class SolverOpts(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
-                ("restart", ctypes.c_int), ("inner_rtol", ctypes.c_double), ("inner_maxit", ctypes.c_int)]
+                ("restart", ctypes.c_int), ("inner_rtol", ctypes.c_double), ("inner_maxit", ctypes.c_int),
+                ("smooth_sweeps", ctypes.c_int), ("omega_velocity", ctypes.c_double),
+                ("schur_mass", ctypes.c_double), ("schur_full_diagonal", ctypes.c_int),
+                ("coarse_cells", ctypes.c_int), ("coarse_sweeps", ctypes.c_int), ("small_cells", ctypes.c_int)]
+
+    @classmethod
+    def make(cls, solver="fgmres64", rtol=1e-10, maxit=500, restart=30, inner_rtol=1e-4, inner_maxit=60,
+             smooth_sweeps=0, omega_velocity=0.0, schur_mass=0.0, schur_full_diagonal=False,
+             coarse_cells=0, coarse_sweeps=0, small_cells=0):
+        return cls(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit),
+                   int(smooth_sweeps), float(omega_velocity), float(schur_mass), int(bool(schur_full_diagonal)),
+                   int(coarse_cells), int(coarse_sweeps), int(small_cells))
 
 
 class SolverStats(ctypes.Structure):
@@ -119,6 +130,7 @@ def lib():
             "xc_update_dt": (ip, [vp, dp, D6]),
             "xc_resnorm": (ip, [vp, dp, D6]),
             "xc_conservation_sums": (ip, [vp, D6]),
+            "xc_history_stats": (ip, [vp, D6]),
             "xc_initialize": (ip, [vp, vp, vp, vp]),
             "xc_step": (ip, [vp, ip, dp, ip, vp, vp, ctypes.POINTER(SolverOpts), ctypes.POINTER(StepStats)]),
             "xc_fill_ghosts": (ip, [vp, ip, ip, ip, ip, ip, vp]),
@@ -366,15 +378,15 @@ class State:
         scheme = -1 if ADVN is None else SCHEMES[ADVN]
         _check(lib().xc_phsevo(self._h, scheme, c6, float(dt), float(self.par.alpha if alpha is None else alpha)))
 
-    def fluidmech(self, coefs, dt, solver="fgmres64", rtol=1e-10, maxit=500, restart=40,
-                  inner_rtol=1e-4, inner_maxit=60, mms=None):
+    def fluidmech(self, coefs, dt, solver="fgmres64", rtol=1e-10, maxit=500, restart=30,
+                  inner_rtol=1e-4, inner_maxit=60, mms=None, **knobs):
         """fluidmech!(fluid, grid, par; phase, ..., dt, a1..b3) -- src/fluidmech.jl:71-534.
 
         The sparse LU of the reference is replaced by an iterative solve;
         returns its statistics.  ``mms`` = dict of src_W/src_U/src_P/W_exact/
         U_exact/P_exact host arrays selects the manufactured-solution branch."""
         c6 = (ctypes.c_double * 6)(*coefs)
-        o = SolverOpts(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit))
+        o = SolverOpts.make(solver, rtol, maxit, restart, inner_rtol, inner_maxit, **knobs)
         st = SolverStats()
         if mms is None:
             status = lib().xc_fluidmech(self._h, c6, float(dt), ctypes.byref(o), ctypes.byref(st))
@@ -426,6 +438,17 @@ class State:
                 "top_dM", "bot_dM")
         return dict(zip(keys, out))
 
+    HISTORY_KEYS = (["x_min", "x_mean", "x_max", "x_std"]
+                    + [f"{f}_{s}" for f in ("V", "vx", "vm", "xie", "xix", "xis") for s in ("min", "rms", "max")]
+                    + [f"{f}_{s}" for f in ("Ra", "Rc", "ReD", "Red", "ks", "ke", "kx", "eta", "etamix", "etae",
+                                            "etas", "etat") for s in ("min", "gm", "max")])
+
+    def history_stats(self):
+        """Field statistics of record_history! -- src/history.jl:183-222."""
+        out = (ctypes.c_double * 58)()
+        _check(lib().xc_history_stats(self._h, out))
+        return dict(zip(self.HISTORY_KEYS, out))
+
     def initialize(self, x_init, re, rs):
         """Fresh-start initialize! -- src/run.jl:71-140 (x_init replaces the
         seeded perturbation, re/rs the first noise draw)."""
@@ -435,12 +458,12 @@ class State:
         _check(lib().xc_initialize(self._h, x.ctypes.data, a.ctypes.data, b.ctypes.data))
 
     def step(self, step, dt, re=None, rs=None, sweeps=3, solver="fgmres64", rtol=1e-10, maxit=500,
-             restart=40, inner_rtol=1e-4, inner_maxit=60):
+             restart=30, inner_rtol=1e-4, inner_maxit=60, **knobs):
         """One outer step of run! (src/run.jl:204-274) with `sweeps` Picard sweeps."""
         g = self.grid
         a = _host(re, (g.Nz, g.Nx)) if re is not None else None
         b = _host(rs, (g.Nz, g.Nx)) if rs is not None else None
-        o = SolverOpts(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit))
+        o = SolverOpts.make(solver, rtol, maxit, restart, inner_rtol, inner_maxit, **knobs)
         st = StepStats()
         _check(lib().xc_step(self._h, int(step), float(dt), int(sweeps),
                              a.ctypes.data if a is not None else None, b.ctypes.data if b is not None else None,

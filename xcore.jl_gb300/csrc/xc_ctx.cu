@@ -258,6 +258,12 @@ extern "C" int xc_conservation_sums(xc_ctx* c, double out[12]) {
   return sums_impl(c, out);
 }
 
+extern "C" int xc_history_stats(xc_ctx* c, double out[58]) {
+  XC_TRY(check_ctx(c));
+  if (!out) { xc_set_error("xc_history_stats: null output"); return XC_BAD_ARG; }
+  return history_impl(c, out);
+}
+
 static int upload_async(xc_ctx* c, int id, const void* host) {
   size_t n = (size_t)c->shape[id].rows * c->shape[id].cols * c->elem[id];
   XC_CUDA_TRY(cudaMemcpyAsync(c->field[id], host, n, cudaMemcpyHostToDevice, c->stream));

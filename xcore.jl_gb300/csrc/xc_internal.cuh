@@ -172,7 +172,7 @@ inline dim3 grid2d(int rows, int cols, dim3 blk) {
 
 // deterministic reductions (xc_reduce.cu): block partials + single-block final
 enum RedOp : int { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2, RED_SUMSQ = 3, RED_MAXABS = 4,
-                   RED_SUMSQDIFF = 5 };
+                   RED_SUMSQDIFF = 5, RED_SUMLOG = 6 /* sum of log(max(a, eps)) */ };
 // reduce a column-major view of rows x cols into dscal[slot] (device); b may be
 // null unless op == RED_SUMSQDIFF (sum of (a-b)^2)
 int reduce_view(xc_ctx* c, int op, CView a, CView b, int rows, int cols, int slot);
@@ -204,6 +204,7 @@ int snapshot_impl(xc_ctx* c);
 int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out);
 int resnorm_impl(xc_ctx* c, double dt, double out[3]);
 int sums_impl(xc_ctx* c, double out[12]);
+int history_impl(xc_ctx* c, double out[58]);
 
 int noise_plan_create(xc_ctx* c);
 void noise_plan_destroy(xc_ctx* c);

@@ -54,6 +54,7 @@ __global__ void __launch_bounds__(RB) partial_kernel(int op, CView a, CView b, c
       case RED_SUMSQ: v = v * v; break;
       case RED_MAXABS: v = fabs(v); break;
       case RED_SUMSQDIFF: { double d = v - AT(b, j, i); v = d * d; } break;
+      case RED_SUMLOG: v = log(fmax(v, XC_EPS)); break;
       default: break;
     }
     if (center) { double d = AT(a, j, i) - ctr; v = d * d; }
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(RB) final_kernel(int op, const double* partial
 
 int reduce_to(xc_ctx* c, int op, CView a, CView b, const double* center, int rows, int cols,
               double* out, cudaStream_t s, double divisor) {
-  int combine_op = (op == RED_SUMSQ || op == RED_SUMSQDIFF) ? RED_SUM : op;
+  int combine_op = (op == RED_SUMSQ || op == RED_SUMSQDIFF || op == RED_SUMLOG) ? RED_SUM : op;
   if (center) combine_op = RED_SUM;
   partial_kernel<<<RG, RB, 0, s>>>(op, a, b, center, rows, cols, c->red_partials); xc_count_launch();
   XC_LAUNCH_CHECK();

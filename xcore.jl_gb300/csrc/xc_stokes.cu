@@ -62,7 +62,8 @@ __device__ __forceinline__ int icxp(int i, int Nx) { return i == 0 ? Nx - 1 : (i
 //               5 U(j,i-1), 6 U(j+1,i-1), 7 U(j,i), 8 U(j+1,i)
 // U row planes: 0 diag, 1 U(j,il), 2 U(j,ir), 3 U(j-1,i), 4 U(j+1,i),
 //               5 W(j-1,i), 6 W(j-1,i+1), 7 W(j,i), 8 W(j,i+1)
-// Also the inertia(+drunken-sailor) part of the diagonal in plane 9.
+// Plane 9 holds the inertial part a1*rho/dt of the diagonal alone (without the
+// drunken-sailor term, which can make it negative at large dt).
 // (fluidmech.jl:194-233, 270-307)
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -101,7 +102,7 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
       c[6] = +(0.5 * C1 - c13 * P2) * invh2;
       c[7] = +(0.5 * C2 - c13 * P1) * invh2;
       c[8] = -(0.5 * C2 - c13 * P2) * invh2;
-      c[9] = iner + sail;
+      c[9] = iner;
     }
     for (int q = 0; q < 10; ++q) cw[(size_t)q * g.NW + t] = (T)c[q];
     return;
@@ -134,7 +135,7 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
       c[6] = +(0.5 * C1 - c13 * P2) * invh2;
       c[7] = +(0.5 * C2 - c13 * P1) * invh2;
       c[8] = -(0.5 * C2 - c13 * P2) * invh2;
-      c[9] = iner + sail;
+      c[9] = iner;
     }
     for (int q = 0; q < 10; ++q) cu[(size_t)q * g.NU + t] = (T)c[q];
   }
@@ -142,11 +143,13 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
 
 // y = A x over all velocity rows of a level (ghost / boundary rows included);
 // if b != null: y = b - A x.  With FULL (fine level): adds the pressure
-// gradient GG p (fluidmech.jl:343-356).
+// gradient GG p (fluidmech.jl:343-356).  The unknowns are not __restrict__:
+// the one-CTA multigrid kernels read them after other threads of the CTA wrote
+// them, which the read-only load path does not see.
 template <typename T, bool FULL>
 __device__ __forceinline__ T vel_row(const Geo& g, const OpConst& k, const T* __restrict__ cw,
-                                     const T* __restrict__ cu, const T* __restrict__ xw,
-                                     const T* __restrict__ xu, const T* __restrict__ xp, long long t) {
+                                     const T* __restrict__ cu, const T* xw, const T* xu, const T* xp,
+                                     long long t) {
   const int Nz = g.Nz, Nx = g.Nx;
   const int lw = Nz + 1, lu = Nz + 2;
   if (t < g.NW) {
@@ -269,21 +272,27 @@ __global__ void refine_update_kernel(long long n, const T* __restrict__ dy, cons
 // ---------------------------------------------------------------------------
 // velocity multigrid
 // ---------------------------------------------------------------------------
+// Each multigrid operation is a per-unknown body (`*_at`, index t) used both by
+// a grid-wide kernel and by the one-CTA kernels of the small levels.
+template <typename T>
+__device__ __forceinline__ void vel_residual_at(const Geo& g, const OpConst& k, const T* __restrict__ cw,
+                                                const T* __restrict__ cu, const T* x, const T* b, T* r,
+                                                long long t) {
+  r[t] = b[t] - vel_row<T, false>(g, k, cw, cu, x, x + g.NW, nullptr, t);
+}
 template <typename T>
 __global__ void vel_residual_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
                                     const T* __restrict__ x, const T* __restrict__ b, T* r) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)g.NW + g.NU) return;
-  r[t] = b[t] - vel_row<T, false>(g, k, cw, cu, x, x + g.NW, nullptr, t);
+  vel_residual_at<T>(g, k, cw, cu, x, b, r, t);
 }
 
 // damped Jacobi: xo = xi + w D^-1 (b - A xi); ghost / boundary rows exact
 template <typename T>
-__global__ void vel_jacobi_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
-                                  const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
-                                  int zero_init) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)g.NW + g.NU) return;
+__device__ __forceinline__ void vel_jacobi_at(const Geo& g, const OpConst& k, const T* __restrict__ cw,
+                                              const T* __restrict__ cu, const T* xi, const T* b, T* xo,
+                                              T omega, int zero_init, long long t) {
   const int Nz = g.Nz, Nx = g.Nx;
   bool exact;
   T d;
@@ -304,13 +313,19 @@ __global__ void vel_jacobi_kernel(Geo g, OpConst k, const T* __restrict__ cw, co
   T res = b[t] - vel_row<T, false>(g, k, cw, cu, xi, xi + g.NW, nullptr, t);
   xo[t] = xi[t] + (exact ? (T)1 : omega) * res / d;
 }
+template <typename T>
+__global__ void vel_jacobi_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
+                                  const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
+                                  int zero_init) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)g.NW + g.NU) return;
+  vel_jacobi_at<T>(g, k, cw, cu, xi, b, xo, omega, zero_init, t);
+}
 
 // restriction of the interior-row residual (full weighting / 4 of the
 // bilinear prolongation); coarse ghost / boundary rows get zero
 template <typename T>
-__global__ void vel_restrict_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)c.NW + c.NU) return;
+__device__ __forceinline__ void vel_restrict_at(const Geo& f, const Geo& c, const T* r, T* bc, long long t) {
   const int lwf = f.Nz + 1, luf = f.Nz + 2;
   const T* rw = r;
   const T* ru = r + f.NW;
@@ -355,12 +370,17 @@ __global__ void vel_restrict_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc
   }
   bc[c.NW + t] = acc;
 }
+template <typename T>
+__global__ void vel_restrict_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)c.NW + c.NU) return;
+  vel_restrict_at<T>(f, c, r, bc, t);
+}
 
 // x_f += P x_c (bilinear; ghost rows of U follow the reflection rule)
 template <typename T>
-__global__ void vel_prolong_kernel(Geo f, Geo c, OpConst k, const T* __restrict__ xc, T* xf) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)f.NW + f.NU) return;
+__device__ __forceinline__ void vel_prolong_at(const Geo& f, const Geo& c, const OpConst& k, const T* xc, T* xf,
+                                               long long t) {
   const int lwc = c.Nz + 1, luc = c.Nz + 2;
   const T* cw = xc;
   const T* cu = xc + c.NW;
@@ -402,6 +422,12 @@ __global__ void vel_prolong_kernel(Geo f, Geo c, OpConst k, const T* __restrict_
   else v = interior(j);
   xf[t] += v;
 }
+template <typename T>
+__global__ void vel_prolong_kernel(Geo f, Geo c, OpConst k, const T* __restrict__ xc, T* xf) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)f.NW + f.NU) return;
+  vel_prolong_at<T>(f, c, k, xc, xf, t);
+}
 
 // coarse coefficient fields: eta (avg4), etaco (injection), rho (avg4),
 // rhow / rhou (avg of the two fine faces of the coarse face)
@@ -429,10 +455,27 @@ __global__ void coarsen_fields_kernel(int Nzc, int Nxc, const double* __restrict
   }
 }
 
-// many damped-Jacobi sweeps on the coarsest velocity level in one CTA
+// sum of v over the CTA (all threads get it); red holds 32 doubles
+__device__ __forceinline__ double cta_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0;
+  for (int q = 0; q < nw; ++q) s += red[q];
+  return s;
+}
+
+// many damped-Jacobi sweeps on the coarsest velocity level, by one whole CTA.
+// With free slip at top and bottom (top_cnv = bot_cnv = -1) and periodic x, a
+// uniform U shift is a null mode of the viscous rows; where inertia does not
+// lift it (the inertia-free limit of the manufactured solution) the sweeps
+// would let that mode grow with the sweep count, so it is removed from the
+// coarse correction and left to the pinned fine level and the Krylov method.
 template <typename T>
-__global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
-                                  T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+__device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const T* __restrict__ cw, const T* __restrict__ cu,
+                               T* x, T* x2, const T* b, int sweeps, T omega) {
   const long long n = (long long)g.NW + g.NU;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
   __syncthreads();
@@ -449,7 +492,7 @@ __global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, co
       } else {
         long long u = t - g.NW;
         int j = (int)(u % (g.Nz + 2));
-        exact = (j == 0 || j == g.Nz + 1);
+        exact = (j == 0 || j == g.Nz + 1) || (k.mms && (int)u == k.pin_u);
         d = cu[u];
       }
       T res = b[t] - vel_row<T, false>(g, k, cw, cu, a, a + g.NW, nullptr, t);
@@ -460,6 +503,29 @@ __global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, co
   }
   if (a != x)
     for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = a[t];
+  __syncthreads();
+  if (k.top_cnv == -1 && k.bot_cnv == -1 && !k.mms) {
+    __shared__ double red[32];
+    double si = 0, sd = 0, sx = 0;
+    for (long long u = threadIdx.x; u < g.NU; u += blockDim.x) {
+      int j = (int)(u % (g.Nz + 2));
+      if (j >= 1 && j <= g.Nz) { si += (double)cu[9 * (size_t)g.NU + u]; sd += (double)cu[u]; }
+      sx += (double)x[g.NW + u];
+    }
+    si = cta_sum(si, red);
+    sd = cta_sum(sd, red);
+    sx = cta_sum(sx, red);
+    if (si <= 1e-6 * sd) {
+      const T m = (T)(sx / (double)g.NU);
+      for (long long u = threadIdx.x; u < g.NU; u += blockDim.x) x[g.NW + u] -= m;
+    }
+    __syncthreads();
+  }
+}
+template <typename T>
+__global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
+                                  T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+  vel_coarse_cta<T>(g, k, cw, cu, x, x2, b, sweeps, omega);
 }
 
 // ---------------------------------------------------------------------------
@@ -469,7 +535,7 @@ __global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, co
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ T p_apply_at(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
-                                        int pin, T dpin, const T* __restrict__ p, int j, int i, T* diag) {
+                                        int pin, T dpin, const T* p, int j, int i, T* diag) {
   size_t c = (size_t)i * Nz + j;
   int il = i == 0 ? Nx - 1 : i - 1, ir = i == Nx - 1 ? 0 : i + 1;
   T kl = kx[c], kr = kx[(size_t)ir * Nz + j];
@@ -485,46 +551,59 @@ __device__ __forceinline__ T p_apply_at(int Nz, int Nx, const T* __restrict__ kx
 }
 
 template <typename T>
+__device__ __forceinline__ void p_jacobi_at(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
+                                            int pin, T dpin, const T* xi, const T* b, T* xo, T omega,
+                                            int zero_init, int t) {
+  int j = t % Nz, i = t / Nz;
+  T d;
+  if (zero_init) {
+    p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, b, j, i, &d);   // only the diagonal is used
+    xo[t] = d > (T)0 ? omega * b[t] / d : (T)0;
+    return;
+  }
+  T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, j, i, &d);
+  xo[t] = d > (T)0 ? xi[t] + omega * (b[t] - ax) / d : (T)0;
+}
+template <typename T>
 __global__ void p_jacobi_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
                                 T dpin, const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
                                 int zero_init) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= Nz * Nx) return;
-  int j = t % Nz, i = t / Nz;
-  T d;
-  if (zero_init) {
-    p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, b, j, i, &d);   // only the diagonal is used
-    xo[t] = omega * b[t] / d;
-    return;
-  }
-  T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, j, i, &d);
-  xo[t] = xi[t] + omega * (b[t] - ax) / d;
+  p_jacobi_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, b, xo, omega, zero_init, t);
 }
 
+template <typename T>
+__device__ __forceinline__ void p_residual_at(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
+                                              int pin, T dpin, const T* x, const T* b, T* r, int t) {
+  T d;
+  r[t] = b[t] - p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, x, t % Nz, t / Nz, &d);
+}
 template <typename T>
 __global__ void p_residual_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
                                   T dpin, const T* __restrict__ x, const T* __restrict__ b, T* r) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= Nz * Nx) return;
-  T d;
-  r[t] = b[t] - p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, x, t % Nz, t / Nz, &d);
+  p_residual_at<T>(Nz, Nx, kx, kz, pin, dpin, x, b, r, t);
 }
 
 template <typename T>
-__global__ void p_restrict_kernel(int Nzc, int Nxc, const T* __restrict__ r, T* bc) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= Nzc * Nxc) return;
+__device__ __forceinline__ void p_restrict_at(int Nzc, int Nxc, const T* r, T* bc, int t) {
   int J = t % Nzc, I = t / Nzc;
   const int Nz = 2 * Nzc;
   size_t a = (size_t)(2 * I) * Nz + 2 * J, b = (size_t)(2 * I + 1) * Nz + 2 * J;
   bc[t] = (T)0.25 * (r[a] + r[a + 1] + r[b] + r[b + 1]);
 }
+template <typename T>
+__global__ void p_restrict_kernel(int Nzc, int Nxc, const T* __restrict__ r, T* bc) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nzc * Nxc) return;
+  p_restrict_at<T>(Nzc, Nxc, r, bc, t);
+}
 
 template <typename T>
-__global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* xf) {
-  const int Nz = 2 * Nzc, Nx = 2 * Nxc;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= Nz * Nx) return;
+__device__ __forceinline__ void p_prolong_at(int Nzc, int Nxc, const T* xc, T* xf, int t) {
+  const int Nz = 2 * Nzc;
   int j = t % Nz, i = t / Nz;
   int J = j / 2, I = i / 2;
   int Jn = (j % 2 == 0) ? (J > 0 ? J - 1 : 0) : (J < Nzc - 1 ? J + 1 : Nzc - 1);
@@ -532,6 +611,12 @@ __global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* 
   T v = (T)9 * xc[(size_t)I * Nzc + J] + (T)3 * xc[(size_t)I * Nzc + Jn] + (T)3 * xc[(size_t)In * Nzc + J] +
         xc[(size_t)In * Nzc + Jn];
   xf[t] += v / (T)16;
+}
+template <typename T>
+__global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* xf) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * Nzc * Nxc) return;
+  p_prolong_at<T>(Nzc, Nxc, xc, xf, t);
 }
 
 template <typename T>
@@ -548,8 +633,8 @@ __global__ void p_coarsen_kernel(int Nzc, int Nxc, const T* __restrict__ kx, con
 }
 
 template <typename T>
-__global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
-                                T dpin, T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+__device__ void p_coarse_cta(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
+                             T dpin, T* x, T* x2, const T* b, int sweeps, T omega) {
   const int n = Nz * Nx;
   for (int t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
   __syncthreads();
@@ -559,13 +644,156 @@ __global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const 
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
       T d;
       T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, a, t % Nz, t / Nz, &d);
-      o[t] = a[t] + omega * (b[t] - ax) / d;
+      o[t] = d > (T)0 ? a[t] + omega * (b[t] - ax) / d : (T)0;
     }
     __syncthreads();
     T* tmp = a; a = o; o = tmp;
   }
   if (a != x)
     for (int t = threadIdx.x; t < n; t += blockDim.x) x[t] = a[t];
+  __syncthreads();
+}
+template <typename T>
+__global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
+                                T dpin, T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+  p_coarse_cta<T>(Nz, Nx, kx, kz, pin, dpin, x, x2, b, sweeps, omega);
+}
+
+// ---------------------------------------------------------------------------
+// Small levels in one CTA.  Below about 64x64 cells a level holds a few
+// thousand unknowns, and each phase of its V-cycle (a smoothing sweep, the
+// residual, the restriction, the prolongation) is bound by launch latency, not
+// by bandwidth.  These kernels run the V-cycle from level l0 down to the
+// coarsest level lc and back up inside one CTA, with CTA barriers between the
+// phases; the level data stays in L1/L2.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct VelLevels {
+  Geo g[kMaxLevels];
+  const T* cw[kMaxLevels];
+  const T* cu[kMaxLevels];
+  T* x[kMaxLevels];
+  T* x2[kMaxLevels];
+  T* b[kMaxLevels];
+  T* r[kMaxLevels];
+};
+
+// `sweeps` damped-Jacobi sweeps (the first from zero when from_zero), x holds the result
+template <typename T>
+__device__ void vel_smooth_cta(const Geo& g, const OpConst& k, const T* __restrict__ cw, const T* __restrict__ cu,
+                               T* x, T* x2, const T* b, T om, int sweeps, bool from_zero) {
+  const long long n = (long long)g.NW + g.NU;
+  T* a = x;
+  T* o = x2;
+  int q = 0;
+  if (from_zero) {
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, cw, cu, x, b, x, om, 1, t);
+    __syncthreads();
+    q = 1;
+  }
+  for (; q < sweeps; ++q) {
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, cw, cu, a, b, o, om, 0, t);
+    __syncthreads();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != x) {
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = a[t];
+    __syncthreads();
+  }
+}
+
+// the MMS pins (k.mms) belong to level 0 only
+__host__ __device__ __forceinline__ OpConst level_const(const OpConst& k, int l) {
+  OpConst c = k;
+  if (l > 0) c.mms = 0;
+  return c;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> L, OpConst kf, int l0, int lc, int nu,
+                                                                T om, int csweeps) {
+  for (int l = l0; l < lc; ++l) {
+    const OpConst k = level_const(kf, l);
+    const Geo& g = L.g[l];
+    const Geo& c = L.g[l + 1];
+    vel_smooth_cta<T>(g, k, L.cw[l], L.cu[l], L.x[l], L.x2[l], L.b[l], om, nu, true);
+    const long long n = (long long)g.NW + g.NU;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x)
+      vel_residual_at<T>(g, k, L.cw[l], L.cu[l], L.x[l], L.b[l], L.r[l], t);
+    __syncthreads();
+    const long long nc = (long long)c.NW + c.NU;
+    for (long long t = threadIdx.x; t < nc; t += blockDim.x) vel_restrict_at<T>(g, c, L.r[l], L.b[l + 1], t);
+    __syncthreads();
+  }
+  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.cw[lc], L.cu[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om);
+  for (int l = lc - 1; l >= l0; --l) {
+    const OpConst k = level_const(kf, l);
+    const Geo& g = L.g[l];
+    const long long n = (long long)g.NW + g.NU;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_prolong_at<T>(g, L.g[l + 1], k, L.x[l + 1], L.x[l], t);
+    __syncthreads();
+    vel_smooth_cta<T>(g, k, L.cw[l], L.cu[l], L.x[l], L.x2[l], L.b[l], om, nu, false);
+  }
+}
+
+template <typename T>
+struct PLevels {
+  int Nz[kMaxLevels], Nx[kMaxLevels], pin[kMaxLevels];
+  T dpin[kMaxLevels];
+  const T* kx[kMaxLevels];
+  const T* kz[kMaxLevels];
+  T* x[kMaxLevels];
+  T* x2[kMaxLevels];
+  T* b[kMaxLevels];
+  T* r[kMaxLevels];
+};
+
+template <typename T>
+__device__ void p_smooth_cta(const PLevels<T>& L, int l, T om, int sweeps, bool from_zero) {
+  const int Nz = L.Nz[l], Nx = L.Nx[l], n = Nz * Nx;
+  T* x = L.x[l];
+  T* a = x;
+  T* o = L.x2[l];
+  int q = 0;
+  if (from_zero) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x)
+      p_jacobi_at<T>(Nz, Nx, L.kx[l], L.kz[l], L.pin[l], L.dpin[l], x, L.b[l], x, om, 1, t);
+    __syncthreads();
+    q = 1;
+  }
+  for (; q < sweeps; ++q) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x)
+      p_jacobi_at<T>(Nz, Nx, L.kx[l], L.kz[l], L.pin[l], L.dpin[l], a, L.b[l], o, om, 0, t);
+    __syncthreads();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != x) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) x[t] = a[t];
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> L, int l0, int lc, int nu, T om,
+                                                              int csweeps) {
+  for (int l = l0; l < lc; ++l) {
+    const int Nz = L.Nz[l], Nx = L.Nx[l], n = Nz * Nx;
+    p_smooth_cta<T>(L, l, om, nu, true);
+    for (int t = threadIdx.x; t < n; t += blockDim.x)
+      p_residual_at<T>(Nz, Nx, L.kx[l], L.kz[l], L.pin[l], L.dpin[l], L.x[l], L.b[l], L.r[l], t);
+    __syncthreads();
+    const int nc = L.Nz[l + 1] * L.Nx[l + 1];
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) p_restrict_at<T>(L.Nz[l + 1], L.Nx[l + 1], L.r[l], L.b[l + 1], t);
+    __syncthreads();
+  }
+  p_coarse_cta<T>(L.Nz[lc], L.Nx[lc], L.kx[lc], L.kz[lc], L.pin[lc], L.dpin[lc], L.x[lc], L.x2[lc], L.b[lc],
+                  csweeps, om);
+  for (int l = lc - 1; l >= l0; --l) {
+    const int n = L.Nz[l] * L.Nx[l];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) p_prolong_at<T>(L.Nz[l + 1], L.Nx[l + 1], L.x[l + 1], L.x[l], t);
+    __syncthreads();
+    p_smooth_cta<T>(L, l, om, nu, false);
+  }
 }
 
 // fine-level pressure coefficients from the velocity diagonal (plane 0: full,
@@ -577,22 +805,28 @@ __global__ void p_kcoef_kernel(Geo g, const double* __restrict__ rhow, const dou
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx;
   const double ih2 = g.invh * g.invh;
+  // k = rho_face / (h^2 a) with a the chosen diagonal; 0 where the inertial
+  // diagonal is negligible against the full one (a Stokes limit, e.g. MMS)
+  auto kval = [&](double rho_f, double a, double full) -> T {
+    if (!(a > 1e-12 * fabs(full))) return (T)0;
+    return (T)(rho_f * ih2 / a);
+  };
   if (t < Nz * Nx) {
     int j = t % Nz, i = t / Nz;
     // face left of cell (j,i) is U(j+1, i)
-    double a = (double)cu[(size_t)plane * g.NU + (size_t)i * (Nz + 2) + j + 1];
-    kx[t] = (T)(rhou[(size_t)i * Nz + j] * ih2 / a);
+    size_t o = (size_t)i * (Nz + 2) + j + 1;
+    kx[t] = kval(rhou[(size_t)i * Nz + j], (double)cu[(size_t)plane * g.NU + o], (double)cu[o]);
     if (i == Nx - 1) {    // right face of the last column is U(j+1, Nx)
-      double ar = (double)cu[(size_t)plane * g.NU + (size_t)Nx * (Nz + 2) + j + 1];
-      kr[j] = (T)(rhou[(size_t)Nx * Nz + j] * ih2 / ar);
+      size_t orr = (size_t)Nx * (Nz + 2) + j + 1;
+      kr[j] = kval(rhou[(size_t)Nx * Nz + j], (double)cu[(size_t)plane * g.NU + orr], (double)cu[orr]);
     }
   }
   if (t < (Nz + 1) * Nx) {
     int j = t % (Nz + 1), i = t / (Nz + 1);
     T v = 0;
     if (j >= 1 && j <= Nz - 1) {
-      double a = (double)cw[(size_t)plane * g.NW + (size_t)(i + 1) * (Nz + 1) + j];
-      v = (T)(rhow[(size_t)i * (Nz + 1) + j] * ih2 / a);
+      size_t o = (size_t)(i + 1) * (Nz + 1) + j;
+      v = kval(rhow[(size_t)i * (Nz + 1) + j], (double)cw[(size_t)plane * g.NW + o], (double)cw[o]);
     }
     kz[t] = v;
   }
@@ -665,26 +899,53 @@ __global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, T* rv) {
 // Krylov vector kernels
 // ---------------------------------------------------------------------------
 constexpr int KB = 256;
-constexpr int KG = 2 * kNumSMs;
+constexpr int KG = 6 * kNumSMs;   // one wave of the 8-accumulator multidot (40 registers): 1536 threads per SM
 
-// partial dot products of w with V[0..m) -> part[blk * m + k]
-template <typename T>
+// partial dot products of w with V[0..m) -> part[blk * m + k], m <= MAXK.
+// One pass: w is read once, every thread keeps m running sums in the working
+// precision T (FP32 for the inner solver -- FP64 arithmetic is 58x slower on
+// GB300), then warps and the CTA combine them in FP64.  MAXK (8, 16, 32) is
+// picked by the host so that few accumulators keep the occupancy high; the
+// grid-stride loop takes two elements per step for more loads in flight.
+template <typename T, int MAXK>
 __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
                                                       const T* __restrict__ w, double* part) {
-  __shared__ double sh[KB];
-  for (int k = 0; k < m; ++k) {
-    double acc = 0;
-    const T* v = V + (size_t)k * ldv;
-    for (long long t = blockIdx.x * (long long)KB + threadIdx.x; t < n; t += (long long)KG * KB)
-      acc += (double)v[t] * (double)w[t];
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = KB / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-      __syncthreads();
+  __shared__ double sh[KB / 32][MAXK];
+  T acc[MAXK];
+#pragma unroll
+  for (int k = 0; k < MAXK; ++k) acc[k] = (T)0;
+  const long long stride = (long long)KG * KB;
+  long long t = blockIdx.x * (long long)KB + threadIdx.x;
+  for (; t + stride < n; t += 2 * stride) {
+    const T w0 = w[t], w1 = w[t + stride];
+#pragma unroll
+    for (int k = 0; k < MAXK; ++k)
+      if (k < m) {
+        const T* vk = V + (size_t)k * ldv;
+        acc[k] += vk[t] * w0;
+        acc[k] += vk[t + stride] * w1;
+      }
+  }
+  if (t < n) {
+    const T w0 = w[t];
+#pragma unroll
+    for (int k = 0; k < MAXK; ++k)
+      if (k < m) acc[k] += V[(size_t)k * ldv + t] * w0;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < MAXK; ++k) {
+    if (k < m) {
+      double v = (double)acc[k];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) sh[warp][k] = v;
     }
-    if (threadIdx.x == 0) part[(size_t)blockIdx.x * m + k] = sh[0];
-    __syncthreads();
+  }
+  __syncthreads();
+  if (threadIdx.x < m) {
+    double s = 0;
+    for (int q = 0; q < KB / 32; ++q) s += sh[q][threadIdx.x];
+    part[(size_t)blockIdx.x * m + threadIdx.x] = s;
   }
 }
 __global__ void multidot_final_kernel(int m, const double* __restrict__ part, double* out) {
@@ -700,33 +961,62 @@ __global__ void multidot_final_kernel(int m, const double* __restrict__ part, do
   }
   if (threadIdx.x == 0) out[k] = sh[0];
 }
+// ||v||^2 from one partial column -> *nrm2, and 1/||v|| (1 for a zero norm) -> *inv
+__global__ void norm_final_kernel(const double* __restrict__ part, double* nrm2, double* inv) {
+  __shared__ double sh[KB];
+  double acc = 0;
+  for (int b = threadIdx.x; b < KG; b += KB) acc += part[b];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = KB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *nrm2 = sh[0];
+    *inv = sh[0] > 0.0 ? 1.0 / sqrt(sh[0]) : 1.0;
+  }
+}
 // w -= sum_k h[k] V[k]
 template <typename T>
 __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
                                  const double* __restrict__ h, T* w) {
+  __shared__ T hs[32];
+  if (threadIdx.x < m) hs[threadIdx.x] = (T)h[threadIdx.x];
+  __syncthreads();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  double s = (double)w[t];
-  for (int k = 0; k < m; ++k) s -= h[k] * (double)V[(size_t)k * ldv + t];
-  w[t] = (T)s;
+  T s = w[t];
+  for (int k = 0; k < m; ++k) s -= hs[k] * V[(size_t)k * ldv + t];
+  w[t] = s;
 }
 // x += sum_k y[k] Z[k]
 template <typename T>
 __global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long long ldz,
                                const double* __restrict__ y, T* x) {
+  __shared__ T ys[64];
+  if (threadIdx.x < m) ys[threadIdx.x] = (T)y[threadIdx.x];
+  __syncthreads();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  double s = (double)x[t];
-  for (int k = 0; k < m; ++k) s += y[k] * (double)Z[(size_t)k * ldz + t];
-  x[t] = (T)s;
+  T s = x[t];
+  for (int k = 0; k < m; ++k) s += ys[k] * Z[(size_t)k * ldz + t];
+  x[t] = s;
 }
+// v = w * inv with a scale factor computed once elsewhere (a per-CTA FP64
+// reciprocal in front of a barrier stalls every CTA of the grid)
 template <typename T>
-__global__ void scale_kernel(long long n, const double* __restrict__ alpha_inv, const T* __restrict__ w,
-                             T* v) {
+__global__ void scale_kernel(long long n, const double* __restrict__ inv, const T* __restrict__ w, T* v) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t < n) v[t] = (T)((double)w[t] / *alpha_inv);
+  if (t < n) v[t] = w[t] * (T)__ldg(inv);
 }
-__global__ void sqrt_kernel(double* a) { *a = sqrt(*a); }
+// v *= inv (inv = 1/||v|| from norm_final_kernel; 1 on a zero norm, which the
+// host reports as breakdown)
+template <typename T>
+__global__ void normalize_kernel(long long n, const double* __restrict__ inv, T* v) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) v[t] = v[t] * (T)__ldg(inv);
+}
 
 // ---------------------------------------------------------------------------
 // RHS assembly
@@ -899,6 +1189,10 @@ struct Hier {
   T* rv;          // preconditioner scratch (velocity part, physical)
   T* rp;          // preconditioner scratch (pressure, physical full layout)
   T* rin;         // interior pressure rhs
+  // one captured graph per Arnoldi index; rebuilt when the key changes
+  cudaGraphExec_t gexec[kMaxRestart];
+  long long gnodes[kMaxRestart];
+  unsigned long long gkey;
 };
 
 struct StokesWork {
@@ -945,7 +1239,7 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
     XC_CUDA_TRY(cudaMalloc(&H.vb[H.nv], sizeof(T) * nvv));
     XC_CUDA_TRY(cudaMalloc(&H.vr[H.nv], sizeof(T) * nvv));
     H.nv++;
-    if (Nz % 2 || Nx % 2 || Nz / 2 < 4 || Nx / 2 < 4 || (long long)Nz * Nx <= 256) break;
+    if (Nz % 2 || Nx % 2 || Nz / 2 < 4 || Nx / 2 < 4) break;
     Nz /= 2; Nx /= 2; h *= 2;
   }
   // pressure levels
@@ -962,7 +1256,7 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
     XC_CUDA_TRY(cudaMalloc(&H.pb[L], sizeof(T) * Nz * Nx));
     XC_CUDA_TRY(cudaMalloc(&H.pr[L], sizeof(T) * Nz * Nx));
     H.np_lv++;
-    if (Nz % 2 || Nx % 2 || Nz / 2 < 2 || Nx / 2 < 2 || (long long)Nz * Nx <= 64) break;
+    if (Nz % 2 || Nx % 2 || Nz / 2 < 2 || Nx / 2 < 2) break;
     Nz /= 2; Nx /= 2; pz /= 2; px /= 2;
   }
   XC_CUDA_TRY(cudaMalloc(&H.kr, sizeof(T) * g.Nz));
@@ -982,6 +1276,8 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
 
 template <typename T>
 void free_hier(Hier<T>& H) {
+  for (int q = 0; q < kMaxRestart; ++q)
+    if (H.gexec[q]) { cudaGraphExecDestroy(H.gexec[q]); H.gexec[q] = nullptr; }
   for (int l = 0; l < H.nv; ++l) {
     cudaFree(H.cw[l]); cudaFree(H.cu[l]); cudaFree(H.vx[l]); cudaFree(H.vx2[l]); cudaFree(H.vb[l]); cudaFree(H.vr[l]);
   }
@@ -996,20 +1292,60 @@ void free_hier(Hier<T>& H) {
 struct SolveCfg {
   double omega_v = 0.7, omega_p = 0.8;
   int nu = 2;
-  int coarse_sweeps = 200;
-  double cmass = 0.0;     // eta/rho mass term in the Schur approximation
-  int kplane = 0;         // 0: full velocity diagonal, 9: inertia-only
+  int coarse_sweeps = 0;   // 0: 4 * (Nz + Nx) of the coarsest level, at least 32
+  int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
+                           // solved by Jacobi sweeps
+  int small_cells = 4096;  // levels of at most this many cells run in one CTA
+  // Schur approximation (Cahouet-Chabard): S^-1 ~ L_in^-1 + cmass * eta/rho with
+  // L_in = DM diag(a1 rho/dt)^-1 GG (kplane 9); kplane 0 builds L from the full
+  // velocity diagonal instead (cmass then defaults to 0)
+  double cmass = 0.5;
+  int kplane = 9;
 };
+
+// Jacobi sweeps on a coarsest level of Nz x Nx cells: a few times the grid's
+// diameter, enough for the smoothing to reach across the level
+static int coarse_sweeps(const SolveCfg& cfg, int Nz, int Nx) {
+  if (cfg.coarse_sweeps > 0) return cfg.coarse_sweeps;
+  return 4 * (Nz + Nx) > 32 ? 4 * (Nz + Nx) : 32;
+}
+
+template <typename T>
+static bool vel_coarsest(const Hier<T>& H, const SolveCfg& cfg, int l) {
+  return l == H.nv - 1 || (long long)H.vg[l].Nz * H.vg[l].Nx <= cfg.coarse_cells;
+}
+template <typename T>
+static bool p_coarsest(const Hier<T>& H, const SolveCfg& cfg, int l) {
+  return l == H.np_lv - 1 || 4LL * H.pNz[l] * H.pNx[l] <= cfg.coarse_cells;
+}
+
+// one CTA runs the coarsest level; fewer threads make each sweep's barrier cheaper
+static int coarse_threads(long long n) { return n > 512 ? 1024 : (n > 128 ? 256 : 128); }
 
 // ---- velocity V-cycle on level l: solve A x = vb[l] approximately (x := vx[l])
 template <typename T>
-int vcycle_vel(Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int l, cudaStream_t s) {
+int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaStream_t s) {
   const Geo& g = H.vg[l];
   const long long n = (long long)g.NW + g.NU;
   const T om = (T)cfg.omega_v;
-  if (l == H.nv - 1) {
-    vel_coarse_kernel<T><<<1, 1024, 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vx2[l], H.vb[l],
-                                            cfg.coarse_sweeps, om); xc_count_launch();
+  const OpConst k = level_const(kf, l);
+  if (!vel_coarsest(H, cfg, l) && (long long)g.Nz * g.Nx <= cfg.small_cells) {
+    int lc = l;
+    while (!vel_coarsest(H, cfg, lc)) ++lc;
+    VelLevels<T> L;
+    for (int q = 0; q <= lc; ++q) {
+      L.g[q] = H.vg[q]; L.cw[q] = H.cw[q]; L.cu[q] = H.cu[q];
+      L.x[q] = H.vx[q]; L.x2[q] = H.vx2[q]; L.b[q] = H.vb[q]; L.r[q] = H.vr[q];
+    }
+    vel_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, kf, l, lc, cfg.nu, om,
+                                                              coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx));
+    xc_count_launch();
+    XC_LAUNCH_CHECK();
+    return XC_OK;
+  }
+  if (vel_coarsest(H, cfg, l)) {
+    vel_coarse_kernel<T><<<1, coarse_threads(n), 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vx2[l], H.vb[l],
+                                                        coarse_sweeps(cfg, g.Nz, g.Nx), om); xc_count_launch();
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
@@ -1026,7 +1362,7 @@ int vcycle_vel(Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int l, cudaStr
   const Geo& c = H.vg[l + 1];
   vel_restrict_kernel<T><<<nblk((long long)c.NW + c.NU), 256, 0, s>>>(g, c, H.vr[l], H.vb[l + 1]); xc_count_launch();
   XC_LAUNCH_CHECK();
-  XC_TRY(vcycle_vel<T>(H, k, cfg, l + 1, s));
+  XC_TRY(vcycle_vel<T>(H, kf, cfg, l + 1, s));
   vel_prolong_kernel<T><<<nblk(n), 256, 0, s>>>(g, c, k, H.vx[l + 1], H.vx[l]); xc_count_launch();
   a = H.vx[l];
   o = H.vx2[l];
@@ -1043,9 +1379,25 @@ template <typename T>
 int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
   const int Nz = H.pNz[l], Nx = H.pNx[l], n = Nz * Nx;
   const T om = (T)cfg.omega_p;
-  if (l == H.np_lv - 1) {
-    p_coarse_kernel<T><<<1, 1024, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.px2[l],
-                                          H.pb[l], cfg.coarse_sweeps, om); xc_count_launch();
+  if (!p_coarsest(H, cfg, l) && (long long)n <= cfg.small_cells) {
+    int lc = l;
+    while (!p_coarsest(H, cfg, lc)) ++lc;
+    PLevels<T> L;
+    for (int q = 0; q <= lc; ++q) {
+      L.Nz[q] = H.pNz[q]; L.Nx[q] = H.pNx[q]; L.pin[q] = H.ppin[q]; L.dpin[q] = H.pdpin[q];
+      L.kx[q] = H.kx[q]; L.kz[q] = H.kz[q];
+      L.x[q] = H.px[q]; L.x2[q] = H.px2[q]; L.b[q] = H.pb[q]; L.r[q] = H.pr[q];
+    }
+    p_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, l, lc, cfg.nu, om,
+                                                            coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]));
+    xc_count_launch();
+    XC_LAUNCH_CHECK();
+    return XC_OK;
+  }
+  if (p_coarsest(H, cfg, l)) {
+    p_coarse_kernel<T><<<1, coarse_threads(n), 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l],
+                                                      H.px2[l], H.pb[l], coarse_sweeps(cfg, Nz, Nx), om);
+    xc_count_launch();
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
@@ -1118,12 +1470,91 @@ int apply_scaled(StokesWork* w, Hier<T>& H, const OpConst& k, const T* v, const 
   return XC_OK;
 }
 
-// ||v||^2 -> hdev[slot] (device), deterministic
+// partial dots of wv with V[0..m), accumulator count chosen from m
+template <typename T>
+void launch_multidot(long long n, int m, const T* V, long long ldv, const T* wv, double* part, cudaStream_t s) {
+  if (m <= 8) multidot_kernel<T, 8><<<KG, KB, 0, s>>>(n, m, V, ldv, wv, part);
+  else if (m <= 16) multidot_kernel<T, 16><<<KG, KB, 0, s>>>(n, m, V, ldv, wv, part);
+  else multidot_kernel<T, 32><<<KG, KB, 0, s>>>(n, m, V, ldv, wv, part);
+  xc_count_launch();
+}
+
+// ||v||^2 -> hdev[slot] (device), deterministic; 1/||v|| -> hdev[6]
 template <typename T>
 int dot_self(StokesWork* w, Hier<T>& H, const T* v, long long n, int slot, cudaStream_t s) {
-  multidot_kernel<T><<<KG, KB, 0, s>>>(n, 1, v, n, v, w->part); xc_count_launch();
-  multidot_final_kernel<<<1, KB, 0, s>>>(1, w->part, w->hdev + slot); xc_count_launch();
+  launch_multidot<T>(n, 1, v, n, v, w->part, s);
+  norm_final_kernel<<<1, KB, 0, s>>>(w->part, w->hdev + slot, w->hdev + 6); xc_count_launch();
   XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+// The launches of one Arnoldi step k: z_k = M v_k; w = A z_k; two classical
+// Gram-Schmidt passes against v_0..v_k (coefficients to hdev[8..]); ||w||^2 to
+// hdev[2]; v_{k+1} = w / ||w||; the H column to the pinned host mirror.
+template <typename T>
+int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s) {
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  T* vk = H.V + (size_t)kk * n;
+  T* zk = H.Z + (size_t)kk * n;
+  T* wv = H.V + (size_t)(kk + 1) * n;
+  if (kk + 1 > 32) { xc_set_error("fgmres: restart above 32 basis vectors"); return XC_BAD_ARG; }
+  XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
+  XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
+  double* hd = w->hdev + 8;
+  for (int pass = 0; pass < 2; ++pass) {
+    launch_multidot<T>(n, kk + 1, H.V, n, wv, w->part, s);
+    multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, w->part, hd + pass * kMaxRestart); xc_count_launch();
+    multiaxpy_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv); xc_count_launch();
+  }
+  XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
+  normalize_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, wv); xc_count_launch();
+  XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
+  XC_LAUNCH_CHECK();
+  return XC_OK;
+}
+
+unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
+  unsigned long long h = 1469598103934665603ULL;
+  auto mix = [&](double v) {
+    unsigned long long b;
+    std::memcpy(&b, &v, sizeof(b));
+    h = (h ^ b) * 1099511628211ULL;
+  };
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.cmass); mix(cfg.kplane);
+  mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
+  return h | 1ULL;
+}
+
+template <typename T>
+void drop_graphs(Hier<T>& H) {
+  for (int q = 0; q < kMaxRestart; ++q)
+    if (H.gexec[q]) { cudaGraphExecDestroy(H.gexec[q]); H.gexec[q] = nullptr; }
+  H.gkey = 0;
+}
+
+// Arnoldi step kk as a CUDA graph captured on first use (the buffers are fixed
+// per context, so a graph stays valid across solves while the key holds)
+template <typename T>
+int arnoldi_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s) {
+  const unsigned long long key = graph_key(k, cfg);
+  if (H.gkey != key) { drop_graphs(H); H.gkey = key; }
+  if (!H.gexec[kk]) {
+    cudaGraph_t graph = nullptr;
+    XC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const long long before = g_xc_launches;
+    int st = arnoldi_launches<T>(w, H, k, cfg, kk, s);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (st != XC_OK) { if (graph) cudaGraphDestroy(graph); return st; }
+    if (e != cudaSuccess) { xc_set_error("graph capture failed: %s", cudaGetErrorString(e)); return XC_CUDA; }
+    H.gnodes[kk] = g_xc_launches - before;
+    g_xc_launches = before;
+    e = cudaGraphInstantiate(&H.gexec[kk], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { H.gexec[kk] = nullptr; xc_set_error("graph instantiate: %s", cudaGetErrorString(e)); return XC_CUDA; }
+  }
+  XC_CUDA_TRY(cudaGraphLaunch(H.gexec[kk], s));
+  g_xc_launches += H.gnodes[kk];
   return XC_OK;
 }
 
@@ -1154,35 +1585,21 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
     relres = beta / bnorm;
     if (!(relres > rtol) || its >= maxit) break;
     if (!std::isfinite(beta)) { *its_out = its; *relres_out = relres; xc_set_error("fgmres: non-finite residual"); return XC_NAN; }
-    hh[0] = beta;
+    hh[0] = 1.0 / beta;
     XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 1, hh, sizeof(double), cudaMemcpyHostToDevice, s));
     scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 1, H.V, H.V); xc_count_launch();
     std::fill(gv.begin(), gv.end(), 0.0);
     gv[0] = beta;
     int kk = 0;
     for (; kk < m && its < maxit; ++kk) {
-      T* vk = H.V + (size_t)kk * n;
-      T* zk = H.Z + (size_t)kk * n;
-      XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
-      T* wv = H.V + (size_t)(kk + 1) * n;
-      XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
-      // classical Gram-Schmidt, two passes
-      double* hd = w->hdev + 8;
-      for (int pass = 0; pass < 2; ++pass) {
-        multidot_kernel<T><<<KG, KB, 0, s>>>(n, kk + 1, H.V, n, wv, w->part); xc_count_launch();
-        multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, w->part, hd + pass * kMaxRestart); xc_count_launch();
-        multiaxpy_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv); xc_count_launch();
-      }
-      XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
-      XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
+      // z_k = M v_k, v_{k+1} = A z_k orthogonalised and normalised, H column
+      // copied to pinned host memory -- one CUDA graph launch per iteration
+      XC_TRY(arnoldi_step<T>(w, H, k, cfg, kk, s));
       XC_CUDA_TRY(cudaStreamSynchronize(s));
       XC_LAUNCH_CHECK();
       for (int i = 0; i <= kk; ++i) Hm[(size_t)kk * (m + 1) + i] = hh[8 + i] + hh[8 + kMaxRestart + i];
       double hn = std::sqrt(hh[2]);
       Hm[(size_t)kk * (m + 1) + kk + 1] = hn;
-      hh[1] = hn > 0 ? hn : 1.0;
-      XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 1, hh + 1, sizeof(double), cudaMemcpyHostToDevice, s));
-      scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 1, wv, wv); xc_count_launch();
       // Givens rotations on column kk
       double* col = &Hm[(size_t)kk * (m + 1)];
       for (int i = 0; i < kk; ++i) {
@@ -1329,7 +1746,10 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (c->p.open_cnv) { xc_set_error("fluidmech: open_cnv = true is not supported"); return XC_BAD_ARG; }
   xc_solver_opts o;
   if (opts) o = *opts;
-  else { o.kind = XC_SOLVER_FGMRES_FP64; o.rtol = 1e-10; o.maxit = 500; o.restart = 30; o.inner_rtol = 1e-4; o.inner_maxit = 60; }
+  else {
+    std::memset(&o, 0, sizeof(o));
+    o.kind = XC_SOLVER_FGMRES_FP64; o.rtol = 1e-10; o.maxit = 500; o.restart = 30; o.inner_rtol = 1e-4; o.inner_maxit = 60;
+  }
   if (o.restart < 2) o.restart = 30;
   if (o.restart > 30) o.restart = 30;
   const Geo& g = w->g;
@@ -1408,6 +1828,17 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     XC_LAUNCH_CHECK();
   }
   SolveCfg cfg;
+  if (o.smooth_sweeps > 0) cfg.nu = o.smooth_sweeps;
+  if (o.omega_velocity > 0) cfg.omega_v = o.omega_velocity;
+  if (o.schur_full_diagonal) { cfg.kplane = 0; cfg.cmass = 0.0; }
+  if (o.schur_mass > 0) cfg.cmass = o.schur_mass;
+  // The manufactured-solution system is the inertia-free limit: its coarse
+  // levels (which carry no U pin) leave a uniform U shift free, and long
+  // Jacobi runs on a 16x16 coarsest level serve it better than deep coarsening.
+  if (mms) { cfg.coarse_cells = 256; cfg.coarse_sweeps = 200; }
+  if (o.coarse_cells > 0) cfg.coarse_cells = o.coarse_cells;
+  if (o.coarse_sweeps > 0) cfg.coarse_sweeps = o.coarse_sweeps;
+  if (o.small_cells != 0) cfg.small_cells = o.small_cells;
   w->last_k = k;
   w->have_k = true;
   XC_TRY(setup_hier<double>(w, w->d, k, cfg, c, s));

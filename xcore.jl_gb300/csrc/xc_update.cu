@@ -517,3 +517,42 @@ int sums_impl(xc_ctx* c, double out[12]) {
   for (int k = 4; k < 12; ++k) out[k] = q[k] * h;
   return XC_OK;
 }
+
+// Per-step statistics of record_history! (src/history.jl:183-222):
+// x: min, mean, max, std; V, vx, vm, xie, xix, xis: min, rms, max;
+// Ra, Rc, ReD, Red, ks, ke, kx, eta, etamix, etae, etas, etat: min, geomean, max
+// (_rms = sqrt(mean(x^2)), _geomean = exp(mean(log(max(x, eps))))).
+int history_impl(xc_ctx* c, double out[58]) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  const double n = (double)Nz * (double)Nx;
+  cudaStream_t s = c->stream;
+  double* d = c->tmp[7];    // 64 device scalars
+  const CView none{nullptr, 0};
+  int k = 0;
+  CView x = CF(c, FLD_x);
+  XC_TRY(reduce_to(c, RED_MIN, x, none, nullptr, Nz, Nx, d + k++, s));
+  XC_TRY(reduce_to(c, RED_SUM, x, none, nullptr, Nz, Nx, d + k++, s, n));
+  XC_TRY(reduce_to(c, RED_MAX, x, none, nullptr, Nz, Nx, d + k++, s));
+  XC_TRY(reduce_to(c, RED_SUM, x, none, d + 1, Nz, Nx, d + k++, s));      // sum (x - mean)^2
+  const int rms_f[6] = {FLD_V, FLD_vx, FLD_vm, FLD_xie, FLD_xix, FLD_xis};
+  for (int q = 0; q < 6; ++q) {
+    CView f = CF(c, rms_f[q]);
+    XC_TRY(reduce_to(c, RED_MIN, f, none, nullptr, Nz, Nx, d + k++, s));
+    XC_TRY(reduce_to(c, RED_SUMSQ, f, none, nullptr, Nz, Nx, d + k++, s, n));
+    XC_TRY(reduce_to(c, RED_MAX, f, none, nullptr, Nz, Nx, d + k++, s));
+  }
+  const int gm_f[12] = {FLD_Ra, FLD_Rc, FLD_ReD, FLD_Red, FLD_ks, FLD_ke, FLD_kx, FLD_eta, FLD_etamix,
+                        FLD_etae, FLD_etas, FLD_etat};
+  for (int q = 0; q < 12; ++q) {
+    CView f = CF(c, gm_f[q]);
+    XC_TRY(reduce_to(c, RED_MIN, f, none, nullptr, Nz, Nx, d + k++, s));
+    XC_TRY(reduce_to(c, RED_SUMLOG, f, none, nullptr, Nz, Nx, d + k++, s, n));
+    XC_TRY(reduce_to(c, RED_MAX, f, none, nullptr, Nz, Nx, d + k++, s));
+  }
+  XC_CUDA_TRY(cudaMemcpyAsync(out, d, sizeof(double) * 58, cudaMemcpyDeviceToHost, s));
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  out[3] = std::sqrt(out[3] / (n - 1.0));
+  for (int q = 0; q < 6; ++q) out[4 + 3 * q + 1] = std::sqrt(out[4 + 3 * q + 1]);
+  for (int q = 0; q < 12; ++q) out[22 + 3 * q + 1] = std::exp(out[22 + 3 * q + 1]);
+  return XC_OK;
+}

@@ -36,7 +36,11 @@ end
 
 struct SolverOpts
     kind::Cint; rtol::Cdouble; maxit::Cint; restart::Cint; inner_rtol::Cdouble; inner_maxit::Cint
+    smooth_sweeps::Cint; omega_velocity::Cdouble; schur_mass::Cdouble; schur_full_diagonal::Cint
+    coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint
 end
+SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
+    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0)
 
 struct SolverStats
     iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
