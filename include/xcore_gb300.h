@@ -237,6 +237,26 @@ int xc_diffus_with_flux(double* dff, double* qx, double* qz, const double* f_hal
                         const double* k_halo, int Nz, int Nx, double h, int xBC, int zBC,
                         void* stream);
 
+/* The CFL step of xc_update_dt for callers that cannot let a library allocate
+   device memory (no counterpart in the reference).  A process whose device
+   memory is owned by its own pool -- a Julia session using CUDA.jl, or a
+   framework with a caching allocator -- cannot have a library call cudaMalloc
+   behind its back, and cudaMalloc / cudaFree would also synchronise the whole
+   device inside its time-step loop.  This call allocates nothing: kx (Nz,Nx),
+   Wx, Wm (Nz+1,Nx+2), Ux, Um (Nz+2,Nx+1) are the caller's device arrays and
+   dt_out is one caller-owned double in device memory; block partials live in
+   a fixed 80 KiB static device array that every device loading the library
+   holds until exit.  Limit: at most 2048 * 4096 = 8,388,608 elements per
+   array (about 2894 x 2894 cells); larger grids return XC_BAD_ARG.  The first
+   call on each device looks up the array's device address
+   (cudaGetSymbolAddress), so make that first call before any stream capture.
+   All calls share the array: calls that overlap on the GPU race and must not
+   be issued.  Nothing carries over between calls.  Stream-ordered on
+   `stream`; no host synchronisation. */
+int xc_update_dt_noalloc(const double* kx, const double* Wx, const double* Wm, const double* Ux,
+                         const double* Um, int Nz, int Nx, double h, double CFL, double dtmax,
+                         double dt_prev, double* dt_out, void* stream);
+
 /* time_coefs(Float64, TINT, step) -> (a1, a2, a3, b1, b2, b3)    src/timing.jl:18-36 */
 int xc_time_coefs(int tint, int step, double out[6]);
 

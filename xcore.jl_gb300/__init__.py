@@ -143,6 +143,7 @@ def lib():
             "xc_stream": (vp, [vp]),
             "xc_launch_count": (ctypes.c_longlong, []),
             "xc_bench_kernel": (ip, [vp, ip, ip, D6]),
+            "xc_update_dt_noalloc": (ip, [vp, vp, vp, vp, vp, ip, ip, dp, dp, dp, dp, vp, vp]),
             "xc_last_error": (ctypes.c_char_p, []),
             "xc_version": (ctypes.c_char_p, []),
         }
