@@ -90,7 +90,7 @@ typedef struct xc_solver_opts {
   double inner_rtol; /* mixed: relative reduction per FP32 inner solve */
   int inner_maxit;   /* mixed: FP32 FGMRES iterations per refinement pass */
   /* preconditioner knobs (0 selects the default) */
-  int smooth_sweeps;       /* Jacobi sweeps before and after each coarse correction (2) */
+  int smooth_sweeps;       /* Jacobi sweeps before and after each coarse correction (2; 4 for MMS) */
   double omega_velocity;   /* damping of the velocity Jacobi smoother (0.7) */
   double schur_mass;       /* weight c of the c*eta/rho term added to the Schur inverse (0.5) */
   int schur_full_diagonal; /* 1: pressure Laplacian from the full velocity diagonal, no mass term */
@@ -98,7 +98,7 @@ typedef struct xc_solver_opts {
                               level of a quarter of it (16; 256 for MMS) */
   int coarse_sweeps;       /* Jacobi sweeps there (4 (Nz + Nx), at least 32; 200 for MMS) */
   int small_cells;         /* levels of at most this many cells run their V-cycle in one CTA
-                              (4096; -1: none) */
+                              (256; -1: none) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

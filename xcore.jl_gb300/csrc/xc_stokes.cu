@@ -19,8 +19,10 @@
 // pressure Laplacian with the pin (plus an optional eta/rho mass term).
 // Mixed precision: the same Krylov/multigrid machinery in FP32 inside FP64
 // iterative refinement on the FP64 residual.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "xc_internal.cuh"
@@ -53,8 +55,6 @@ struct OpConst {
   int mms;             // 1: MMS pins (P row and U row are identity rows)
   int pin_u;           // flat U index of the MMS velocity pin
 };
-
-__device__ __forceinline__ int icxp(int i, int Nx) { return i == 0 ? Nx - 1 : (i == Nx + 1 ? 0 : i - 1); }
 
 // ---------------------------------------------------------------------------
 // coefficient planes of the velocity block (physical, unscaled), one level.
@@ -141,62 +141,211 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
   }
 }
 
+// ---------------------------------------------------------------------------
+// Velocity-block coefficients of one level, as the kernels see them.  The
+// FP64 hierarchy (whose operator defines the residual the solve converges on)
+// reads the ten planes above.  The FP32 hierarchy (preconditioner and inner
+// operator) rebuilds the nine stencil weights of a row from FP32 copies of
+// eta and etaco plus one precomputed diagonal term per row: 16 bytes per cell
+// from HBM instead of 80, the rest is arithmetic the FP32 pipes have to spare.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct VOp {
+  const T* cw;      // planes (FP64 hierarchy)
+  const T* cu;
+  const T* eta;     // FP32 hierarchy: cell viscosity (Nz, Nx)
+  const T* etaco;   //   corner viscosity (Nz+1, Nx+1)
+  const T* dw;      //   W rows: inertia + drunken-sailor term; bottom row: its diagonal
+  const T* du;      //   U rows: inertia + drunken-sailor term
+};
+template <typename T>
+constexpr bool kFly = std::is_same<T, float>::value;
+
+// dw / du and the FP32 viscosity copies of one level (terms as vel_coef_kernel)
+template <typename T>
+__global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta,
+                                const double* __restrict__ etaco, const double* __restrict__ rho,
+                                const double* __restrict__ rhow, const double* __restrict__ rhou,
+                                T* feta, T* fetaco, T* dw, T* du) {
+  const int Nz = g.Nz, Nx = g.Nx;
+  const double invh = g.invh;
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < (long long)Nz * Nx) feta[t] = (T)eta[t];
+  if (t < (long long)(Nz + 1) * (Nx + 1)) fetaco[t] = (T)etaco[t];
+  if (t < g.NW) {
+    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    double v = 1.0;
+    if (i >= 1 && i <= Nx && j == Nz) {
+      v = rhow[(size_t)(i - 1) * (Nz + 1) + Nz] * invh;
+    } else if (i >= 1 && i <= Nx && j >= 1 && j < Nz) {
+      v = k.a1 * rhow[(size_t)(i - 1) * (Nz + 1) + j] / k.dt;
+      if (k.sailor) v += (rho[(size_t)(i - 1) * Nz + j] - rho[(size_t)(i - 1) * Nz + j - 1]) * invh * k.g0 * k.dt;
+    }
+    dw[t] = (T)v;
+  }
+  if (t < g.NU) {
+    int j = (int)(t % (Nz + 2)), i = (int)(t / (Nz + 2));
+    double v = 1.0;
+    if (j >= 1 && j <= Nz) {
+      int ia = (i == 0) ? Nx - 1 : i - 1, ib = (i == Nx) ? 0 : i;
+      v = (k.a1 + k.gamma) * rhou[(size_t)i * Nz + j - 1] / k.dt;
+      if (k.sailor) v += (rho[(size_t)ib * Nz + j - 1] - rho[(size_t)ia * Nz + j - 1]) * invh * k.g0 * k.dt;
+    }
+    du[t] = (T)v;
+  }
+}
+
+// the nine weights of an interior row from its two corner (C) and two cell (P)
+// viscosities (fluidmech.jl:194-233 for W rows, 270-307 for U rows)
+template <typename T>
+struct RowW { T d, c1, c2, c3, c4, c5, c6, c7, c8; };
+template <typename T>
+__device__ __forceinline__ RowW<T> fly_row(T C1, T C2, T P1, T P2, T extra, T ih2) {
+  const T c23 = (T)(2.0 / 3.0), c13 = (T)(1.0 / 3.0), hf = (T)0.5;
+  RowW<T> w;
+  w.d = extra + (c23 * (P1 + P2) * ih2 + hf * (C1 + C2) * ih2);
+  w.c1 = -c23 * P1 * ih2;
+  w.c2 = -c23 * P2 * ih2;
+  w.c3 = -hf * C1 * ih2;
+  w.c4 = -hf * C2 * ih2;
+  w.c5 = -(hf * C1 - c13 * P1) * ih2;
+  w.c6 = +(hf * C1 - c13 * P2) * ih2;
+  w.c7 = +(hf * C2 - c13 * P1) * ih2;
+  w.c8 = -(hf * C2 - c13 * P2) * ih2;
+  return w;
+}
+template <typename T>
+__device__ __forceinline__ RowW<T> plane_row(const T* __restrict__ c, size_t N, long long t) {
+  RowW<T> w;
+  w.d = c[t]; w.c1 = c[N + t]; w.c2 = c[2 * N + t]; w.c3 = c[3 * N + t]; w.c4 = c[4 * N + t];
+  w.c5 = c[5 * N + t]; w.c6 = c[6 * N + t]; w.c7 = c[7 * N + t]; w.c8 = c[8 * N + t];
+  return w;
+}
+// weights of interior W row t = (j, i) and interior U row u = (j, i)
+template <typename T>
+__device__ __forceinline__ RowW<T> w_row(const Geo& g, const VOp<T>& op, long long t, int j, int i) {
+  if constexpr (kFly<T>) {
+    const int Nz = g.Nz;
+    return fly_row<T>(op.etaco[(size_t)(i - 1) * (Nz + 1) + j], op.etaco[(size_t)i * (Nz + 1) + j],
+                      op.eta[(size_t)(i - 1) * Nz + j - 1], op.eta[(size_t)(i - 1) * Nz + j], op.dw[t],
+                      (T)(g.invh * g.invh));
+  } else {
+    return plane_row<T>(op.cw, (size_t)g.NW, t);
+  }
+}
+template <typename T>
+__device__ __forceinline__ RowW<T> u_row(const Geo& g, const VOp<T>& op, long long u, int j, int i) {
+  if constexpr (kFly<T>) {
+    const int Nz = g.Nz, Nx = g.Nx;
+    const int ia = (i == 0) ? Nx - 1 : i - 1, ib = (i == Nx) ? 0 : i;
+    return fly_row<T>(op.etaco[(size_t)i * (Nz + 1) + j - 1], op.etaco[(size_t)i * (Nz + 1) + j],
+                      op.eta[(size_t)ia * Nz + j - 1], op.eta[(size_t)ib * Nz + j - 1], op.du[u],
+                      (T)(g.invh * g.invh));
+  } else {
+    return plane_row<T>(op.cu, (size_t)g.NU, u);
+  }
+}
+// W row t = (j, i) and U row u = (j, i) of A x, with the row's diagonal in *dg
+// (boundary rows: their exact-row value).  FULL adds the pressure gradient GG p
+// of the fine level (fluidmech.jl:343-356).
+template <typename T, bool FULL>
+__device__ __forceinline__ T vel_row_w(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xw,
+                                       const T* xu, const T* xp, long long t, int j, int i, T* dg) {
+  const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
+  if (i == 0) { *dg = (T)1; return xw[t] + (T)k.sds * xw[(size_t)Nx * lw + j]; }
+  if (i == Nx + 1) { *dg = (T)1; return xw[t] + (T)k.sds * xw[(size_t)1 * lw + j]; }
+  if (j == 0 || j == Nz) {
+    T d;
+    if constexpr (kFly<T>) d = j == 0 ? (T)1 : op.dw[t];
+    else d = op.cw[t];
+    *dg = d;
+    return d * xw[t];
+  }
+  const RowW<T> c = w_row<T>(g, op, t, j, i);
+  *dg = c.d;
+  T s = c.d * xw[t];
+  s += c.c1 * xw[t - 1];
+  s += c.c2 * xw[t + 1];
+  s += c.c3 * xw[t - lw];
+  s += c.c4 * xw[t + lw];
+  s += c.c5 * xu[(size_t)(i - 1) * lu + j];
+  s += c.c6 * xu[(size_t)(i - 1) * lu + j + 1];
+  s += c.c7 * xu[(size_t)i * lu + j];
+  s += c.c8 * xu[(size_t)i * lu + j + 1];
+  if (FULL) s += (T)g.invh * (xp[(size_t)i * lu + j + 1] - xp[(size_t)i * lu + j]);
+  return s;
+}
+template <typename T, bool FULL>
+__device__ __forceinline__ T vel_row_u(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xw,
+                                       const T* xu, const T* xp, long long u, int j, int i, T* dg) {
+  const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
+  if (j == 0) { *dg = (T)1; return xu[u] + (T)k.top_cnv * xu[u + 1]; }
+  if (j == Nz + 1) { *dg = (T)1; return xu[u] + (T)k.bot_cnv * xu[u - 1]; }
+  if (k.mms && (int)u == k.pin_u) { *dg = (T)1; return xu[u]; }
+  const int il = (i == 0) ? Nx - 1 : i - 1, ir = (i == Nx) ? 1 : i + 1;
+  const RowW<T> c = u_row<T>(g, op, u, j, i);
+  *dg = c.d;
+  T s = c.d * xu[u];
+  s += c.c1 * xu[(size_t)il * lu + j];
+  s += c.c2 * xu[(size_t)ir * lu + j];
+  s += c.c3 * xu[u - 1];
+  s += c.c4 * xu[u + 1];
+  s += c.c5 * xw[(size_t)i * lw + j - 1];
+  s += c.c6 * xw[(size_t)(i + 1) * lw + j - 1];
+  s += c.c7 * xw[(size_t)i * lw + j];
+  s += c.c8 * xw[(size_t)(i + 1) * lw + j];
+  if (FULL) s += (T)g.invh * (xp[(size_t)(i + 1) * lu + j] - xp[(size_t)i * lu + j]);
+  return s;
+}
+// diagonal alone (the first Jacobi sweep from zero needs nothing else)
+template <typename T>
+__device__ __forceinline__ T vel_diag_w(const Geo& g, const VOp<T>& op, long long t, int j, int i) {
+  if (i == 0 || i == g.Nx + 1 || j == 0) return (T)1;
+  if constexpr (kFly<T>) return j == g.Nz ? op.dw[t] : w_row<T>(g, op, t, j, i).d;
+  else return op.cw[t];
+}
+template <typename T>
+__device__ __forceinline__ T vel_diag_u(const Geo& g, const OpConst& k, const VOp<T>& op, long long u, int j,
+                                        int i) {
+  if (j == 0 || j == g.Nz + 1 || (k.mms && (int)u == k.pin_u)) return (T)1;
+  if constexpr (kFly<T>) return u_row<T>(g, op, u, j, i).d;
+  else return op.cu[u];
+}
+// diagonal of velocity row t (flat index over W then U rows)
+template <typename T>
+__device__ __forceinline__ T vel_diag(const Geo& g, const OpConst& k, const VOp<T>& op, long long t) {
+  if (t < g.NW) return vel_diag_w<T>(g, op, t, (int)(t % (g.Nz + 1)), (int)(t / (g.Nz + 1)));
+  const long long u = t - g.NW;
+  return vel_diag_u<T>(g, k, op, u, (int)(u % (g.Nz + 2)), (int)(u / (g.Nz + 2)));
+}
+// inertial part of the diagonal of interior U row u
+template <typename T>
+__device__ __forceinline__ T vel_inertia_u(const Geo& g, const VOp<T>& op, long long u) {
+  if constexpr (kFly<T>) return op.du[u];
+  else return op.cu[9 * (size_t)g.NU + u];
+}
+
 // y = A x over all velocity rows of a level (ghost / boundary rows included);
 // if b != null: y = b - A x.  With FULL (fine level): adds the pressure
 // gradient GG p (fluidmech.jl:343-356).  The unknowns are not __restrict__:
 // the one-CTA multigrid kernels read them after other threads of the CTA wrote
 // them, which the read-only load path does not see.
 template <typename T, bool FULL>
-__device__ __forceinline__ T vel_row(const Geo& g, const OpConst& k, const T* __restrict__ cw,
-                                     const T* __restrict__ cu, const T* xw, const T* xu, const T* xp,
-                                     long long t) {
-  const int Nz = g.Nz, Nx = g.Nx;
-  const int lw = Nz + 1, lu = Nz + 2;
-  if (t < g.NW) {
-    int j = (int)(t % lw), i = (int)(t / lw);
-    if (i == 0) return xw[t] + (T)k.sds * xw[(size_t)Nx * lw + j];
-    if (i == Nx + 1) return xw[t] + (T)k.sds * xw[(size_t)1 * lw + j];
-    if (j == 0 || j == Nz) return cw[t] * xw[t];
-    const size_t NW = g.NW;
-    T s = cw[t] * xw[t];
-    s += cw[1 * NW + t] * xw[t - 1];
-    s += cw[2 * NW + t] * xw[t + 1];
-    s += cw[3 * NW + t] * xw[t - lw];
-    s += cw[4 * NW + t] * xw[t + lw];
-    s += cw[5 * NW + t] * xu[(size_t)(i - 1) * lu + j];
-    s += cw[6 * NW + t] * xu[(size_t)(i - 1) * lu + j + 1];
-    s += cw[7 * NW + t] * xu[(size_t)i * lu + j];
-    s += cw[8 * NW + t] * xu[(size_t)i * lu + j + 1];
-    if (FULL) s += (T)g.invh * (xp[(size_t)i * lu + j + 1] - xp[(size_t)i * lu + j]);
-    return s;
-  }
-  t -= g.NW;
-  int j = (int)(t % lu), i = (int)(t / lu);
-  if (j == 0) return xu[t] + (T)k.top_cnv * xu[t + 1];
-  if (j == Nz + 1) return xu[t] + (T)k.bot_cnv * xu[t - 1];
-  if (k.mms && (int)t == k.pin_u) return xu[t];
-  const size_t NU = g.NU;
-  int il = (i == 0) ? Nx - 1 : i - 1, ir = (i == Nx) ? 1 : i + 1;
-  T s = cu[t] * xu[t];
-  s += cu[1 * NU + t] * xu[(size_t)il * lu + j];
-  s += cu[2 * NU + t] * xu[(size_t)ir * lu + j];
-  s += cu[3 * NU + t] * xu[t - 1];
-  s += cu[4 * NU + t] * xu[t + 1];
-  s += cu[5 * NU + t] * xw[(size_t)i * lw + j - 1];
-  s += cu[6 * NU + t] * xw[(size_t)(i + 1) * lw + j - 1];
-  s += cu[7 * NU + t] * xw[(size_t)i * lw + j];
-  s += cu[8 * NU + t] * xw[(size_t)(i + 1) * lw + j];
-  if (FULL) s += (T)g.invh * (xp[(size_t)(i + 1) * lu + j] - xp[(size_t)i * lu + j]);
-  return s;
+__device__ __forceinline__ T vel_row(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xw, const T* xu,
+                                     const T* xp, long long t) {
+  T d;
+  if (t < g.NW)
+    return vel_row_w<T, FULL>(g, k, op, xw, xu, xp, t, (int)(t % (g.Nz + 1)), (int)(t / (g.Nz + 1)), &d);
+  const long long u = t - g.NW;
+  return vel_row_u<T, FULL>(g, k, op, xw, xu, xp, u, (int)(u % (g.Nz + 2)), (int)(u / (g.Nz + 2)), &d);
 }
 
 // pressure rows of LL: ghost ring, pin, rho-weighted divergence (fluidmech.jl:367-488)
 template <typename T>
 __device__ __forceinline__ T p_row(const Geo& g, const OpConst& k, const T* __restrict__ cp,
                                    const T* __restrict__ xw, const T* __restrict__ xu,
-                                   const T* __restrict__ xp, int t) {
+                                   const T* __restrict__ xp, int t, int j, int i) {
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2, lw = Nz + 1;
-  int j = t % lp, i = t / lp;
   if (j == 0) return xp[t] - xp[t + 1];
   if (j == Nz + 1) return xp[t] - xp[t - 1];
   if (i == 0) return xp[t] - xp[(size_t)Nx * lp + j];
@@ -227,23 +376,36 @@ __global__ void p_coef_kernel(Geo g, const double* __restrict__ rhow, const doub
 }
 
 // y = S o (LL (S o v)) on the whole unknown vector; t must hold S o v.
-// If b != null: y = b - S o (LL t).
+// If b != null: y = b - S o (LL t).  Thread (j, i) of the 2-D grid takes the
+// W, U and P rows at (j, i).
 template <typename T>
-__global__ void stokes_apply_kernel(Geo g, OpConst k, const T* __restrict__ cw,
-                                    const T* __restrict__ cu, const T* __restrict__ cp,
-                                    const T* __restrict__ scl, const T* __restrict__ tv,
-                                    const T* __restrict__ b, T* y) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long n = (long long)g.NW + g.NU + g.NP;
-  if (t >= n) return;
+__global__ void __launch_bounds__(256) stokes_apply_kernel(Geo g, OpConst k, VOp<T> op, const T* __restrict__ cp,
+                                                           const T* __restrict__ scl, const T* __restrict__ tv,
+                                                           const T* __restrict__ b, T* y) {
+  const int j = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  const int Nz = g.Nz, Nx = g.Nx;
+  if (j > Nz + 1 || i > Nx + 1) return;
   const T* xw = tv;
   const T* xu = tv + g.NW;
   const T* xp = tv + g.NW + g.NU;
-  T v;
-  if (t < (long long)g.NW + g.NU) v = vel_row<T, true>(g, k, cw, cu, xw, xu, xp, t);
-  else v = p_row<T>(g, k, cp, xw, xu, xp, (int)(t - g.NW - g.NU));
-  v *= scl[t];
-  y[t] = b ? b[t] - v : v;
+  T d;
+  if (j <= Nz) {
+    const long long t = (long long)i * (Nz + 1) + j;
+    const T v = vel_row_w<T, true>(g, k, op, xw, xu, xp, t, j, i, &d) * scl[t];
+    y[t] = b ? b[t] - v : v;
+  }
+  if (i <= Nx) {
+    const long long u = (long long)i * (Nz + 2) + j, t = g.NW + u;
+    const T v = vel_row_u<T, true>(g, k, op, xw, xu, xp, u, j, i, &d) * scl[t];
+    y[t] = b ? b[t] - v : v;
+  }
+  {
+    const int pt = i * (Nz + 2) + j;
+    const long long t = (long long)g.NW + g.NU + pt;
+    const T v = p_row<T>(g, k, cp, xw, xu, xp, pt, j, i) * scl[t];
+    y[t] = b ? b[t] - v : v;
+  }
 }
 
 template <typename T>
@@ -274,52 +436,76 @@ __global__ void refine_update_kernel(long long n, const T* __restrict__ dy, cons
 // ---------------------------------------------------------------------------
 // Each multigrid operation is a per-unknown body (`*_at`, index t) used both by
 // a grid-wide kernel and by the one-CTA kernels of the small levels.
-template <typename T>
-__device__ __forceinline__ void vel_residual_at(const Geo& g, const OpConst& k, const T* __restrict__ cw,
-                                                const T* __restrict__ cu, const T* x, const T* b, T* r,
-                                                long long t) {
-  r[t] = b[t] - vel_row<T, false>(g, k, cw, cu, x, x + g.NW, nullptr, t);
+// one velocity row of a Jacobi sweep (MODE 0: first sweep from zero, 1: sweep)
+// or of the residual (MODE 2): out = xi + w D^-1 (b - A xi), resp. b - A xi;
+// ghost / boundary rows are relaxed exactly (w = 1)
+template <typename T, int MODE>
+__device__ __forceinline__ void vel_update_w(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi,
+                                             const T* b, T* out, T omega, long long t, int j, int i) {
+  const bool exact = i == 0 || i == g.Nx + 1 || j == 0 || j == g.Nz;
+  if (MODE == 0) {
+    out[t] = (exact ? (T)1 : omega) * b[t] / vel_diag_w<T>(g, op, t, j, i);
+    return;
+  }
+  T d;
+  const T ax = vel_row_w<T, false>(g, k, op, xi, xi + g.NW, nullptr, t, j, i, &d);
+  if (MODE == 2) out[t] = b[t] - ax;
+  else out[t] = xi[t] + (exact ? (T)1 : omega) * (b[t] - ax) / d;
 }
-template <typename T>
-__global__ void vel_residual_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
-                                    const T* __restrict__ x, const T* __restrict__ b, T* r) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)g.NW + g.NU) return;
-  vel_residual_at<T>(g, k, cw, cu, x, b, r, t);
+template <typename T, int MODE>
+__device__ __forceinline__ void vel_update_u(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi,
+                                             const T* b, T* out, T omega, long long u, int j, int i) {
+  const bool exact = j == 0 || j == g.Nz + 1 || (k.mms && (int)u == k.pin_u);
+  const long long t = g.NW + u;
+  if (MODE == 0) {
+    out[t] = (exact ? (T)1 : omega) * b[t] / vel_diag_u<T>(g, k, op, u, j, i);
+    return;
+  }
+  T d;
+  const T ax = vel_row_u<T, false>(g, k, op, xi, xi + g.NW, nullptr, u, j, i, &d);
+  if (MODE == 2) out[t] = b[t] - ax;
+  else out[t] = xi[t] + (exact ? (T)1 : omega) * (b[t] - ax) / d;
 }
+// a level's rows on a 2-D grid: thread (j, i) takes W row (j, i) and U row
+// (j, i) -- no index division, and the two rows share viscosity loads
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) vel_sweep2d_kernel(Geo g, OpConst k, VOp<T> op, const T* __restrict__ xi,
+                                                          const T* __restrict__ b, T* out, T omega) {
+  const int j = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  if (j <= g.Nz && i <= g.Nx + 1)
+    vel_update_w<T, MODE>(g, k, op, xi, b, out, omega, (long long)i * (g.Nz + 1) + j, j, i);
+  if (j <= g.Nz + 1 && i <= g.Nx)
+    vel_update_u<T, MODE>(g, k, op, xi, b, out, omega, (long long)i * (g.Nz + 2) + j, j, i);
+}
+
 
 // damped Jacobi: xo = xi + w D^-1 (b - A xi); ghost / boundary rows exact
 template <typename T>
-__device__ __forceinline__ void vel_jacobi_at(const Geo& g, const OpConst& k, const T* __restrict__ cw,
-                                              const T* __restrict__ cu, const T* xi, const T* b, T* xo,
-                                              T omega, int zero_init, long long t) {
-  const int Nz = g.Nz, Nx = g.Nx;
-  bool exact;
-  T d;
-  if (t < g.NW) {
-    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
-    exact = (i == 0 || i == Nx + 1 || j == 0 || j == Nz);
-    d = cw[t];
+__device__ __forceinline__ void vel_jacobi_at(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi,
+                                              const T* b, T* xo, T omega, int zero_init, long long t) {
+  // flat index over W then U rows; levels stay below 2^31 unknowns
+  const int tt = (int)t;
+  if (tt < g.NW) {
+    const int j = tt % (g.Nz + 1), i = tt / (g.Nz + 1);
+    if (zero_init) vel_update_w<T, 0>(g, k, op, xi, b, xo, omega, t, j, i);
+    else vel_update_w<T, 1>(g, k, op, xi, b, xo, omega, t, j, i);
   } else {
-    long long u = t - g.NW;
-    int j = (int)(u % (Nz + 2));
-    exact = (j == 0 || j == Nz + 1) || (k.mms && (int)u == k.pin_u);
-    d = cu[u];
+    const int u = tt - g.NW, j = u % (g.Nz + 2), i = u / (g.Nz + 2);
+    if (zero_init) vel_update_u<T, 0>(g, k, op, xi, b, xo, omega, u, j, i);
+    else vel_update_u<T, 1>(g, k, op, xi, b, xo, omega, u, j, i);
   }
-  if (zero_init) {
-    xo[t] = (exact ? (T)1 : omega) * b[t] / d;
-    return;
-  }
-  T res = b[t] - vel_row<T, false>(g, k, cw, cu, xi, xi + g.NW, nullptr, t);
-  xo[t] = xi[t] + (exact ? (T)1 : omega) * res / d;
 }
 template <typename T>
-__global__ void vel_jacobi_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
-                                  const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
-                                  int zero_init) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)g.NW + g.NU) return;
-  vel_jacobi_at<T>(g, k, cw, cu, xi, b, xo, omega, zero_init, t);
+__device__ __forceinline__ void vel_residual_at(const Geo& g, const OpConst& k, const VOp<T>& op, const T* x,
+                                                const T* b, T* r, long long t) {
+  const int tt = (int)t;
+  if (tt < g.NW) {
+    vel_update_w<T, 2>(g, k, op, x, b, r, (T)0, t, tt % (g.Nz + 1), tt / (g.Nz + 1));
+  } else {
+    const int u = tt - g.NW;
+    vel_update_u<T, 2>(g, k, op, x, b, r, (T)0, u, u % (g.Nz + 2), u / (g.Nz + 2));
+  }
 }
 
 // restriction of the interior-row residual (full weighting / 4 of the
@@ -438,7 +624,7 @@ __global__ void coarsen_fields_kernel(int Nzc, int Nxc, const double* __restrict
                                       double* rhouc) {
   int J = blockIdx.x * blockDim.x + threadIdx.x;
   int I = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Nz = 2 * Nzc, Nx = 2 * Nxc;
+  const int Nz = 2 * Nzc;
   if (J > Nzc || I > Nxc) return;
   etacoc[(size_t)I * (Nzc + 1) + J] = etaco[(size_t)(2 * I) * (Nz + 1) + 2 * J];
   if (I < Nxc) {
@@ -474,30 +660,15 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
 // would let that mode grow with the sweep count, so it is removed from the
 // coarse correction and left to the pinned fine level and the Krylov method.
 template <typename T>
-__device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const T* __restrict__ cw, const T* __restrict__ cu,
-                               T* x, T* x2, const T* b, int sweeps, T omega) {
+__device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const VOp<T>& op, T* x, T* x2, const T* b,
+                               int sweeps, T omega) {
   const long long n = (long long)g.NW + g.NU;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
   __syncthreads();
   T* a = x;
   T* o = x2;
   for (int s = 0; s < sweeps; ++s) {
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-      bool exact;
-      T d;
-      if (t < g.NW) {
-        int j = (int)(t % (g.Nz + 1)), i = (int)(t / (g.Nz + 1));
-        exact = (i == 0 || i == g.Nx + 1 || j == 0 || j == g.Nz);
-        d = cw[t];
-      } else {
-        long long u = t - g.NW;
-        int j = (int)(u % (g.Nz + 2));
-        exact = (j == 0 || j == g.Nz + 1) || (k.mms && (int)u == k.pin_u);
-        d = cu[u];
-      }
-      T res = b[t] - vel_row<T, false>(g, k, cw, cu, a, a + g.NW, nullptr, t);
-      o[t] = a[t] + (exact ? (T)1 : omega) * res / d;
-    }
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, op, a, b, o, omega, 0, t);
     __syncthreads();
     T* tmp = a; a = o; o = tmp;
   }
@@ -509,7 +680,10 @@ __device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const T* __restri
     double si = 0, sd = 0, sx = 0;
     for (long long u = threadIdx.x; u < g.NU; u += blockDim.x) {
       int j = (int)(u % (g.Nz + 2));
-      if (j >= 1 && j <= g.Nz) { si += (double)cu[9 * (size_t)g.NU + u]; sd += (double)cu[u]; }
+      if (j >= 1 && j <= g.Nz) {
+        si += (double)vel_inertia_u<T>(g, op, u);
+        sd += (double)vel_diag<T>(g, k, op, g.NW + u);
+      }
       sx += (double)x[g.NW + u];
     }
     si = cta_sum(si, red);
@@ -523,9 +697,9 @@ __device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const T* __restri
   }
 }
 template <typename T>
-__global__ void vel_coarse_kernel(Geo g, OpConst k, const T* __restrict__ cw, const T* __restrict__ cu,
-                                  T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
-  vel_coarse_cta<T>(g, k, cw, cu, x, x2, b, sweeps, omega);
+__global__ void vel_coarse_kernel(Geo g, OpConst k, VOp<T> op, T* x, T* x2, const T* __restrict__ b, int sweeps,
+                                  T omega) {
+  vel_coarse_cta<T>(g, k, op, x, x2, b, sweeps, omega);
 }
 
 // ---------------------------------------------------------------------------
@@ -660,18 +834,19 @@ __global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const 
 }
 
 // ---------------------------------------------------------------------------
-// Small levels in one CTA.  Below about 64x64 cells a level holds a few
-// thousand unknowns, and each phase of its V-cycle (a smoothing sweep, the
-// residual, the restriction, the prolongation) is bound by launch latency, not
-// by bandwidth.  These kernels run the V-cycle from level l0 down to the
-// coarsest level lc and back up inside one CTA, with CTA barriers between the
-// phases; the level data stays in L1/L2.
+// Small levels in one CTA.  A level of a few hundred cells is a few hundred
+// unknowns, and each phase of its V-cycle (a smoothing sweep, the residual,
+// the restriction, the prolongation) is bound by launch latency, not by
+// bandwidth.  These kernels run the V-cycle from level l0 down to the coarsest
+// level lc and back up inside one CTA, with CTA barriers between the phases;
+// the level data stays in L1/L2.  Measured at 1024^2 against one launch per
+// phase: handing the levels up to 16x16 to one CTA saves 3% of the solve; up
+// to 64x64 it costs 6% (one CTA then streams too many rows per phase).
 // ---------------------------------------------------------------------------
 template <typename T>
 struct VelLevels {
   Geo g[kMaxLevels];
-  const T* cw[kMaxLevels];
-  const T* cu[kMaxLevels];
+  VOp<T> op[kMaxLevels];
   T* x[kMaxLevels];
   T* x2[kMaxLevels];
   T* b[kMaxLevels];
@@ -680,19 +855,19 @@ struct VelLevels {
 
 // `sweeps` damped-Jacobi sweeps (the first from zero when from_zero), x holds the result
 template <typename T>
-__device__ void vel_smooth_cta(const Geo& g, const OpConst& k, const T* __restrict__ cw, const T* __restrict__ cu,
-                               T* x, T* x2, const T* b, T om, int sweeps, bool from_zero) {
+__device__ void vel_smooth_cta(const Geo& g, const OpConst& k, const VOp<T>& op, T* x, T* x2, const T* b, T om,
+                               int sweeps, bool from_zero) {
   const long long n = (long long)g.NW + g.NU;
   T* a = x;
   T* o = x2;
   int q = 0;
   if (from_zero) {
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, cw, cu, x, b, x, om, 1, t);
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, op, x, b, x, om, 1, t);
     __syncthreads();
     q = 1;
   }
   for (; q < sweeps; ++q) {
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, cw, cu, a, b, o, om, 0, t);
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_jacobi_at<T>(g, k, op, a, b, o, om, 0, t);
     __syncthreads();
     T* tmp = a; a = o; o = tmp;
   }
@@ -716,23 +891,23 @@ __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> L, 
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
     const Geo& c = L.g[l + 1];
-    vel_smooth_cta<T>(g, k, L.cw[l], L.cu[l], L.x[l], L.x2[l], L.b[l], om, nu, true);
+    vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, true);
     const long long n = (long long)g.NW + g.NU;
     for (long long t = threadIdx.x; t < n; t += blockDim.x)
-      vel_residual_at<T>(g, k, L.cw[l], L.cu[l], L.x[l], L.b[l], L.r[l], t);
+      vel_residual_at<T>(g, k, L.op[l], L.x[l], L.b[l], L.r[l], t);
     __syncthreads();
     const long long nc = (long long)c.NW + c.NU;
     for (long long t = threadIdx.x; t < nc; t += blockDim.x) vel_restrict_at<T>(g, c, L.r[l], L.b[l + 1], t);
     __syncthreads();
   }
-  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.cw[lc], L.cu[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om);
+  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.op[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om);
   for (int l = lc - 1; l >= l0; --l) {
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
     const long long n = (long long)g.NW + g.NU;
     for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_prolong_at<T>(g, L.g[l + 1], k, L.x[l + 1], L.x[l], t);
     __syncthreads();
-    vel_smooth_cta<T>(g, k, L.cw[l], L.cu[l], L.x[l], L.x2[l], L.b[l], om, nu, false);
+    vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, false);
   }
 }
 
@@ -800,8 +975,8 @@ __global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> L, int 
 // plane 9: inertia only) -- k = rho_face / (h^2 A_ff)
 template <typename T>
 __global__ void p_kcoef_kernel(Geo g, const double* __restrict__ rhow, const double* __restrict__ rhou,
-                               const T* __restrict__ cw, const T* __restrict__ cu, int plane, T* kx, T* kz,
-                               T* kr) {
+                               const double* __restrict__ cw, const double* __restrict__ cu, int plane, T* kx,
+                               T* kz, T* kr) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx;
   const double ih2 = g.invh * g.invh;
@@ -1151,6 +1326,9 @@ __global__ void pack_kernel(Geo g, CView W, CView U, CView P, double* x) {
 }
 
 inline unsigned nblk(long long n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+// 2-D launch over the (Nz + 2) x (Nx + 2) row positions of a level
+inline dim3 blk2() { return dim3(32, 8); }
+inline dim3 grid2(const Geo& g) { return dim3((unsigned)((g.Nz + 2 + 31) / 32), (unsigned)((g.Nx + 2 + 7) / 8)); }
 
 }  // namespace
 
@@ -1161,8 +1339,12 @@ template <typename T>
 struct Hier {
   int nv, np_lv;               // velocity and pressure level counts
   Geo vg[kMaxLevels];
-  T* cw[kMaxLevels];
+  T* cw[kMaxLevels];           // coefficient planes (FP64 hierarchy only)
   T* cu[kMaxLevels];
+  T* feta[kMaxLevels];         // FP32 hierarchy: the VOp fields
+  T* fetaco[kMaxLevels];
+  T* fdw[kMaxLevels];
+  T* fdu[kMaxLevels];
   T* vx[kMaxLevels];
   T* vx2[kMaxLevels];
   T* vb[kMaxLevels];
@@ -1232,8 +1414,15 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
     Geo lg = make_geo(Nz, Nx, h);
     H.vg[H.nv] = lg;
     long long nvv = (long long)lg.NW + lg.NU;
-    XC_CUDA_TRY(cudaMalloc(&H.cw[H.nv], sizeof(T) * 10 * lg.NW));
-    XC_CUDA_TRY(cudaMalloc(&H.cu[H.nv], sizeof(T) * 10 * lg.NU));
+    if (kFly<T>) {
+      XC_CUDA_TRY(cudaMalloc(&H.feta[H.nv], sizeof(T) * lg.Nz * lg.Nx));
+      XC_CUDA_TRY(cudaMalloc(&H.fetaco[H.nv], sizeof(T) * (lg.Nz + 1) * (lg.Nx + 1)));
+      XC_CUDA_TRY(cudaMalloc(&H.fdw[H.nv], sizeof(T) * lg.NW));
+      XC_CUDA_TRY(cudaMalloc(&H.fdu[H.nv], sizeof(T) * lg.NU));
+    } else {
+      XC_CUDA_TRY(cudaMalloc(&H.cw[H.nv], sizeof(T) * 10 * lg.NW));
+      XC_CUDA_TRY(cudaMalloc(&H.cu[H.nv], sizeof(T) * 10 * lg.NU));
+    }
     XC_CUDA_TRY(cudaMalloc(&H.vx[H.nv], sizeof(T) * nvv));
     XC_CUDA_TRY(cudaMalloc(&H.vx2[H.nv], sizeof(T) * nvv));
     XC_CUDA_TRY(cudaMalloc(&H.vb[H.nv], sizeof(T) * nvv));
@@ -1280,6 +1469,7 @@ void free_hier(Hier<T>& H) {
     if (H.gexec[q]) { cudaGraphExecDestroy(H.gexec[q]); H.gexec[q] = nullptr; }
   for (int l = 0; l < H.nv; ++l) {
     cudaFree(H.cw[l]); cudaFree(H.cu[l]); cudaFree(H.vx[l]); cudaFree(H.vx2[l]); cudaFree(H.vb[l]); cudaFree(H.vr[l]);
+    cudaFree(H.feta[l]); cudaFree(H.fetaco[l]); cudaFree(H.fdw[l]); cudaFree(H.fdu[l]);
   }
   for (int l = 0; l < H.np_lv; ++l) {
     cudaFree(H.kx[l]); cudaFree(H.kz[l]); cudaFree(H.px[l]); cudaFree(H.px2[l]); cudaFree(H.pb[l]); cudaFree(H.pr[l]);
@@ -1289,13 +1479,21 @@ void free_hier(Hier<T>& H) {
   H.nv = H.np_lv = 0;
 }
 
+template <typename T>
+VOp<T> vop(const Hier<T>& H, int l) {
+  VOp<T> o;
+  o.cw = H.cw[l]; o.cu = H.cu[l];
+  o.eta = H.feta[l]; o.etaco = H.fetaco[l]; o.dw = H.fdw[l]; o.du = H.fdu[l];
+  return o;
+}
+
 struct SolveCfg {
   double omega_v = 0.7, omega_p = 0.8;
   int nu = 2;
   int coarse_sweeps = 0;   // 0: 4 * (Nz + Nx) of the coarsest level, at least 32
   int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
                            // solved by Jacobi sweeps
-  int small_cells = 4096;  // levels of at most this many cells run in one CTA
+  int small_cells = 256;   // levels of at most this many cells run in one CTA
   // Schur approximation (Cahouet-Chabard): S^-1 ~ L_in^-1 + cmass * eta/rho with
   // L_in = DM diag(a1 rho/dt)^-1 GG (kplane 9); kplane 0 builds L from the full
   // velocity diagonal instead (cmass then defaults to 0)
@@ -1334,7 +1532,7 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
     while (!vel_coarsest(H, cfg, lc)) ++lc;
     VelLevels<T> L;
     for (int q = 0; q <= lc; ++q) {
-      L.g[q] = H.vg[q]; L.cw[q] = H.cw[q]; L.cu[q] = H.cu[q];
+      L.g[q] = H.vg[q]; L.op[q] = vop(H, q);
       L.x[q] = H.vx[q]; L.x2[q] = H.vx2[q]; L.b[q] = H.vb[q]; L.r[q] = H.vr[q];
     }
     vel_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, kf, l, lc, cfg.nu, om,
@@ -1344,21 +1542,22 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
     return XC_OK;
   }
   if (vel_coarsest(H, cfg, l)) {
-    vel_coarse_kernel<T><<<1, coarse_threads(n), 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vx2[l], H.vb[l],
+    vel_coarse_kernel<T><<<1, coarse_threads(n), 0, s>>>(g, k, vop(H, l), H.vx[l], H.vx2[l], H.vb[l],
                                                         coarse_sweeps(cfg, g.Nz, g.Nx), om); xc_count_launch();
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
   // pre-smoothing (first sweep from zero)
-  vel_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vb[l], H.vx[l], om, 1); xc_count_launch();
+  const VOp<T> op = vop(H, l);
+  vel_sweep2d_kernel<T, 0><<<grid2(g), blk2(), 0, s>>>(g, k, op, H.vx[l], H.vb[l], H.vx[l], om); xc_count_launch();
   T* a = H.vx[l];
   T* o = H.vx2[l];
   for (int q = 1; q < cfg.nu; ++q) {
-    vel_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], a, H.vb[l], o, om, 0); xc_count_launch();
+    vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op, a, H.vb[l], o, om); xc_count_launch();
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-  vel_residual_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], H.vx[l], H.vb[l], H.vr[l]); xc_count_launch();
+  vel_sweep2d_kernel<T, 2><<<grid2(g), blk2(), 0, s>>>(g, k, op, H.vx[l], H.vb[l], H.vr[l], om); xc_count_launch();
   const Geo& c = H.vg[l + 1];
   vel_restrict_kernel<T><<<nblk((long long)c.NW + c.NU), 256, 0, s>>>(g, c, H.vr[l], H.vb[l + 1]); xc_count_launch();
   XC_LAUNCH_CHECK();
@@ -1367,7 +1566,7 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   a = H.vx[l];
   o = H.vx2[l];
   for (int q = 0; q < cfg.nu; ++q) {
-    vel_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[l], H.cu[l], a, H.vb[l], o, om, 0); xc_count_launch();
+    vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op, a, H.vb[l], o, om); xc_count_launch();
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
@@ -1465,7 +1664,7 @@ int apply_scaled(StokesWork* w, Hier<T>& H, const OpConst& k, const T* v, const 
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   mul_kernel<T><<<nblk(n), 256, 0, s>>>(n, v, H.scl, H.t); xc_count_launch();
-  stokes_apply_kernel<T><<<nblk(n), 256, 0, s>>>(g, k, H.cw[0], H.cu[0], H.cp, H.scl, H.t, b, y); xc_count_launch();
+  stokes_apply_kernel<T><<<grid2(g), blk2(), 0, s>>>(g, k, vop(H, 0), H.cp, H.scl, H.t, b, y); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -1647,8 +1846,14 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
     const double* rhou = l ? w->rhou[l] : (const double*)c->field[FLD_rhou];
     OpConst kl = k;
     if (l) kl.mms = 0;
-    vel_coef_kernel<T><<<nblk((long long)lg.NW + lg.NU), 256, 0, s>>>(lg, kl, eta, etaco, rho, rhow, rhou,
-                                                                      H.cw[l], H.cu[l]); xc_count_launch();
+    if (kFly<T>) {
+      const long long nt = std::max((long long)lg.NW + lg.NU, (long long)(lg.Nz + 1) * (lg.Nx + 1));
+      fly_coef_kernel<T><<<nblk(nt), 256, 0, s>>>(lg, kl, eta, etaco, rho, rhow, rhou, H.feta[l], H.fetaco[l],
+                                                  H.fdw[l], H.fdu[l]); xc_count_launch();
+    } else {
+      vel_coef_kernel<T><<<nblk((long long)lg.NW + lg.NU), 256, 0, s>>>(lg, kl, eta, etaco, rho, rhow, rhou,
+                                                                        H.cw[l], H.cu[l]); xc_count_launch();
+    }
     XC_LAUNCH_CHECK();
   }
   // DM planes, scaling, eta/rho (double), converted for FP32
@@ -1666,7 +1871,7 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
   }
   // pressure hierarchy
   p_kcoef_kernel<T><<<nblk((long long)(g.Nz + 1) * g.Nx), 256, 0, s>>>(
-      g, (const double*)c->field[FLD_rhow], (const double*)c->field[FLD_rhou], H.cw[0], H.cu[0], cfg.kplane,
+      g, (const double*)c->field[FLD_rhow], (const double*)c->field[FLD_rhou], w->d.cw[0], w->d.cu[0], cfg.kplane,
       H.kx[0], H.kz[0], H.kr); xc_count_launch();
   XC_LAUNCH_CHECK();
   H.pdpin[0] = (T)1.0;
@@ -1828,14 +2033,15 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     XC_LAUNCH_CHECK();
   }
   SolveCfg cfg;
+  // The manufactured-solution system is the inertia-free limit, where damped
+  // Jacobi smooths the grad-div coupled viscous rows poorly: four sweeps per
+  // level and long Jacobi runs on a 16x16 coarsest level converge in about a
+  // third of the iterations of the defaults there.
+  if (mms) { cfg.nu = 4; cfg.coarse_cells = 256; cfg.coarse_sweeps = 200; }
   if (o.smooth_sweeps > 0) cfg.nu = o.smooth_sweeps;
   if (o.omega_velocity > 0) cfg.omega_v = o.omega_velocity;
   if (o.schur_full_diagonal) { cfg.kplane = 0; cfg.cmass = 0.0; }
   if (o.schur_mass > 0) cfg.cmass = o.schur_mass;
-  // The manufactured-solution system is the inertia-free limit: its coarse
-  // levels (which carry no U pin) leave a uniform U shift free, and long
-  // Jacobi runs on a 16x16 coarsest level serve it better than deep coarsening.
-  if (mms) { cfg.coarse_cells = 256; cfg.coarse_sweeps = 200; }
   if (o.coarse_cells > 0) cfg.coarse_cells = o.coarse_cells;
   if (o.coarse_sweeps > 0) cfg.coarse_sweeps = o.coarse_sweeps;
   if (o.small_cells != 0) cfg.small_cells = o.small_cells;
@@ -1933,21 +2139,20 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   const Geo& g = w->g;
   const OpConst& k = w->last_k;
   cudaStream_t s = c->stream;
-  const long long n = (long long)g.NW + g.NU + g.NP, nvv = (long long)g.NW + g.NU;
   cudaEvent_t e0, e1;
   XC_CUDA_TRY(cudaEventCreate(&e0));
   XC_CUDA_TRY(cudaEventCreate(&e1));
   for (int it = -1; it < iters; ++it) {
     if (it == 0) cudaEventRecord(e0, s);
     if (which == 1) {
-      stokes_apply_kernel<double><<<nblk(n), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], w->d.cp, w->d.scl, w->d.t,
+      stokes_apply_kernel<double><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.cp, w->d.scl, w->d.t,
                                                           nullptr, w->d.w); xc_count_launch();
     } else if (which == 2) {
-      vel_jacobi_kernel<float><<<nblk(nvv), 256, 0, s>>>(g, k, w->f.cw[0], w->f.cu[0], w->f.vx[0], w->f.vb[0],
-                                                         w->f.vx2[0], 0.7f, 0); xc_count_launch();
+      vel_sweep2d_kernel<float, 1><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->f, 0), w->f.vx[0], w->f.vb[0],
+                                                               w->f.vx2[0], 0.7f); xc_count_launch();
     } else {
-      vel_jacobi_kernel<double><<<nblk(nvv), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], w->d.vx[0], w->d.vb[0],
-                                                          w->d.vx2[0], 0.7, 0); xc_count_launch();
+      vel_sweep2d_kernel<double, 1><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.vx[0], w->d.vb[0],
+                                                                w->d.vx2[0], 0.7); xc_count_launch();
     }
   }
   cudaEventRecord(e1, s);
