@@ -99,6 +99,9 @@ typedef struct xc_solver_opts {
   int coarse_sweeps;       /* Jacobi sweeps there (4 (Nz + Nx), at least 32; 200 for MMS) */
   int small_cells;         /* levels of at most this many cells run their V-cycle in one CTA
                               (256; -1: none) */
+  int pressure_sweeps;     /* pressure-multigrid Jacobi sweeps before and after each coarse
+                              correction (2) */
+  int inner_gs_passes;     /* mixed: Gram-Schmidt passes of the FP32 inner solve (1; 1 or 2) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {
@@ -269,7 +272,8 @@ void* xc_stream(xc_ctx* ctx);
 long long xc_launch_count(void);
 /* Time one kernel of the path on the context's current state with CUDA
    events on the context stream: `iters` back-to-back launches after one
-   warm-up launch.  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
+   warm-up launch (kernels 1-3: each launch timed alone after a 256 MiB write
+   that evicts L2).  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
    1 FP64 Stokes operator apply, 2 FP32 velocity Jacobi sweep (finest level),
    3 FP64 velocity Jacobi sweep, 4 FFT line filter (z pass of psie),
    5 volume fractions + rheology.  out = {ms per launch, algorithmic bytes per

@@ -73,15 +73,17 @@ class SolverOpts(ctypes.Structure):
                 ("restart", ctypes.c_int), ("inner_rtol", ctypes.c_double), ("inner_maxit", ctypes.c_int),
                 ("smooth_sweeps", ctypes.c_int), ("omega_velocity", ctypes.c_double),
                 ("schur_mass", ctypes.c_double), ("schur_full_diagonal", ctypes.c_int),
-                ("coarse_cells", ctypes.c_int), ("coarse_sweeps", ctypes.c_int), ("small_cells", ctypes.c_int)]
+                ("coarse_cells", ctypes.c_int), ("coarse_sweeps", ctypes.c_int), ("small_cells", ctypes.c_int),
+                ("pressure_sweeps", ctypes.c_int), ("inner_gs_passes", ctypes.c_int)]
 
     @classmethod
     def make(cls, solver="fgmres64", rtol=1e-10, maxit=500, restart=30, inner_rtol=1e-4, inner_maxit=60,
              smooth_sweeps=0, omega_velocity=0.0, schur_mass=0.0, schur_full_diagonal=False,
-             coarse_cells=0, coarse_sweeps=0, small_cells=0):
+             coarse_cells=0, coarse_sweeps=0, small_cells=0, pressure_sweeps=0, inner_gs_passes=0):
         return cls(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit),
                    int(smooth_sweeps), float(omega_velocity), float(schur_mass), int(bool(schur_full_diagonal)),
-                   int(coarse_cells), int(coarse_sweeps), int(small_cells))
+                   int(coarse_cells), int(coarse_sweeps), int(small_cells), int(pressure_sweeps),
+                   int(inner_gs_passes))
 
 
 class SolverStats(ctypes.Structure):
@@ -175,6 +177,26 @@ def build(force: bool = False) -> str:
 def field_names():
     L = lib()
     return [L.xc_field_name(i).decode() for i in range(L.xc_field_count())]
+
+
+# What save_checkpoint writes (src/restart.jl:53-83): every array field of
+# FluidState (src/state.jl:74-122; its solver cache is rebuilt on load) and of
+# PhaseState (src/state.jl:165-258), and the time-evolving NoiseState fields
+# of noise_dynamic_fields (src/restart.jl:25-28).  The noise RNG stays with the
+# caller: the library takes each step's white-noise draws as inputs.
+CHECKPOINT_GROUPS = {
+    "fluid": ("W", "U", "P", "eta", "etaco", "rho", "rhow", "rhou", "Drho", "rhoo", "rhooo", "drhodt",
+              "drhodto", "drhodtoo", "MFS", "rhoWo", "rhoWoo", "rhoUo", "rhoUoo"),
+    "phase": ("x", "m", "X", "M", "Xo", "Xoo", "Mo", "Moo", "chi", "mu", "hasx", "hasm", "chiw", "muw", "chiu",
+              "muu", "x_w", "m_w", "x_u", "m_u", "Drhom", "Drhox", "Pl", "Pt", "etamix", "etae", "ke", "kx",
+              "etat", "etas", "etasw", "ks", "V", "Div_V", "exx", "ezz", "exz", "eII", "vx", "vm", "txx", "tzz",
+              "txz", "tII", "fReL", "ReL", "ReD", "Ra", "fRel", "Rel", "Red", "Rc", "Wx", "Wm", "Ux", "Um", "wx",
+              "wm", "bndtaperw", "bndshape", "advn_X", "advn_M", "advn_rho", "qx_advn_X", "qz_advn_X",
+              "qx_advn_M", "qz_advn_M", "qx_dffn_X", "qz_dffn_X", "qx_dffn_M", "qz_dffn_M", "dffn_X", "Gx",
+              "dXdt", "dXdto", "dXdtoo"),
+    "noise": ("psie", "psix", "psis", "psieo", "psixo", "psiso", "re", "rs", "xiew", "xieu", "xixw", "xixu",
+              "xisw", "xisu", "xie", "xix", "xis"),
+}
 
 
 # ---------------------------------------------------------------------------
@@ -449,6 +471,40 @@ class State:
         out = (ctypes.c_double * 58)()
         _check(lib().xc_history_stats(self._h, out))
         return dict(zip(self.HISTORY_KEYS, out))
+
+    # ---- checkpoints -------------------------------------------------------
+    def checkpoint(self):
+        """The device state as save_checkpoint groups it (src/restart.jl:53-83):
+        {"fluid/<name>", "phase/<name>", "noise/<name>": host array}."""
+        out = {}
+        for group, names in CHECKPOINT_GROUPS.items():
+            for n in names:
+                out[f"{group}/{n}"] = self[n]
+        return out
+
+    def restore(self, ckpt):
+        """Upload every field of a checkpoint dict (load_checkpoint!,
+        src/restart.jl:94-127); sizes must match this context's grid."""
+        for group, names in CHECKPOINT_GROUPS.items():
+            for n in names:
+                self[n] = ckpt[f"{group}/{n}"]
+
+    def save_checkpoint(self, path, time, dt, step):
+        """Write the checkpoint with the reference's dataset names and the
+        meta/time, meta/dt, meta/step scalars to an .npz file (no HDF5
+        writer is available to Python here; the Julia binding writes the
+        reference's JLD2 file through xcore.save_checkpoint)."""
+        d = self.checkpoint()
+        d.update({"meta/time": np.float64(time), "meta/dt": np.float64(dt), "meta/step": np.int64(step)})
+        with open(path, "wb") as f:
+            np.savez(f, **d)
+
+    def load_checkpoint(self, path):
+        """Read a file written by save_checkpoint into this context; returns
+        (time, dt, step) to resume the time loop."""
+        with np.load(path) as z:
+            self.restore({k: z[k] for k in z.files})
+            return float(z["meta/time"]), float(z["meta/dt"]), int(z["meta/step"])
 
     def initialize(self, x_init, re, rs):
         """Fresh-start initialize! -- src/run.jl:71-140 (x_init replaces the

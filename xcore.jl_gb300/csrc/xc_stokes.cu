@@ -161,6 +161,15 @@ struct VOp {
 template <typename T>
 constexpr bool kFly = std::is_same<T, float>::value;
 
+// smoother update r / d: the FP32 preconditioner takes the fast approximate
+// division (2 ulp; d is a positive diagonal far inside its range), FP64 the
+// IEEE one
+template <typename T>
+__device__ __forceinline__ T sdiv(T r, T d) {
+  if constexpr (kFly<T>) return __fdividef(r, d);
+  else return r / d;
+}
+
 // dw / du and the FP32 viscosity copies of one level (terms as vel_coef_kernel)
 template <typename T>
 __global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta,
@@ -444,13 +453,13 @@ __device__ __forceinline__ void vel_update_w(const Geo& g, const OpConst& k, con
                                              const T* b, T* out, T omega, long long t, int j, int i) {
   const bool exact = i == 0 || i == g.Nx + 1 || j == 0 || j == g.Nz;
   if (MODE == 0) {
-    out[t] = (exact ? (T)1 : omega) * b[t] / vel_diag_w<T>(g, op, t, j, i);
+    out[t] = sdiv<T>((exact ? (T)1 : omega) * b[t], vel_diag_w<T>(g, op, t, j, i));
     return;
   }
   T d;
   const T ax = vel_row_w<T, false>(g, k, op, xi, xi + g.NW, nullptr, t, j, i, &d);
   if (MODE == 2) out[t] = b[t] - ax;
-  else out[t] = xi[t] + (exact ? (T)1 : omega) * (b[t] - ax) / d;
+  else out[t] = xi[t] + sdiv<T>((exact ? (T)1 : omega) * (b[t] - ax), d);
 }
 template <typename T, int MODE>
 __device__ __forceinline__ void vel_update_u(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi,
@@ -458,13 +467,13 @@ __device__ __forceinline__ void vel_update_u(const Geo& g, const OpConst& k, con
   const bool exact = j == 0 || j == g.Nz + 1 || (k.mms && (int)u == k.pin_u);
   const long long t = g.NW + u;
   if (MODE == 0) {
-    out[t] = (exact ? (T)1 : omega) * b[t] / vel_diag_u<T>(g, k, op, u, j, i);
+    out[t] = sdiv<T>((exact ? (T)1 : omega) * b[t], vel_diag_u<T>(g, k, op, u, j, i));
     return;
   }
   T d;
   const T ax = vel_row_u<T, false>(g, k, op, xi, xi + g.NW, nullptr, u, j, i, &d);
   if (MODE == 2) out[t] = b[t] - ax;
-  else out[t] = xi[t] + (exact ? (T)1 : omega) * (b[t] - ax) / d;
+  else out[t] = xi[t] + sdiv<T>((exact ? (T)1 : omega) * (b[t] - ax), d);
 }
 // a level's rows on a 2-D grid: thread (j, i) takes W row (j, i) and U row
 // (j, i) -- no index division, and the two rows share viscosity loads
@@ -732,11 +741,11 @@ __device__ __forceinline__ void p_jacobi_at(int Nz, int Nx, const T* __restrict_
   T d;
   if (zero_init) {
     p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, b, j, i, &d);   // only the diagonal is used
-    xo[t] = d > (T)0 ? omega * b[t] / d : (T)0;
+    xo[t] = d > (T)0 ? sdiv<T>(omega * b[t], d) : (T)0;
     return;
   }
   T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, j, i, &d);
-  xo[t] = d > (T)0 ? xi[t] + omega * (b[t] - ax) / d : (T)0;
+  xo[t] = d > (T)0 ? xi[t] + sdiv<T>(omega * (b[t] - ax), d) : (T)0;
 }
 template <typename T>
 __global__ void p_jacobi_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
@@ -818,7 +827,7 @@ __device__ void p_coarse_cta(int Nz, int Nx, const T* __restrict__ kx, const T* 
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
       T d;
       T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, a, t % Nz, t / Nz, &d);
-      o[t] = d > (T)0 ? a[t] + omega * (b[t] - ax) / d : (T)0;
+      o[t] = d > (T)0 ? a[t] + sdiv<T>(omega * (b[t] - ax), d) : (T)0;
     }
     __syncthreads();
     T* tmp = a; a = o; o = tmp;
@@ -1494,6 +1503,8 @@ struct SolveCfg {
   int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
                            // solved by Jacobi sweeps
   int small_cells = 256;   // levels of at most this many cells run in one CTA
+  int nu_p = 2;            // pressure smoothing sweeps before and after each coarse correction
+  int gs_passes = 2;       // classical Gram-Schmidt passes per Arnoldi step
   // Schur approximation (Cahouet-Chabard): S^-1 ~ L_in^-1 + cmass * eta/rho with
   // L_in = DM diag(a1 rho/dt)^-1 GG (kplane 9); kplane 0 builds L from the full
   // velocity diagonal instead (cmass then defaults to 0)
@@ -1587,7 +1598,7 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
       L.kx[q] = H.kx[q]; L.kz[q] = H.kz[q];
       L.x[q] = H.px[q]; L.x2[q] = H.px2[q]; L.b[q] = H.pb[q]; L.r[q] = H.pr[q];
     }
-    p_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, l, lc, cfg.nu, om,
+    p_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, l, lc, cfg.nu_p, om,
                                                             coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]));
     xc_count_launch();
     XC_LAUNCH_CHECK();
@@ -1604,7 +1615,7 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
                                              H.px[l], om, 1); xc_count_launch();
   T* a = H.px[l];
   T* o = H.px2[l];
-  for (int q = 1; q < cfg.nu; ++q) {
+  for (int q = 1; q < cfg.nu_p; ++q) {
     p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
                                                om, 0); xc_count_launch();
     T* tmp = a; a = o; o = tmp;
@@ -1619,7 +1630,7 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
   p_prolong_kernel<T><<<nblk(n), 256, 0, s>>>(Nzc, Nxc, H.px[l + 1], H.px[l]); xc_count_launch();
   a = H.px[l];
   o = H.px2[l];
-  for (int q = 0; q < cfg.nu; ++q) {
+  for (int q = 0; q < cfg.nu_p; ++q) {
     p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
                                                om, 0); xc_count_launch();
     T* tmp = a; a = o; o = tmp;
@@ -1701,7 +1712,7 @@ int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg
   XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
   XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
   double* hd = w->hdev + 8;
-  for (int pass = 0; pass < 2; ++pass) {
+  for (int pass = 0; pass < cfg.gs_passes; ++pass) {
     launch_multidot<T>(n, kk + 1, H.V, n, wv, w->part, s);
     multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, w->part, hd + pass * kMaxRestart); xc_count_launch();
     multiaxpy_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv); xc_count_launch();
@@ -1720,7 +1731,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.cmass); mix(cfg.kplane);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.cmass); mix(cfg.kplane);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -1796,7 +1807,8 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
       XC_TRY(arnoldi_step<T>(w, H, k, cfg, kk, s));
       XC_CUDA_TRY(cudaStreamSynchronize(s));
       XC_LAUNCH_CHECK();
-      for (int i = 0; i <= kk; ++i) Hm[(size_t)kk * (m + 1) + i] = hh[8 + i] + hh[8 + kMaxRestart + i];
+      for (int i = 0; i <= kk; ++i)
+        Hm[(size_t)kk * (m + 1) + i] = hh[8 + i] + (cfg.gs_passes > 1 ? hh[8 + kMaxRestart + i] : 0.0);
       double hn = std::sqrt(hh[2]);
       Hm[(size_t)kk * (m + 1) + kk + 1] = hn;
       // Givens rotations on column kk
@@ -2045,6 +2057,12 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.coarse_cells > 0) cfg.coarse_cells = o.coarse_cells;
   if (o.coarse_sweeps > 0) cfg.coarse_sweeps = o.coarse_sweeps;
   if (o.small_cells != 0) cfg.small_cells = o.small_cells;
+  if (o.pressure_sweeps > 0) cfg.nu_p = o.pressure_sweeps;
+  // the FP32 inner solve only has to reduce its residual by inner_rtol (1e-2
+  // to 3e-2 with at most ~30 basis vectors), so one Gram-Schmidt pass does;
+  // the FP64 solve keeps two
+  SolveCfg icfg = cfg;
+  icfg.gs_passes = o.inner_gs_passes >= 2 ? 2 : 1;
   w->last_k = k;
   w->have_k = true;
   XC_TRY(setup_hier<double>(w, w->d, k, cfg, c, s));
@@ -2089,7 +2107,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       int iits = 0;
       double irr = 1.0;
       // fgmres uses H.w only through its rhs pointer; H.t is scratch for apply
-      XC_TRY(fgmres<float>(w, w->f, k, cfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s));
+      XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s));
       its += iits;
       refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
       XC_LAUNCH_CHECK();
@@ -2139,14 +2157,21 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   const Geo& g = w->g;
   const OpConst& k = w->last_k;
   cudaStream_t s = c->stream;
+  // every launch is timed alone after a write of 256 MiB (twice the L2), so
+  // the time is that of a launch whose operands come from HBM
+  const size_t flush_bytes = 256u << 20;
+  void* flush = nullptr;
+  XC_CUDA_TRY(cudaMalloc(&flush, flush_bytes));
   cudaEvent_t e0, e1;
   XC_CUDA_TRY(cudaEventCreate(&e0));
   XC_CUDA_TRY(cudaEventCreate(&e1));
+  double total_ms = 0;
   for (int it = -1; it < iters; ++it) {
-    if (it == 0) cudaEventRecord(e0, s);
+    cudaMemsetAsync(flush, it & 0xff, flush_bytes, s);
+    cudaEventRecord(e0, s);
     if (which == 1) {
       stokes_apply_kernel<double><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.cp, w->d.scl, w->d.t,
-                                                          nullptr, w->d.w); xc_count_launch();
+                                                              nullptr, w->d.w); xc_count_launch();
     } else if (which == 2) {
       vel_sweep2d_kernel<float, 1><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->f, 0), w->f.vx[0], w->f.vb[0],
                                                                w->f.vx2[0], 0.7f); xc_count_launch();
@@ -2154,18 +2179,27 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
       vel_sweep2d_kernel<double, 1><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.vx[0], w->d.vb[0],
                                                                 w->d.vx2[0], 0.7); xc_count_launch();
     }
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      cudaFree(flush);
+      xc_set_error("xc_bench_kernel: %s", cudaGetErrorString(e));
+      return XC_CUDA;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (it >= 0) total_ms += ms;
   }
-  cudaEventRecord(e1, s);
-  XC_CUDA_TRY(cudaEventSynchronize(e1));
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaFree(flush);
   XC_LAUNCH_CHECK();
   const double cells = (double)g.Nz * g.Nx;
-  out[0] = ms / iters;
-  // algorithmic bytes: read the unknowns and the operator's material fields
-  // (eta, etaco, rho, rhow, rhou), write the result; FP64 88 B/cell, FP32 44 B/cell
+  out[0] = total_ms / iters;
+  // algorithmic bytes: read the unknowns (W, U; and P for the apply) or the
+  // unknowns and the right-hand side (W, U, bW, bU for a sweep) and the
+  // operator's material fields (eta, etaco, rho, rhow, rhou), write the
+  // result: 11 arrays, FP64 88 B/cell, FP32 44 B/cell
   out[1] = (which == 2 ? 44.0 : 88.0) * cells;
   out[2] = 52.0 * cells;            // 2 flops per stencil entry, ~26 entries per cell
   out[3] = cells;

@@ -15,6 +15,8 @@
 #     XcoreGPU.download!(gpu, phase, fluid, ns)
 module XcoreGPU
 
+import xcore
+
 const LIB = joinpath(@__DIR__, "..", "_build", "libxcore_gb300.so")
 
 const SCHEMES = Dict(:centr => 0, :upwd1 => 1, :quick => 2, :fromm => 3, :weno3 => 4, :weno5 => 5, :tvdim => 6)
@@ -37,10 +39,10 @@ end
 struct SolverOpts
     kind::Cint; rtol::Cdouble; maxit::Cint; restart::Cint; inner_rtol::Cdouble; inner_maxit::Cint
     smooth_sweeps::Cint; omega_velocity::Cdouble; schur_mass::Cdouble; schur_full_diagonal::Cint
-    coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint
+    coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint; pressure_sweeps::Cint; inner_gs_passes::Cint
 end
 SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
-    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0)
+    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0)
 
 struct SolverStats
     iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
@@ -104,6 +106,24 @@ end
 
 upload!(ctx::Context, structs...) = foreach_field((n, v) -> upload!(ctx, n, v), structs...)
 download!(ctx::Context, structs...) = foreach_field((n, v) -> download!(ctx, n, v), structs...)
+
+# ---- checkpoints (src/restart.jl:53-127) -------------------------------------------
+# The reference's own JLD2 writer and reader, with the device state moved through
+# download!/upload! (every array of FluidState, PhaseState and the NoiseState
+# fields the library holds).  The noise RNG never leaves Julia -- the library takes
+# each step's white-noise draws as inputs -- so ns.rng is saved and restored by the
+# reference code unchanged, and a GPU run resumes from a CPU checkpoint or the
+# other way round.
+function save_checkpoint(ctx::Context, path, phase, fluid, ns, hst; time, dt, step)
+    download!(ctx, phase, fluid, ns)
+    xcore.save_checkpoint(path, phase, fluid, ns, hst; time = time, dt = dt, step = step)
+end
+
+function load_checkpoint!(ctx::Context, path, phase, fluid, ns, hst)
+    r = xcore.load_checkpoint!(path, phase, fluid, ns, hst)
+    upload!(ctx, phase, fluid, ns)
+    return r
+end
 
 coefs(a1, a2, a3, b1, b2, b3) = Cdouble[a1, a2, a3, b1, b2, b3]
 
