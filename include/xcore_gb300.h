@@ -275,8 +275,8 @@ long long xc_launch_count(void);
    warm-up launch (kernels 1-3: each launch timed alone after a 256 MiB write
    that evicts L2).  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
    1 FP64 Stokes operator apply, 2 FP32 velocity Jacobi sweep (finest level),
-   3 FP64 velocity Jacobi sweep, 4 FFT line filter (z pass of psie),
-   5 volume fractions + rheology.  out = {ms per launch, algorithmic bytes per
+   3 FP64 velocity Jacobi sweep, 4 FFT line filter (z pass of psie).
+   out = {ms per launch, algorithmic bytes per
    launch, algorithmic flops per launch, units per launch}.  Kernels 1-3 need
    a previous xc_fluidmech call (2 needs the mixed solver). */
 int xc_bench_kernel(xc_ctx* ctx, int which, int iters, double out[4]);

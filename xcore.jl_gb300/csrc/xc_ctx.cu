@@ -399,7 +399,9 @@ extern "C" int xc_bench_kernel(xc_ctx* c, int which, int iters, double out[4]) {
   cudaEventDestroy(e1);
   if (st != XC_OK) return st;
   const double cells = (double)Nz * Nx;
-  const double fpc = c->p.ADVN == XC_WENO5 ? 282.0 : (c->p.ADVN == XC_QUICK ? 38.0 : 20.0);
+  // WENO5: two upwind reconstructions per cell (one x face, one z face) of
+  // about 66 flops with 6 divisions each, the flux products and the divergence
+  const double fpc = c->p.ADVN == XC_WENO5 ? 150.0 : (c->p.ADVN == XC_QUICK ? 38.0 : 20.0);
   out[0] = ms / iters;
   out[1] = 48.0 * cells;     // read f, u, w; write adv, qx, qz (8 B each per cell)
   out[2] = fpc * cells;

@@ -83,14 +83,20 @@ __device__ __forceinline__ double face_flux(double s0, double s1, double s2, dou
     double pos = s2 + 0.25 * (s3 - s1);
     double neg = s3 + 0.25 * (s2 - s4);
     return vpos(v) * pos + vneg(v) * neg;
-  } else if (S == XC_WENO3) {
-    double pos = weno3_poly(s1, s2, s3);
-    double neg = weno3_poly(s4, s3, s2);
-    return vpos(v) * pos + vneg(v) * neg;
-  } else if (S == XC_WENO5) {
-    double pos = weno5_poly(s0, s1, s2, s3, s4);
-    double neg = weno5_poly(s5, s4, s3, s2, s1);
-    return vpos(v) * pos + vneg(v) * neg;
+  } else if (S == XC_WENO3 || S == XC_WENO5) {
+    // vpos(v) pos + vneg(v) neg has one weight exactly zero: only the upwind
+    // reconstruction is evaluated.  The dropped term is (+0) x (finite) = +-0,
+    // which changes no value (at most the sign of a zero result); v = +-0
+    // gives 0 and a NaN v stays NaN, as in the full formula.
+    // The mirrored stencil is selected first, so a warp with faces of both
+    // signs still evaluates one polynomial per face.
+    const bool up = v > 0.0;
+    const double a0 = up ? s0 : s5, a1 = up ? s1 : s4, a2 = up ? s2 : s3, a3 = up ? s3 : s2,
+                 a4 = up ? s4 : s1;
+    const double p = S == XC_WENO5 ? weno5_poly(a0, a1, a2, a3, a4) : weno3_poly(a1, a2, a3);
+    if (up) return vpos(v) * p;
+    if (v < 0.0) return vneg(v) * p;
+    return v * 0.0;
   } else {  // XC_TVDIM
     double cpos = vpos(v), cneg = vneg(v);
     double pos = tvd_flux(s1, s2, s3, vpos(vl), cpos);

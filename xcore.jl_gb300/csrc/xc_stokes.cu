@@ -518,110 +518,127 @@ __device__ __forceinline__ void vel_residual_at(const Geo& g, const OpConst& k, 
 }
 
 // restriction of the interior-row residual (full weighting / 4 of the
-// bilinear prolongation); coarse ghost / boundary rows get zero
+// bilinear prolongation); coarse ghost / boundary rows get zero.  W row
+// (J, Ic) and U row (Jr, I) of the coarse level.
 template <typename T>
-__device__ __forceinline__ void vel_restrict_at(const Geo& f, const Geo& c, const T* r, T* bc, long long t) {
-  const int lwf = f.Nz + 1, luf = f.Nz + 2;
-  const T* rw = r;
-  const T* ru = r + f.NW;
+__device__ __forceinline__ T vel_restrict_w(const Geo& f, const Geo& c, const T* rw, int J, int Ic) {
+  const int lwf = f.Nz + 1;
   T acc = 0;
-  if (t < c.NW) {
-    int J = (int)(t % (c.Nz + 1)), Ic = (int)(t / (c.Nz + 1));
-    if (J >= 1 && J <= c.Nz - 1 && Ic >= 1 && Ic <= c.Nx) {
-      int I = Ic - 1;
-      const int ixs[4] = {2 * I - 1, 2 * I, 2 * I + 1, 2 * I + 2};
-      const T wx[4] = {(T)0.25, (T)0.75, (T)0.75, (T)0.25};
-      for (int dj = -1; dj <= 1; ++dj) {
-        T wz = dj == 0 ? (T)1 : (T)0.5;
-        int j = 2 * J + dj;
-        for (int q = 0; q < 4; ++q) {
-          int ix = ixs[q];
-          ix = ix < 0 ? ix + f.Nx : (ix >= f.Nx ? ix - f.Nx : ix);
-          acc += wz * wx[q] * rw[(size_t)(ix + 1) * lwf + j];
-        }
-      }
-      acc *= (T)0.25;
-    }
-    bc[t] = acc;
-    return;
-  }
-  t -= c.NW;
-  int Jr = (int)(t % (c.Nz + 2)), I = (int)(t / (c.Nz + 2));
-  if (Jr >= 1 && Jr <= c.Nz) {
-    int Jc = Jr - 1;
-    const int jzs[4] = {2 * Jc - 1, 2 * Jc, 2 * Jc + 1, 2 * Jc + 2};
-    const T wz[4] = {(T)0.25, (T)0.75, (T)0.75, (T)0.25};
-    for (int q = 0; q < 4; ++q) {
-      int jz = jzs[q];
-      if (jz < 0 || jz >= f.Nz) continue;
-      for (int di = -1; di <= 1; ++di) {
-        int i = 2 * I + di;
-        if (i < 0 || i > f.Nx) continue;
-        T wx = di == 0 ? (T)1 : (T)0.5;
-        acc += wz[q] * wx * ru[(size_t)i * luf + jz + 1];
+  if (J >= 1 && J <= c.Nz - 1 && Ic >= 1 && Ic <= c.Nx) {
+    const int I = Ic - 1;
+    const int ixs[4] = {2 * I - 1, 2 * I, 2 * I + 1, 2 * I + 2};
+    const T wx[4] = {(T)0.25, (T)0.75, (T)0.75, (T)0.25};
+    for (int dj = -1; dj <= 1; ++dj) {
+      const T wz = dj == 0 ? (T)1 : (T)0.5;
+      const int j = 2 * J + dj;
+      for (int q = 0; q < 4; ++q) {
+        int ix = ixs[q];
+        ix = ix < 0 ? ix + f.Nx : (ix >= f.Nx ? ix - f.Nx : ix);
+        acc += wz * wx[q] * rw[(ix + 1) * lwf + j];
       }
     }
     acc *= (T)0.25;
   }
-  bc[c.NW + t] = acc;
+  return acc;
 }
 template <typename T>
-__global__ void vel_restrict_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)c.NW + c.NU) return;
-  vel_restrict_at<T>(f, c, r, bc, t);
+__device__ __forceinline__ T vel_restrict_u(const Geo& f, const Geo& c, const T* ru, int Jr, int I) {
+  const int luf = f.Nz + 2;
+  T acc = 0;
+  if (Jr >= 1 && Jr <= c.Nz) {
+    const int Jc = Jr - 1;
+    const int jzs[4] = {2 * Jc - 1, 2 * Jc, 2 * Jc + 1, 2 * Jc + 2};
+    const T wz[4] = {(T)0.25, (T)0.75, (T)0.75, (T)0.25};
+    for (int q = 0; q < 4; ++q) {
+      const int jz = jzs[q];
+      if (jz < 0 || jz >= f.Nz) continue;
+      for (int di = -1; di <= 1; ++di) {
+        const int i = 2 * I + di;
+        if (i < 0 || i > f.Nx) continue;
+        const T wx = di == 0 ? (T)1 : (T)0.5;
+        acc += wz[q] * wx * ru[i * luf + jz + 1];
+      }
+    }
+    acc *= (T)0.25;
+  }
+  return acc;
+}
+// flat index over the coarse W then U rows (levels stay below 2^31 unknowns)
+template <typename T>
+__device__ __forceinline__ void vel_restrict_at(const Geo& f, const Geo& c, const T* r, T* bc, long long t) {
+  const int tt = (int)t;
+  if (tt < c.NW) {
+    bc[t] = vel_restrict_w<T>(f, c, r, tt % (c.Nz + 1), tt / (c.Nz + 1));
+  } else {
+    const int u = tt - c.NW;
+    bc[t] = vel_restrict_u<T>(f, c, r + f.NW, u % (c.Nz + 2), u / (c.Nz + 2));
+  }
+}
+// 2-D grid over the coarse row positions (grid2 of the coarse level)
+template <typename T>
+__global__ void __launch_bounds__(256) vel_restrict2d_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc) {
+  const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
+  if (j <= c.Nz && i <= c.Nx + 1) bc[i * (c.Nz + 1) + j] = vel_restrict_w<T>(f, c, r, j, i);
+  if (j <= c.Nz + 1 && i <= c.Nx) bc[c.NW + i * (c.Nz + 2) + j] = vel_restrict_u<T>(f, c, r + f.NW, j, i);
 }
 
-// x_f += P x_c (bilinear; ghost rows of U follow the reflection rule)
+// x_f += P x_c (bilinear; ghost rows of U follow the reflection rule): the
+// correction of fine W row (j, i) and fine U row (j, i)
 template <typename T>
-__device__ __forceinline__ void vel_prolong_at(const Geo& f, const Geo& c, const OpConst& k, const T* xc, T* xf,
-                                               long long t) {
-  const int lwc = c.Nz + 1, luc = c.Nz + 2;
-  const T* cw = xc;
-  const T* cu = xc + c.NW;
-  if (t < f.NW) {
-    int j = (int)(t % (f.Nz + 1)), i = (int)(t / (f.Nz + 1));
-    int ix = (i - 1) % f.Nx;
-    if (ix < 0) ix += f.Nx;
-    int I0 = ix / 2;
-    int In = (ix % 2 == 0) ? (I0 - 1 + c.Nx) % c.Nx : (I0 + 1) % c.Nx;
-    T v = 0;
-    int J0 = j / 2;
-    int nz = (j % 2 == 0) ? 1 : 2;
-    for (int q = 0; q < nz; ++q) {
-      int J = J0 + q;
-      T wz = nz == 1 ? (T)1 : (T)0.5;
-      v += wz * ((T)0.75 * cw[(size_t)(I0 + 1) * lwc + J] + (T)0.25 * cw[(size_t)(In + 1) * lwc + J]);
-    }
-    xf[t] += v;
-    return;
+__device__ __forceinline__ T vel_prolong_w(const Geo& f, const Geo& c, const T* cw, int j, int i) {
+  const int lwc = c.Nz + 1;
+  int ix = (i - 1) % f.Nx;
+  if (ix < 0) ix += f.Nx;
+  const int I0 = ix / 2;
+  const int In = (ix % 2 == 0) ? (I0 - 1 + c.Nx) % c.Nx : (I0 + 1) % c.Nx;
+  T v = 0;
+  const int J0 = j / 2;
+  const int nz = (j % 2 == 0) ? 1 : 2;
+  for (int q = 0; q < nz; ++q) {
+    const int J = J0 + q;
+    const T wz = nz == 1 ? (T)1 : (T)0.5;
+    v += wz * ((T)0.75 * cw[(I0 + 1) * lwc + J] + (T)0.25 * cw[(In + 1) * lwc + J]);
   }
-  long long u = t - f.NW;
-  int j = (int)(u % (f.Nz + 2)), i = (int)(u / (f.Nz + 2));
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T vel_prolong_u(const Geo& f, const Geo& c, const OpConst& k, const T* cu, int j, int i) {
+  const int luc = c.Nz + 2;
   auto interior = [&](int jj) -> T {
-    int jz = jj - 1, J0 = jz / 2;
-    int Jn = (jz % 2 == 0) ? J0 : J0 + 2;     // coarse row of the 1/4 neighbour (full layout)
+    const int jz = jj - 1, J0 = jz / 2;
+    const int Jn = (jz % 2 == 0) ? J0 : J0 + 2;     // coarse row of the 1/4 neighbour (full layout)
     T v = 0;
-    int nx = (i % 2 == 0) ? 1 : 2;
-    int I0 = (i % 2 == 0) ? i / 2 : (i - 1) / 2;
+    const int nx = (i % 2 == 0) ? 1 : 2;
+    const int I0 = (i % 2 == 0) ? i / 2 : (i - 1) / 2;
     for (int q = 0; q < nx; ++q) {
-      T wx = nx == 1 ? (T)1 : (T)0.5;
-      int I = I0 + q;
-      v += wx * ((T)0.75 * cu[(size_t)I * luc + J0 + 1] + (T)0.25 * cu[(size_t)I * luc + Jn]);
+      const T wx = nx == 1 ? (T)1 : (T)0.5;
+      const int I = I0 + q;
+      v += wx * ((T)0.75 * cu[I * luc + J0 + 1] + (T)0.25 * cu[I * luc + Jn]);
     }
     return v;
   };
-  T v;
-  if (j == 0) v = -(T)k.top_cnv * interior(1);
-  else if (j == f.Nz + 1) v = -(T)k.bot_cnv * interior(f.Nz);
-  else v = interior(j);
-  xf[t] += v;
+  if (j == 0) return -(T)k.top_cnv * interior(1);
+  if (j == f.Nz + 1) return -(T)k.bot_cnv * interior(f.Nz);
+  return interior(j);
 }
 template <typename T>
-__global__ void vel_prolong_kernel(Geo f, Geo c, OpConst k, const T* __restrict__ xc, T* xf) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)f.NW + f.NU) return;
-  vel_prolong_at<T>(f, c, k, xc, xf, t);
+__device__ __forceinline__ void vel_prolong_at(const Geo& f, const Geo& c, const OpConst& k, const T* xc, T* xf,
+                                               long long t) {
+  const int tt = (int)t;
+  if (tt < f.NW) {
+    xf[t] += vel_prolong_w<T>(f, c, xc, tt % (f.Nz + 1), tt / (f.Nz + 1));
+  } else {
+    const int u = tt - f.NW;
+    xf[t] += vel_prolong_u<T>(f, c, k, xc + c.NW, u % (f.Nz + 2), u / (f.Nz + 2));
+  }
+}
+// 2-D grid over the fine row positions (grid2 of the fine level)
+template <typename T>
+__global__ void __launch_bounds__(256) vel_prolong2d_kernel(Geo f, Geo c, OpConst k, const T* __restrict__ xc,
+                                                            T* xf) {
+  const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
+  if (j <= f.Nz && i <= f.Nx + 1) xf[i * (f.Nz + 1) + j] += vel_prolong_w<T>(f, c, xc, j, i);
+  if (j <= f.Nz + 1 && i <= f.Nx) xf[f.NW + i * (f.Nz + 2) + j] += vel_prolong_u<T>(f, c, k, xc + c.NW, j, i);
 }
 
 // coarse coefficient fields: eta (avg4), etaco (injection), rho (avg4),
@@ -1570,10 +1587,10 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
   vel_sweep2d_kernel<T, 2><<<grid2(g), blk2(), 0, s>>>(g, k, op, H.vx[l], H.vb[l], H.vr[l], om); xc_count_launch();
   const Geo& c = H.vg[l + 1];
-  vel_restrict_kernel<T><<<nblk((long long)c.NW + c.NU), 256, 0, s>>>(g, c, H.vr[l], H.vb[l + 1]); xc_count_launch();
+  vel_restrict2d_kernel<T><<<grid2(c), blk2(), 0, s>>>(g, c, H.vr[l], H.vb[l + 1]); xc_count_launch();
   XC_LAUNCH_CHECK();
   XC_TRY(vcycle_vel<T>(H, kf, cfg, l + 1, s));
-  vel_prolong_kernel<T><<<nblk(n), 256, 0, s>>>(g, c, k, H.vx[l + 1], H.vx[l]); xc_count_launch();
+  vel_prolong2d_kernel<T><<<grid2(g), blk2(), 0, s>>>(g, c, k, H.vx[l + 1], H.vx[l]); xc_count_launch();
   a = H.vx[l];
   o = H.vx2[l];
   for (int q = 0; q < cfg.nu; ++q) {

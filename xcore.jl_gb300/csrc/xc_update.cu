@@ -58,8 +58,11 @@ __global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rho
   double Xf12 = a1 * f2 + (1.0 - a1) * Sf12;
   double Xf21 = a2 * f1 + (1.0 - a2) * Sf21;
   double Xf22 = a2 * f2 + (1.0 - a2) * Sf22;
-  double thtv1 = pow(r.ex / r.ex, Xf11) * pow(r.em / r.ex, Xf12);
-  double thtv2 = pow(r.ex / r.em, Xf21) * pow(r.em / r.em, Xf22);
+  // update.jl:170-171 multiply by pow(ex/ex, Xf11) and pow(em/em, Xf22): with
+  // positive finite ex, em those are pow(1, y) = 1 exactly, and x * 1 = x, so
+  // the two FP64 pow calls are left out without changing a bit
+  double thtv1 = pow(r.em / r.ex, Xf12);
+  double thtv2 = pow(r.ex / r.em, Xf21);
   double etaf1 = r.ex * thtv1, etaf2 = r.em * thtv2;
   AT(etamix, j, i) = f1 * etaf1 + f2 * etaf2;
 }
