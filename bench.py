@@ -279,6 +279,11 @@ def main():
         peaks = json.load(open(pk))
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = rk[1] / (rk[0] * 1e-3) / 1e9
+    # DRAM bytes (read + write) per cell of one launch, measured by one ncu
+    # capture of each kernel on this workload at 1024^2, scaled to this grid
+    ncu_bytes_per_cell = {0: 25.23e6 / 1048576, 1: (235.73e6 + 18.77e6) / 1048576, 2: 33.64e6 / 1048576,
+                          3: (185.02e6 + 11.52e6) / 1048576, 4: 8.43e6 / 1048576}
+    traffic = ncu_bytes_per_cell[a.roofline_kernel] * rk[3] if a.roofline_kernel in ncu_bytes_per_cell else None
     ms_t = torch.tensor([ms, ms_e2e, ms_plain or 0.0], dtype=torch.float64, device="cuda")
     if world > 1:
         import torch.distributed as dist
@@ -296,8 +301,8 @@ def main():
                "sample": f"one {a.sweeps}-sweep time step at 256^2 ({times[0]:.1f} s on this host) scaled by the "
                          f"cell-count ratio {scale:g} to {N}^2; numpy + SciPy SuperLU, single-threaded"}
     names = {0: "advect_tile_kernel (WENO5, one field)", 1: "stokes_apply_kernel<double>",
-             2: "vel_sweep2d_kernel<float,1> (finest-level velocity Jacobi sweep, L2 evicted before each launch)",
-             3: "vel_sweep2d_kernel<double,1> (finest-level velocity Jacobi sweep, L2 evicted before each launch)",
+             2: "vel_sweep2d_kernel<float,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
+             3: "vel_sweep2d_kernel<double,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
              4: "line_filter_kernel (FFT z pass)"}
     out = {
         "metric": METRIC,
@@ -327,7 +332,7 @@ def main():
         "e2e": {"value": world * 1e3 / ms_e2e, "unit": "timesteps/s", "h2d_bytes_per_step": 2 * 8 * N * N,
                 "d2h_bytes_per_step": 8 * N * N},
         "roofline": {"kernel": names.get(a.roofline_kernel), "bound": "hbm", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
                      "peak_source": "measured" if peaks else "fallback",
                      "ms_per_launch": rk[0], "algorithmic_bytes_per_launch": rk[1],
                      "algorithmic_flops_per_launch": rk[2], "units_per_launch": rk[3]},

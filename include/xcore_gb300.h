@@ -272,8 +272,9 @@ void* xc_stream(xc_ctx* ctx);
 long long xc_launch_count(void);
 /* Time one kernel of the path on the context's current state with CUDA
    events on the context stream: `iters` back-to-back launches after one
-   warm-up launch (kernels 1-3: each launch timed alone after a 256 MiB write
-   that evicts L2).  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
+   warm-up launch (kernel 1: each launch timed alone after a 256 MiB write
+   that evicts L2; kernels 2, 3: back to back over copies of the operands that
+   together exceed twice the L2).  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
    1 FP64 Stokes operator apply, 2 FP32 velocity Jacobi sweep (finest level),
    3 FP64 velocity Jacobi sweep, 4 FFT line filter (z pass of psie).
    out = {ms per launch, algorithmic bytes per

@@ -529,6 +529,35 @@ class State:
                     solver_rel_residual=st.solver_rel_residual, dt_next=st.dt_next)
 
 
+class Ensemble:
+    """Independent instances -- grid sizes, parameters and noise seeds may all
+    differ -- advanced together on one GPU.  Every member is a ``State`` with
+    its own device context and CUDA stream; one host thread per member drives
+    it (ctypes releases the GIL for the duration of each library call), so the
+    kernels of different members overlap on the GPU where one small instance
+    alone would leave it idle between launches.  Results are those of the
+    members stepped one after another: each context computes deterministically
+    on its own stream."""
+
+    def __init__(self, members, threads=None):
+        from concurrent.futures import ThreadPoolExecutor
+        self.members = list(members)
+        self._pool = ThreadPoolExecutor(max_workers=threads or max(1, len(self.members)))
+
+    def step(self, steps, dts, draws, **solver):
+        """One time step of every member: ``steps[i]``, ``dts[i]`` and the
+        noise draws ``draws[i] = (re, rs)`` of member i; returns the members'
+        step statistics in order."""
+        futs = [self._pool.submit(m.step, steps[i], dts[i], draws[i][0], draws[i][1], **solver)
+                for i, m in enumerate(self.members)]
+        return [f.result() for f in futs]
+
+    def close(self):
+        self._pool.shutdown()
+        for m in self.members:
+            m.close()
+
+
 # ---------------------------------------------------------------------------
 # stencil-level functions on device arrays (torch CUDA tensors laid out
 # column-major: a (rows, cols) Julia matrix is a contiguous torch tensor of

@@ -364,10 +364,11 @@ extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double*
 // ---------------------------------------------------------------------------
 // instrumentation
 // ---------------------------------------------------------------------------
-long long g_xc_launches = 0;
+std::atomic<long long> g_xc_launches{0};
+thread_local long long g_xc_thread_launches = 0;
 
 extern "C" void* xc_stream(xc_ctx* c) { return c ? (void*)c->stream : nullptr; }
-extern "C" long long xc_launch_count(void) { return g_xc_launches; }
+extern "C" long long xc_launch_count(void) { return g_xc_launches.load(); }
 
 int noise_bench_zpass(xc_ctx* c, int iters, double out[4]);
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <cstddef>
 #include <cstdio>
 #include <string>
@@ -93,9 +94,15 @@ void xc_set_error(const char* fmt, ...);
 
 #define XC_LAUNCH_CHECK() XC_CUDA_TRY(cudaGetLastError())
 
-// number of kernels this library has launched (host side, process-wide)
-extern long long g_xc_launches;
-inline void xc_count_launch() { ++g_xc_launches; }
+// number of kernels this library has launched (host side): process-wide, and
+// per host thread for the bookkeeping of stream capture (contexts may be
+// driven from several threads at once)
+extern std::atomic<long long> g_xc_launches;
+extern thread_local long long g_xc_thread_launches;
+inline void xc_count_launch() {
+  ++g_xc_thread_launches;
+  g_xc_launches.fetch_add(1, std::memory_order_relaxed);
+}
 
 #define XC_TRY(expr)               \
   do {                             \

@@ -230,14 +230,16 @@ __device__ __forceinline__ RowW<T> plane_row(const T* __restrict__ c, size_t N, 
   w.c5 = c[5 * N + t]; w.c6 = c[6 * N + t]; w.c7 = c[7 * N + t]; w.c8 = c[8 * N + t];
   return w;
 }
-// weights of interior W row t = (j, i) and interior U row u = (j, i)
+// weights of interior W row t = (j, i) and interior U row u = (j, i).  Index
+// arithmetic is 32-bit (a level holds fewer than 2^31 unknowns) and each
+// neighbour is an offset from one base pointer.
 template <typename T>
 __device__ __forceinline__ RowW<T> w_row(const Geo& g, const VOp<T>& op, long long t, int j, int i) {
   if constexpr (kFly<T>) {
     const int Nz = g.Nz;
-    return fly_row<T>(op.etaco[(size_t)(i - 1) * (Nz + 1) + j], op.etaco[(size_t)i * (Nz + 1) + j],
-                      op.eta[(size_t)(i - 1) * Nz + j - 1], op.eta[(size_t)(i - 1) * Nz + j], op.dw[t],
-                      (T)(g.invh * g.invh));
+    const T* pc = op.etaco + ((i - 1) * (Nz + 1) + j);    // corners (j, i-1), (j, i)
+    const T* pe = op.eta + ((i - 1) * Nz + j - 1);        // cells (j-1, i-1), (j, i-1)
+    return fly_row<T>(pc[0], pc[Nz + 1], pe[0], pe[1], op.dw[t], (T)(g.invh * g.invh));
   } else {
     return plane_row<T>(op.cw, (size_t)g.NW, t);
   }
@@ -247,8 +249,8 @@ __device__ __forceinline__ RowW<T> u_row(const Geo& g, const VOp<T>& op, long lo
   if constexpr (kFly<T>) {
     const int Nz = g.Nz, Nx = g.Nx;
     const int ia = (i == 0) ? Nx - 1 : i - 1, ib = (i == Nx) ? 0 : i;
-    return fly_row<T>(op.etaco[(size_t)i * (Nz + 1) + j - 1], op.etaco[(size_t)i * (Nz + 1) + j],
-                      op.eta[(size_t)ia * Nz + j - 1], op.eta[(size_t)ib * Nz + j - 1], op.du[u],
+    const T* pc = op.etaco + (i * (Nz + 1) + j - 1);      // corners (j-1, i), (j, i)
+    return fly_row<T>(pc[0], pc[1], op.eta[ia * Nz + j - 1], op.eta[ib * Nz + j - 1], op.du[u],
                       (T)(g.invh * g.invh));
   } else {
     return plane_row<T>(op.cu, (size_t)g.NU, u);
@@ -272,16 +274,21 @@ __device__ __forceinline__ T vel_row_w(const Geo& g, const OpConst& k, const VOp
   }
   const RowW<T> c = w_row<T>(g, op, t, j, i);
   *dg = c.d;
-  T s = c.d * xw[t];
-  s += c.c1 * xw[t - 1];
-  s += c.c2 * xw[t + 1];
-  s += c.c3 * xw[t - lw];
-  s += c.c4 * xw[t + lw];
-  s += c.c5 * xu[(size_t)(i - 1) * lu + j];
-  s += c.c6 * xu[(size_t)(i - 1) * lu + j + 1];
-  s += c.c7 * xu[(size_t)i * lu + j];
-  s += c.c8 * xu[(size_t)i * lu + j + 1];
-  if (FULL) s += (T)g.invh * (xp[(size_t)i * lu + j + 1] - xp[(size_t)i * lu + j]);
+  const T* pw = xw + t;                          // W(j, i)
+  const T* pu = xu + ((i - 1) * lu + j);         // U(j, i-1)
+  T s = c.d * pw[0];
+  s += c.c1 * pw[-1];
+  s += c.c2 * pw[1];
+  s += c.c3 * pw[-lw];
+  s += c.c4 * pw[lw];
+  s += c.c5 * pu[0];
+  s += c.c6 * pu[1];
+  s += c.c7 * pu[lu];
+  s += c.c8 * pu[lu + 1];
+  if (FULL) {
+    const T* pp = xp + (i * lu + j);
+    s += (T)g.invh * (pp[1] - pp[0]);
+  }
   return s;
 }
 template <typename T, bool FULL>
@@ -294,16 +301,21 @@ __device__ __forceinline__ T vel_row_u(const Geo& g, const OpConst& k, const VOp
   const int il = (i == 0) ? Nx - 1 : i - 1, ir = (i == Nx) ? 1 : i + 1;
   const RowW<T> c = u_row<T>(g, op, u, j, i);
   *dg = c.d;
-  T s = c.d * xu[u];
-  s += c.c1 * xu[(size_t)il * lu + j];
-  s += c.c2 * xu[(size_t)ir * lu + j];
-  s += c.c3 * xu[u - 1];
-  s += c.c4 * xu[u + 1];
-  s += c.c5 * xw[(size_t)i * lw + j - 1];
-  s += c.c6 * xw[(size_t)(i + 1) * lw + j - 1];
-  s += c.c7 * xw[(size_t)i * lw + j];
-  s += c.c8 * xw[(size_t)(i + 1) * lw + j];
-  if (FULL) s += (T)g.invh * (xp[(size_t)(i + 1) * lu + j] - xp[(size_t)i * lu + j]);
+  const T* pu = xu + u;                          // U(j, i)
+  const T* pw = xw + (i * lw + j - 1);           // W(j-1, i)
+  T s = c.d * pu[0];
+  s += c.c1 * xu[il * lu + j];
+  s += c.c2 * xu[ir * lu + j];
+  s += c.c3 * pu[-1];
+  s += c.c4 * pu[1];
+  s += c.c5 * pw[0];
+  s += c.c6 * pw[lw];
+  s += c.c7 * pw[1];
+  s += c.c8 * pw[lw + 1];
+  if (FULL) {
+    const T* pp = xp + (i * lu + j);
+    s += (T)g.invh * (pp[lu] - pp[0]);
+  }
   return s;
 }
 // diagonal alone (the first Jacobi sweep from zero needs nothing else)
@@ -1769,19 +1781,22 @@ int arnoldi_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cf
   if (!H.gexec[kk]) {
     cudaGraph_t graph = nullptr;
     XC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const long long before = g_xc_launches;
+    // launches recorded into the graph run only when it is launched: count
+    // them from this thread's counter and take them out of the totals
+    const long long before = g_xc_thread_launches;
     int st = arnoldi_launches<T>(w, H, k, cfg, kk, s);
     cudaError_t e = cudaStreamEndCapture(s, &graph);
     if (st != XC_OK) { if (graph) cudaGraphDestroy(graph); return st; }
     if (e != cudaSuccess) { xc_set_error("graph capture failed: %s", cudaGetErrorString(e)); return XC_CUDA; }
-    H.gnodes[kk] = g_xc_launches - before;
-    g_xc_launches = before;
+    H.gnodes[kk] = g_xc_thread_launches - before;
+    g_xc_thread_launches = before;
+    g_xc_launches.fetch_sub(H.gnodes[kk]);
     e = cudaGraphInstantiate(&H.gexec[kk], graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) { H.gexec[kk] = nullptr; xc_set_error("graph instantiate: %s", cudaGetErrorString(e)); return XC_CUDA; }
   }
   XC_CUDA_TRY(cudaGraphLaunch(H.gexec[kk], s));
-  g_xc_launches += H.gnodes[kk];
+  g_xc_launches.fetch_add(H.gnodes[kk]);
   return XC_OK;
 }
 
@@ -1919,6 +1934,11 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
 int stokes_create(xc_ctx* c) {
   c->stokes = nullptr;
   if (c->Nz < 4 || c->Nx < 4) return XC_OK;   // no solver for tiny grids
+  // the kernels index a level's unknowns with 32-bit integers
+  if (3LL * (c->Nz + 2) * (c->Nx + 2) >= (1LL << 31)) {
+    xc_set_error("stokes: grid %dx%d has too many unknowns for 32-bit indexing", c->Nz, c->Nx);
+    return XC_BAD_ARG;
+  }
   StokesWork* w = new StokesWork();
   std::memset((void*)w, 0, sizeof(StokesWork));
   c->stokes = w;
@@ -2165,6 +2185,76 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
 }
 
 // CUDA-event timing of one solver kernel on the last solve's operator
+// Timing of the fine-level Jacobi sweep on copies of its operands (viscosity
+// fields or coefficient planes, unknowns, right-hand side, result) that
+// together exceed twice the L2: launches cycle through the copies back to back,
+// so each reads operands the others have evicted and no launch gap is timed.
+template <typename T>
+int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H, int iters, float* ms_out) {
+  const size_t nvv = (size_t)g.NW + g.NU;
+  std::vector<std::pair<const void*, size_t>> src;   // operand, bytes
+  if (kFly<T>) {
+    src = {{H.feta[0], sizeof(T) * g.Nz * g.Nx}, {H.fetaco[0], sizeof(T) * (g.Nz + 1) * (g.Nx + 1)},
+           {H.fdw[0], sizeof(T) * g.NW}, {H.fdu[0], sizeof(T) * g.NU}};
+  } else {
+    src = {{H.cw[0], sizeof(T) * 10 * g.NW}, {H.cu[0], sizeof(T) * 10 * g.NU}};
+  }
+  src.push_back({H.vx[0], sizeof(T) * nvv});
+  src.push_back({H.vb[0], sizeof(T) * nvv});
+  src.push_back({H.vx2[0], sizeof(T) * nvv});
+  size_t per_copy = 0;
+  for (auto& a : src) per_copy += a.second;
+  const size_t l2x2 = (size_t)2 * 132 * 1000 * 1000;
+  const int nc = (int)std::max<size_t>(2, (l2x2 + per_copy - 1) / per_copy + 1);
+  std::vector<std::vector<void*>> cp(nc, std::vector<void*>(src.size(), nullptr));
+  int st = XC_OK;
+  for (int q = 0; q < nc && st == XC_OK; ++q)
+    for (size_t a = 0; a < src.size(); ++a) {
+      if (cudaMalloc(&cp[q][a], src[a].second) != cudaSuccess ||
+          cudaMemcpyAsync(cp[q][a], src[a].first, src[a].second, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+        xc_set_error("xc_bench_kernel: operand copies: %s", cudaGetErrorString(cudaGetLastError()));
+        st = XC_CUDA;
+        break;
+      }
+    }
+  auto op_of = [&](int q) {
+    VOp<T> o{};
+    const auto& v = cp[q];
+    if (kFly<T>) {
+      o.eta = (const T*)v[0]; o.etaco = (const T*)v[1]; o.dw = (const T*)v[2]; o.du = (const T*)v[3];
+    } else {
+      o.cw = (const T*)v[0]; o.cu = (const T*)v[1];
+    }
+    return o;
+  };
+  const size_t xo = src.size() - 3;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (st == XC_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) st = XC_CUDA;
+  if (st == XC_OK) {
+    for (int it = -nc; it < iters; ++it) {   // one untimed pass over all copies first
+      if (it == 0) cudaEventRecord(e0, s);
+      const int q = ((it % nc) + nc) % nc;
+      vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op_of(q), (const T*)cp[q][xo],
+                                                           (const T*)cp[q][xo + 1], (T*)cp[q][xo + 2], (T)0.7);
+      xc_count_launch();
+    }
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      xc_set_error("xc_bench_kernel: %s", cudaGetErrorString(e));
+      st = XC_CUDA;
+    } else {
+      cudaEventElapsedTime(ms_out, e0, e1);
+      *ms_out /= (float)iters;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  for (auto& v : cp)
+    for (void* p : v) cudaFree(p);
+  return st;
+}
+
 int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   StokesWork* w = c->stokes;
   if (!w || !w->have_k || (which == 2 && !w->f_alloc)) {
@@ -2174,8 +2264,22 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   const Geo& g = w->g;
   const OpConst& k = w->last_k;
   cudaStream_t s = c->stream;
-  // every launch is timed alone after a write of 256 MiB (twice the L2), so
-  // the time is that of a launch whose operands come from HBM
+  const double cells = (double)g.Nz * g.Nx;
+  // algorithmic bytes: read the unknowns (W, U; and P for the apply) or the
+  // unknowns and the right-hand side (W, U, bW, bU for a sweep) and the
+  // operator's material fields (eta, etaco, rho, rhow, rhou), write the
+  // result: 11 arrays, FP64 88 B/cell, FP32 44 B/cell
+  out[1] = (which == 2 ? 44.0 : 88.0) * cells;
+  out[2] = 52.0 * cells;            // 2 flops per stencil entry, ~26 entries per cell
+  out[3] = cells;
+  if (which == 2 || which == 3) {
+    float ms = 0;
+    XC_TRY(which == 2 ? sweep_bench<float>(s, g, k, w->f, iters, &ms) : sweep_bench<double>(s, g, k, w->d, iters, &ms));
+    out[0] = ms;
+    return XC_OK;
+  }
+  // the apply: every launch is timed alone after a write of 256 MiB (twice the
+  // L2), so the time is that of a launch whose operands come from HBM
   const size_t flush_bytes = 256u << 20;
   void* flush = nullptr;
   XC_CUDA_TRY(cudaMalloc(&flush, flush_bytes));
@@ -2186,16 +2290,8 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   for (int it = -1; it < iters; ++it) {
     cudaMemsetAsync(flush, it & 0xff, flush_bytes, s);
     cudaEventRecord(e0, s);
-    if (which == 1) {
-      stokes_apply_kernel<double><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.cp, w->d.scl, w->d.t,
-                                                              nullptr, w->d.w); xc_count_launch();
-    } else if (which == 2) {
-      vel_sweep2d_kernel<float, 1><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->f, 0), w->f.vx[0], w->f.vb[0],
-                                                               w->f.vx2[0], 0.7f); xc_count_launch();
-    } else {
-      vel_sweep2d_kernel<double, 1><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.vx[0], w->d.vb[0],
-                                                                w->d.vx2[0], 0.7); xc_count_launch();
-    }
+    stokes_apply_kernel<double><<<grid2(g), blk2(), 0, s>>>(g, k, vop(w->d, 0), w->d.cp, w->d.scl, w->d.t,
+                                                            nullptr, w->d.w); xc_count_launch();
     cudaEventRecord(e1, s);
     cudaError_t e = cudaEventSynchronize(e1);
     if (e != cudaSuccess) {
@@ -2211,14 +2307,6 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   cudaEventDestroy(e1);
   cudaFree(flush);
   XC_LAUNCH_CHECK();
-  const double cells = (double)g.Nz * g.Nx;
   out[0] = total_ms / iters;
-  // algorithmic bytes: read the unknowns (W, U; and P for the apply) or the
-  // unknowns and the right-hand side (W, U, bW, bU for a sweep) and the
-  // operator's material fields (eta, etaco, rho, rhow, rhou), write the
-  // result: 11 arrays, FP64 88 B/cell, FP32 44 B/cell
-  out[1] = (which == 2 ? 44.0 : 88.0) * cells;
-  out[2] = 52.0 * cells;            // 2 flops per stencil entry, ~26 entries per cell
-  out[3] = cells;
   return XC_OK;
 }
