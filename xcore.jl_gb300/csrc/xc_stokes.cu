@@ -21,6 +21,7 @@
 // iterative refinement on the FP64 residual.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -1112,7 +1113,7 @@ __global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, T* rv) {
 // Krylov vector kernels
 // ---------------------------------------------------------------------------
 constexpr int KB = 256;
-constexpr int KG = 6 * kNumSMs;   // one wave of the 8-accumulator multidot (40 registers): 1536 threads per SM
+constexpr int KGMAX = 8 * kNumSMs;   // partial-sum slots: at most 8 CTAs of 256 threads per SM
 
 // partial dot products of w with V[0..m) -> part[blk * m + k], m <= MAXK.
 // One pass: w is read once, every thread keeps m running sums in the working
@@ -1127,7 +1128,7 @@ __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const 
   T acc[MAXK];
 #pragma unroll
   for (int k = 0; k < MAXK; ++k) acc[k] = (T)0;
-  const long long stride = (long long)KG * KB;
+  const long long stride = (long long)gridDim.x * KB;
   long long t = blockIdx.x * (long long)KB + threadIdx.x;
   for (; t + stride < n; t += 2 * stride) {
     const T w0 = w[t], w1 = w[t + stride];
@@ -1161,11 +1162,11 @@ __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const 
     part[(size_t)blockIdx.x * m + threadIdx.x] = s;
   }
 }
-__global__ void multidot_final_kernel(int m, const double* __restrict__ part, double* out) {
+__global__ void multidot_final_kernel(int m, int nb, const double* __restrict__ part, double* out) {
   int k = blockIdx.x;
   __shared__ double sh[KB];
   double acc = 0;
-  for (int b = threadIdx.x; b < KG; b += KB) acc += part[(size_t)b * m + k];
+  for (int b = threadIdx.x; b < nb; b += KB) acc += part[(size_t)b * m + k];
   sh[threadIdx.x] = acc;
   __syncthreads();
   for (int s = KB / 2; s > 0; s >>= 1) {
@@ -1175,10 +1176,10 @@ __global__ void multidot_final_kernel(int m, const double* __restrict__ part, do
   if (threadIdx.x == 0) out[k] = sh[0];
 }
 // ||v||^2 from one partial column -> *nrm2, and 1/||v|| (1 for a zero norm) -> *inv
-__global__ void norm_final_kernel(const double* __restrict__ part, double* nrm2, double* inv) {
+__global__ void norm_final_kernel(int nb, const double* __restrict__ part, double* nrm2, double* inv) {
   __shared__ double sh[KB];
   double acc = 0;
-  for (int b = threadIdx.x; b < KG; b += KB) acc += part[b];
+  for (int b = threadIdx.x; b < nb; b += KB) acc += part[b];
   sh[threadIdx.x] = acc;
   __syncthreads();
   for (int s = KB / 2; s > 0; s >>= 1) {
@@ -1709,20 +1710,45 @@ int apply_scaled(StokesWork* w, Hier<T>& H, const OpConst& k, const T* v, const 
   return XC_OK;
 }
 
-// partial dots of wv with V[0..m), accumulator count chosen from m
+// Grid of each multidot variant: one wave of as many CTAs as its register use
+// lets an SM hold (more accumulators, fewer CTAs), queried once per process.
+int g_md_grid[2][3];   // [FP32, FP64][8, 16, 32 accumulators]
+std::once_flag g_md_once;
+void md_grid_init() {
+  int dev = 0, sms = kNumSMs;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  auto grid = [&](const void* fn) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, KB, 0) != cudaSuccess || b < 1) b = 1;
+    return std::min(std::min(b, 8) * sms, KGMAX);
+  };
+  g_md_grid[0][0] = grid((const void*)multidot_kernel<float, 8>);
+  g_md_grid[0][1] = grid((const void*)multidot_kernel<float, 16>);
+  g_md_grid[0][2] = grid((const void*)multidot_kernel<float, 32>);
+  g_md_grid[1][0] = grid((const void*)multidot_kernel<double, 8>);
+  g_md_grid[1][1] = grid((const void*)multidot_kernel<double, 16>);
+  g_md_grid[1][2] = grid((const void*)multidot_kernel<double, 32>);
+}
+
+// partial dots of wv with V[0..m), accumulator count chosen from m; returns
+// the number of partial rows written
 template <typename T>
-void launch_multidot(long long n, int m, const T* V, long long ldv, const T* wv, double* part, cudaStream_t s) {
-  if (m <= 8) multidot_kernel<T, 8><<<KG, KB, 0, s>>>(n, m, V, ldv, wv, part);
-  else if (m <= 16) multidot_kernel<T, 16><<<KG, KB, 0, s>>>(n, m, V, ldv, wv, part);
-  else multidot_kernel<T, 32><<<KG, KB, 0, s>>>(n, m, V, ldv, wv, part);
+int launch_multidot(long long n, int m, const T* V, long long ldv, const T* wv, double* part, cudaStream_t s) {
+  const int* gr = g_md_grid[std::is_same<T, float>::value ? 0 : 1];
+  int nb;
+  if (m <= 8) multidot_kernel<T, 8><<<(nb = gr[0]), KB, 0, s>>>(n, m, V, ldv, wv, part);
+  else if (m <= 16) multidot_kernel<T, 16><<<(nb = gr[1]), KB, 0, s>>>(n, m, V, ldv, wv, part);
+  else multidot_kernel<T, 32><<<(nb = gr[2]), KB, 0, s>>>(n, m, V, ldv, wv, part);
   xc_count_launch();
+  return nb;
 }
 
 // ||v||^2 -> hdev[slot] (device), deterministic; 1/||v|| -> hdev[6]
 template <typename T>
 int dot_self(StokesWork* w, Hier<T>& H, const T* v, long long n, int slot, cudaStream_t s) {
-  launch_multidot<T>(n, 1, v, n, v, w->part, s);
-  norm_final_kernel<<<1, KB, 0, s>>>(w->part, w->hdev + slot, w->hdev + 6); xc_count_launch();
+  const int nb = launch_multidot<T>(n, 1, v, n, v, w->part, s);
+  norm_final_kernel<<<1, KB, 0, s>>>(nb, w->part, w->hdev + slot, w->hdev + 6); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -1742,8 +1768,8 @@ int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg
   XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
   double* hd = w->hdev + 8;
   for (int pass = 0; pass < cfg.gs_passes; ++pass) {
-    launch_multidot<T>(n, kk + 1, H.V, n, wv, w->part, s);
-    multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, w->part, hd + pass * kMaxRestart); xc_count_launch();
+    const int nb = launch_multidot<T>(n, kk + 1, H.V, n, wv, w->part, s);
+    multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, nb, w->part, hd + pass * kMaxRestart); xc_count_launch();
     multiaxpy_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv); xc_count_launch();
   }
   XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
@@ -1939,6 +1965,7 @@ int stokes_create(xc_ctx* c) {
     xc_set_error("stokes: grid %dx%d has too many unknowns for 32-bit indexing", c->Nz, c->Nx);
     return XC_BAD_ARG;
   }
+  std::call_once(g_md_once, md_grid_init);
   StokesWork* w = new StokesWork();
   std::memset((void*)w, 0, sizeof(StokesWork));
   c->stokes = w;
@@ -1957,7 +1984,7 @@ int stokes_create(xc_ctx* c) {
   XC_CUDA_TRY(cudaMalloc(&w->RR, sizeof(double) * n));
   XC_CUDA_TRY(cudaMalloc(&w->x, sizeof(double) * n));
   XC_CUDA_TRY(cudaMalloc(&w->r, sizeof(double) * n));
-  XC_CUDA_TRY(cudaMalloc(&w->part, sizeof(double) * KG * (kMaxRestart + 1)));
+  XC_CUDA_TRY(cudaMalloc(&w->part, sizeof(double) * KGMAX * (kMaxRestart + 1)));
   XC_CUDA_TRY(cudaMalloc(&w->hdev, sizeof(double) * (8 + 2 * kMaxRestart)));
   XC_CUDA_TRY(cudaMallocHost(&w->hhost, sizeof(double) * (8 + 2 * kMaxRestart + kMaxRestart)));
   const int Nz = g.Nz, Nx = g.Nx;
