@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--roofline-kernel", type=int, default=2)
+    ap.add_argument("--knob", action="append", default=[],
+                    help="extra solver option key=value for the timed solves (e.g. pressure_sweeps=2)")
     ap.add_argument("--profile-kernel", type=int, default=None,
                     help="initialise, run the warm-up steps, then launch only this kernel (xc_bench_kernel "
                          "index) 3 times inside the NVTX range 'xc_profile' and exit (for ncu)")
@@ -204,6 +206,9 @@ def main():
         draws.append(pair)
     st.initialize(x0, draws[0][0], draws[0][1])
     sopt = dict(solver=a.solver, rtol=a.rtol, maxit=400, inner_rtol=3e-2, inner_maxit=30, pressure_sweeps=1)
+    for kv in a.knob:
+        key, val = kv.split("=", 1)
+        sopt[key] = float(val) if any(ch in val for ch in ".e") else int(val)
     dt = st.scales["dt0"]
     step = 0
     k = 1
