@@ -102,6 +102,8 @@ typedef struct xc_solver_opts {
   int pressure_sweeps;     /* pressure-multigrid Jacobi sweeps before and after each coarse
                               correction (2) */
   int inner_gs_passes;     /* mixed: Gram-Schmidt passes of the FP32 inner solve (1; 1 or 2) */
+  int serial_launch;       /* 1: plain stream order inside the solver's CUDA graphs instead of
+                              programmatic dependent launch (same results) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

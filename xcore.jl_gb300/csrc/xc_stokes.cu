@@ -24,11 +24,39 @@
 #include <mutex>
 #include <cstring>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "xc_internal.cuh"
 
 namespace {
+
+// Programmatic dependent launch: every kernel of this unit first waits for the
+// grid it depends on to finish and flush its memory (a no-op when launched
+// without the attribute), so the solver's graph-captured launches may be
+// issued with programmatic serialization -- the next kernel is scheduled while
+// the previous one drains instead of after it, hiding the launch gap.
+#define XC_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+
+// programmatic launches on (the default) or off for the solves of this thread
+thread_local bool g_xc_pdl = true;
+#define PDL_ON g_xc_pdl
+
+template <typename... KArgs, typename... Args>
+void pdl(bool on, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = on ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+  xc_count_launch();
+}
 
 constexpr int kMaxLevels = 12;
 constexpr int kMaxRestart = 64;
@@ -72,6 +100,7 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
                                 const double* __restrict__ etaco, const double* __restrict__ rho,
                                 const double* __restrict__ rhow, const double* __restrict__ rhou,
                                 T* cw, T* cu) {
+  XC_PDL_WAIT();
   const int Nz = g.Nz, Nx = g.Nx;
   const double invh = g.invh, invh2 = invh * invh;
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -177,6 +206,7 @@ __global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
                                 const double* __restrict__ etaco, const double* __restrict__ rho,
                                 const double* __restrict__ rhow, const double* __restrict__ rhou,
                                 T* feta, T* fetaco, T* dw, T* du) {
+  XC_PDL_WAIT();
   const int Nz = g.Nz, Nx = g.Nx;
   const double invh = g.invh;
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -383,6 +413,7 @@ __device__ __forceinline__ T p_row(const Geo& g, const OpConst& k, const T* __re
 // DM coefficients of the interior P rows (fluidmech.jl:373-386)
 __global__ void p_coef_kernel(Geo g, const double* __restrict__ rhow, const double* __restrict__ rhou,
                               double* cp) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.NP) return;
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
@@ -404,6 +435,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) stokes_apply_kernel(Geo g, OpConst k, VOp<T> op, const T* __restrict__ cp,
                                                            const T* __restrict__ scl, const T* __restrict__ tv,
                                                            const T* __restrict__ b, T* y) {
+  XC_PDL_WAIT();
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int i = blockIdx.y * 8 + threadIdx.y;
   const int Nz = g.Nz, Nx = g.Nx;
@@ -432,16 +464,19 @@ __global__ void __launch_bounds__(256) stokes_apply_kernel(Geo g, OpConst k, VOp
 
 template <typename T>
 __global__ void mul_kernel(long long n, const T* __restrict__ a, const T* __restrict__ b, T* out) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) out[t] = a[t] * b[t];
 }
 template <typename T>
 __global__ void div_kernel(long long n, const T* __restrict__ a, const T* __restrict__ b, T* out) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) out[t] = a[t] / b[t];
 }
 template <typename A, typename B>
 __global__ void convert_kernel(long long n, const A* __restrict__ a, B* out) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) out[t] = (B)a[t];
 }
@@ -449,6 +484,7 @@ __global__ void convert_kernel(long long n, const A* __restrict__ a, B* out) {
 template <typename T>
 __global__ void refine_update_kernel(long long n, const T* __restrict__ dy, const double* __restrict__ scl,
                                      double* x) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) x[t] += scl[t] * (double)dy[t];
 }
@@ -493,6 +529,7 @@ __device__ __forceinline__ void vel_update_u(const Geo& g, const OpConst& k, con
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) vel_sweep2d_kernel(Geo g, OpConst k, VOp<T> op, const T* __restrict__ xi,
                                                           const T* __restrict__ b, T* out, T omega) {
+  XC_PDL_WAIT();
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int i = blockIdx.y * 8 + threadIdx.y;
   if (j <= g.Nz && i <= g.Nx + 1)
@@ -590,6 +627,7 @@ __device__ __forceinline__ void vel_restrict_at(const Geo& f, const Geo& c, cons
 // 2-D grid over the coarse row positions (grid2 of the coarse level)
 template <typename T>
 __global__ void __launch_bounds__(256) vel_restrict2d_kernel(Geo f, Geo c, const T* __restrict__ r, T* bc) {
+  XC_PDL_WAIT();
   const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
   if (j <= c.Nz && i <= c.Nx + 1) bc[i * (c.Nz + 1) + j] = vel_restrict_w<T>(f, c, r, j, i);
   if (j <= c.Nz + 1 && i <= c.Nx) bc[c.NW + i * (c.Nz + 2) + j] = vel_restrict_u<T>(f, c, r + f.NW, j, i);
@@ -649,6 +687,7 @@ __device__ __forceinline__ void vel_prolong_at(const Geo& f, const Geo& c, const
 template <typename T>
 __global__ void __launch_bounds__(256) vel_prolong2d_kernel(Geo f, Geo c, OpConst k, const T* __restrict__ xc,
                                                             T* xf) {
+  XC_PDL_WAIT();
   const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
   if (j <= f.Nz && i <= f.Nx + 1) xf[i * (f.Nz + 1) + j] += vel_prolong_w<T>(f, c, xc, j, i);
   if (j <= f.Nz + 1 && i <= f.Nx) xf[f.NW + i * (f.Nz + 2) + j] += vel_prolong_u<T>(f, c, k, xc + c.NW, j, i);
@@ -661,6 +700,7 @@ __global__ void coarsen_fields_kernel(int Nzc, int Nxc, const double* __restrict
                                       const double* __restrict__ rhow, const double* __restrict__ rhou,
                                       double* etac, double* etacoc, double* rhoc, double* rhowc,
                                       double* rhouc) {
+  XC_PDL_WAIT();
   int J = blockIdx.x * blockDim.x + threadIdx.x;
   int I = blockIdx.y * blockDim.y + threadIdx.y;
   const int Nz = 2 * Nzc;
@@ -738,6 +778,7 @@ __device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const VOp<T>& op,
 template <typename T>
 __global__ void vel_coarse_kernel(Geo g, OpConst k, VOp<T> op, T* x, T* x2, const T* __restrict__ b, int sweeps,
                                   T omega) {
+  XC_PDL_WAIT();
   vel_coarse_cta<T>(g, k, op, x, x2, b, sweeps, omega);
 }
 
@@ -781,6 +822,7 @@ template <typename T>
 __global__ void p_jacobi_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
                                 T dpin, const T* __restrict__ xi, const T* __restrict__ b, T* xo, T omega,
                                 int zero_init) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= Nz * Nx) return;
   p_jacobi_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, b, xo, omega, zero_init, t);
@@ -795,6 +837,7 @@ __device__ __forceinline__ void p_residual_at(int Nz, int Nx, const T* __restric
 template <typename T>
 __global__ void p_residual_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
                                   T dpin, const T* __restrict__ x, const T* __restrict__ b, T* r) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= Nz * Nx) return;
   p_residual_at<T>(Nz, Nx, kx, kz, pin, dpin, x, b, r, t);
@@ -809,6 +852,7 @@ __device__ __forceinline__ void p_restrict_at(int Nzc, int Nxc, const T* r, T* b
 }
 template <typename T>
 __global__ void p_restrict_kernel(int Nzc, int Nxc, const T* __restrict__ r, T* bc) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= Nzc * Nxc) return;
   p_restrict_at<T>(Nzc, Nxc, r, bc, t);
@@ -827,6 +871,7 @@ __device__ __forceinline__ void p_prolong_at(int Nzc, int Nxc, const T* xc, T* x
 }
 template <typename T>
 __global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* xf) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 4 * Nzc * Nxc) return;
   p_prolong_at<T>(Nzc, Nxc, xc, xf, t);
@@ -835,6 +880,7 @@ __global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* 
 template <typename T>
 __global__ void p_coarsen_kernel(int Nzc, int Nxc, const T* __restrict__ kx, const T* __restrict__ kz,
                                  T* kxc, T* kzc) {
+  XC_PDL_WAIT();
   int J = blockIdx.x * blockDim.x + threadIdx.x;
   int I = blockIdx.y * blockDim.y + threadIdx.y;
   const int Nz = 2 * Nzc;
@@ -869,6 +915,7 @@ __device__ void p_coarse_cta(int Nz, int Nx, const T* __restrict__ kx, const T* 
 template <typename T>
 __global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
                                 T dpin, T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+  XC_PDL_WAIT();
   p_coarse_cta<T>(Nz, Nx, kx, kz, pin, dpin, x, x2, b, sweeps, omega);
 }
 
@@ -926,6 +973,7 @@ __host__ __device__ __forceinline__ OpConst level_const(const OpConst& k, int l)
 template <typename T>
 __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> L, OpConst kf, int l0, int lc, int nu,
                                                                 T om, int csweeps) {
+  XC_PDL_WAIT();
   for (int l = l0; l < lc; ++l) {
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
@@ -990,6 +1038,7 @@ __device__ void p_smooth_cta(const PLevels<T>& L, int l, T om, int sweeps, bool 
 template <typename T>
 __global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> L, int l0, int lc, int nu, T om,
                                                               int csweeps) {
+  XC_PDL_WAIT();
   for (int l = l0; l < lc; ++l) {
     const int Nz = L.Nz[l], Nx = L.Nx[l], n = Nz * Nx;
     p_smooth_cta<T>(L, l, om, nu, true);
@@ -1016,6 +1065,7 @@ template <typename T>
 __global__ void p_kcoef_kernel(Geo g, const double* __restrict__ rhow, const double* __restrict__ rhou,
                                const double* __restrict__ cw, const double* __restrict__ cu, int plane, T* kx,
                                T* kz, T* kr) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx;
   const double ih2 = g.invh * g.invh;
@@ -1052,6 +1102,7 @@ __global__ void p_kcoef_kernel(Geo g, const double* __restrict__ rhow, const dou
 template <typename T>
 __global__ void p_gather_kernel(Geo g, const T* __restrict__ kx, const T* __restrict__ kr,
                                 const T* __restrict__ rp, T* rin) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
   if (t >= Nz * Nx) return;
@@ -1065,6 +1116,7 @@ __global__ void p_gather_kernel(Geo g, const T* __restrict__ kx, const T* __rest
 template <typename T>
 __global__ void p_scatter_kernel(Geo g, const T* __restrict__ z, const T* __restrict__ rp,
                                  const T* __restrict__ etarho, T cmass, T* zp) {
+  XC_PDL_WAIT();
   // interior cells: z + cmass * (eta/rho) * r
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, lp = Nz + 2;
@@ -1076,6 +1128,7 @@ __global__ void p_scatter_kernel(Geo g, const T* __restrict__ z, const T* __rest
 // ghost columns then ghost rows: P_g = r_g + P_neighbour (fluidmech.jl:403-417)
 template <typename T>
 __global__ void p_scatter_cols_kernel(Geo g, const T* __restrict__ rp, T* zp) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
   if (j < 1 || j > Nz) return;
@@ -1084,6 +1137,7 @@ __global__ void p_scatter_cols_kernel(Geo g, const T* __restrict__ rp, T* zp) {
 }
 template <typename T>
 __global__ void p_scatter_rows_kernel(Geo g, const T* __restrict__ rp, T* zp) {
+  XC_PDL_WAIT();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, lp = Nz + 2;
   if (i >= g.Nx + 2) return;
@@ -1095,6 +1149,7 @@ __global__ void p_scatter_rows_kernel(Geo g, const T* __restrict__ rp, T* zp) {
 // r_v' = r_v - GG z_p on interior velocity rows (fluidmech.jl:343-356)
 template <typename T>
 __global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, T* rv) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
   if (t < g.NW) {
@@ -1124,6 +1179,7 @@ constexpr int KGMAX = 8 * kNumSMs;   // partial-sum slots: at most 8 CTAs of 256
 template <typename T, int MAXK>
 __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
                                                       const T* __restrict__ w, double* part) {
+  XC_PDL_WAIT();
   __shared__ double sh[KB / 32][MAXK];
   T acc[MAXK];
 #pragma unroll
@@ -1163,6 +1219,7 @@ __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const 
   }
 }
 __global__ void multidot_final_kernel(int m, int nb, const double* __restrict__ part, double* out) {
+  XC_PDL_WAIT();
   int k = blockIdx.x;
   __shared__ double sh[KB];
   double acc = 0;
@@ -1177,6 +1234,7 @@ __global__ void multidot_final_kernel(int m, int nb, const double* __restrict__ 
 }
 // ||v||^2 from one partial column -> *nrm2, and 1/||v|| (1 for a zero norm) -> *inv
 __global__ void norm_final_kernel(int nb, const double* __restrict__ part, double* nrm2, double* inv) {
+  XC_PDL_WAIT();
   __shared__ double sh[KB];
   double acc = 0;
   for (int b = threadIdx.x; b < nb; b += KB) acc += part[b];
@@ -1195,6 +1253,7 @@ __global__ void norm_final_kernel(int nb, const double* __restrict__ part, doubl
 template <typename T>
 __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
                                  const double* __restrict__ h, T* w) {
+  XC_PDL_WAIT();
   __shared__ T hs[32];
   if (threadIdx.x < m) hs[threadIdx.x] = (T)h[threadIdx.x];
   __syncthreads();
@@ -1208,6 +1267,7 @@ __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, lo
 template <typename T>
 __global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long long ldz,
                                const double* __restrict__ y, T* x) {
+  XC_PDL_WAIT();
   __shared__ T ys[64];
   if (threadIdx.x < m) ys[threadIdx.x] = (T)y[threadIdx.x];
   __syncthreads();
@@ -1221,6 +1281,7 @@ __global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long
 // reciprocal in front of a barrier stalls every CTA of the grid)
 template <typename T>
 __global__ void scale_kernel(long long n, const double* __restrict__ inv, const T* __restrict__ w, T* v) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) v[t] = w[t] * (T)__ldg(inv);
 }
@@ -1228,6 +1289,7 @@ __global__ void scale_kernel(long long n, const double* __restrict__ inv, const 
 // host reports as breakdown)
 template <typename T>
 __global__ void normalize_kernel(long long n, const double* __restrict__ inv, T* v) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) v[t] = v[t] * (T)__ldg(inv);
 }
@@ -1238,6 +1300,7 @@ __global__ void normalize_kernel(long long n, const double* __restrict__ inv, T*
 // momentum-advection inputs (fluidmech.jl:236-240, 310-314)
 __global__ void mom_prep_kernel(int Nz, int Nx, CView W, CView U, CView rhow, CView rhou, double* fz,
                                 double* uz, double* wz, double* fx, double* ux, double* wxm) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   // z-momentum grid (Nz-1, Nx): f (Nz-1, Nx), u (Nz-1, Nx+1), w (Nz, Nx)
@@ -1265,6 +1328,7 @@ __global__ void rhs_kernel(Geo g, RhsArgs a, CView Drho, CView rhoWo, CView rhoW
                            const double* __restrict__ mfs_mean, const double* __restrict__ src_w,
                            const double* __restrict__ src_u, const double* __restrict__ src_p,
                            double pin_p_val, double pin_u_val, double* RR) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx;
   const long long n = (long long)g.NW + g.NU + g.NP;
@@ -1311,6 +1375,7 @@ __global__ void rhs_kernel(Geo g, RhsArgs a, CView Drho, CView rhoWo, CView rhoW
 __global__ void mfs_kernel(int Nz, int Nx, double a1, double a2, double a3, double b1, double b2, double b3,
                            double dt, double alpha, CView rho, CView rhoo, CView rhooo, CView advn_rho,
                            DView drhodt, CView drhodto, CView drhodtoo, DView MFS) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -1327,6 +1392,7 @@ __global__ void mfs_kernel(int Nz, int Nx, double a1, double a2, double a3, doub
 // scl = 1 / (sqrt|diag LL| + extra) (fluidmech.jl:496-501)
 __global__ void scl_kernel(Geo g, OpConst k, const double* __restrict__ cw, const double* __restrict__ cu,
                            CView rho, CView eta, double* scl, double* etarho) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long n = (long long)g.NW + g.NU + g.NP;
   if (t >= n) return;
@@ -1348,6 +1414,7 @@ __global__ void scl_kernel(Geo g, OpConst k, const double* __restrict__ cw, cons
 
 // write the solution back (x is the physical unknown vector)
 __global__ void unpack_kernel(Geo g, const double* __restrict__ x, DView W, DView U, DView P) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < g.NW) { W.p[t] = x[t]; return; }
   t -= g.NW;
@@ -1356,6 +1423,7 @@ __global__ void unpack_kernel(Geo g, const double* __restrict__ x, DView W, DVie
   if (t < g.NP) P.p[t] = x[g.NW + g.NU + t];
 }
 __global__ void pack_kernel(Geo g, CView W, CView U, CView P, double* x) {
+  XC_PDL_WAIT();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < g.NW) { x[t] = W.p[t]; return; }
   t -= g.NW;
@@ -1535,6 +1603,7 @@ struct SolveCfg {
   int small_cells = 256;   // levels of at most this many cells run in one CTA
   int nu_p = 2;            // pressure smoothing sweeps before and after each coarse correction
   int gs_passes = 2;       // classical Gram-Schmidt passes per Arnoldi step
+  bool pdl = true;         // programmatic dependent launch inside the captured graphs
   // Schur approximation (Cahouet-Chabard): S^-1 ~ L_in^-1 + cmass * eta/rho with
   // L_in = DM diag(a1 rho/dt)^-1 GG (kplane 9); kplane 0 builds L from the full
   // velocity diagonal instead (cmass then defaults to 0)
@@ -1576,38 +1645,37 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
       L.g[q] = H.vg[q]; L.op[q] = vop(H, q);
       L.x[q] = H.vx[q]; L.x2[q] = H.vx2[q]; L.b[q] = H.vb[q]; L.r[q] = H.vr[q];
     }
-    vel_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, kf, l, lc, cfg.nu, om,
+    pdl(PDL_ON, vel_vcycle_small_kernel<T>, 1, coarse_threads(n), s, L, kf, l, lc, cfg.nu, om,
                                                               coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx));
-    xc_count_launch();
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
   if (vel_coarsest(H, cfg, l)) {
-    vel_coarse_kernel<T><<<1, coarse_threads(n), 0, s>>>(g, k, vop(H, l), H.vx[l], H.vx2[l], H.vb[l],
-                                                        coarse_sweeps(cfg, g.Nz, g.Nx), om); xc_count_launch();
+    pdl(PDL_ON, vel_coarse_kernel<T>, 1, coarse_threads(n), s, g, k, vop(H, l), H.vx[l], H.vx2[l], H.vb[l],
+                                                        coarse_sweeps(cfg, g.Nz, g.Nx), om);
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
   // pre-smoothing (first sweep from zero)
   const VOp<T> op = vop(H, l);
-  vel_sweep2d_kernel<T, 0><<<grid2(g), blk2(), 0, s>>>(g, k, op, H.vx[l], H.vb[l], H.vx[l], om); xc_count_launch();
+  pdl(PDL_ON, vel_sweep2d_kernel<T, 0>, grid2(g), blk2(), s, g, k, op, H.vx[l], H.vb[l], H.vx[l], om);
   T* a = H.vx[l];
   T* o = H.vx2[l];
   for (int q = 1; q < cfg.nu; ++q) {
-    vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op, a, H.vb[l], o, om); xc_count_launch();
+    pdl(PDL_ON, vel_sweep2d_kernel<T, 1>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], o, om);
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-  vel_sweep2d_kernel<T, 2><<<grid2(g), blk2(), 0, s>>>(g, k, op, H.vx[l], H.vb[l], H.vr[l], om); xc_count_launch();
+  pdl(PDL_ON, vel_sweep2d_kernel<T, 2>, grid2(g), blk2(), s, g, k, op, H.vx[l], H.vb[l], H.vr[l], om);
   const Geo& c = H.vg[l + 1];
-  vel_restrict2d_kernel<T><<<grid2(c), blk2(), 0, s>>>(g, c, H.vr[l], H.vb[l + 1]); xc_count_launch();
+  pdl(PDL_ON, vel_restrict2d_kernel<T>, grid2(c), blk2(), s, g, c, H.vr[l], H.vb[l + 1]);
   XC_LAUNCH_CHECK();
   XC_TRY(vcycle_vel<T>(H, kf, cfg, l + 1, s));
-  vel_prolong2d_kernel<T><<<grid2(g), blk2(), 0, s>>>(g, c, k, H.vx[l + 1], H.vx[l]); xc_count_launch();
+  pdl(PDL_ON, vel_prolong2d_kernel<T>, grid2(g), blk2(), s, g, c, k, H.vx[l + 1], H.vx[l]);
   a = H.vx[l];
   o = H.vx2[l];
   for (int q = 0; q < cfg.nu; ++q) {
-    vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op, a, H.vb[l], o, om); xc_count_launch();
+    pdl(PDL_ON, vel_sweep2d_kernel<T, 1>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], o, om);
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
@@ -1628,41 +1696,39 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
       L.kx[q] = H.kx[q]; L.kz[q] = H.kz[q];
       L.x[q] = H.px[q]; L.x2[q] = H.px2[q]; L.b[q] = H.pb[q]; L.r[q] = H.pr[q];
     }
-    p_vcycle_small_kernel<T><<<1, coarse_threads(n), 0, s>>>(L, l, lc, cfg.nu_p, om,
+    pdl(PDL_ON, p_vcycle_small_kernel<T>, 1, coarse_threads(n), s, L, l, lc, cfg.nu_p, om,
                                                             coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]));
-    xc_count_launch();
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
   if (p_coarsest(H, cfg, l)) {
-    p_coarse_kernel<T><<<1, coarse_threads(n), 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l],
+    pdl(PDL_ON, p_coarse_kernel<T>, 1, coarse_threads(n), s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l],
                                                       H.px2[l], H.pb[l], coarse_sweeps(cfg, Nz, Nx), om);
-    xc_count_launch();
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
-  p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
-                                             H.px[l], om, 1); xc_count_launch();
+  pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
+                                             H.px[l], om, 1);
   T* a = H.px[l];
   T* o = H.px2[l];
   for (int q = 1; q < cfg.nu_p; ++q) {
-    p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
-                                               om, 0); xc_count_launch();
+    pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                               om, 0);
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.px[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.px[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-  p_residual_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
-                                               H.pr[l]); xc_count_launch();
+  pdl(PDL_ON, p_residual_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
+                                               H.pr[l]);
   const int Nzc = H.pNz[l + 1], Nxc = H.pNx[l + 1];
-  p_restrict_kernel<T><<<nblk(Nzc * Nxc), 256, 0, s>>>(Nzc, Nxc, H.pr[l], H.pb[l + 1]); xc_count_launch();
+  pdl(PDL_ON, p_restrict_kernel<T>, nblk(Nzc * Nxc), 256, s, Nzc, Nxc, H.pr[l], H.pb[l + 1]);
   XC_LAUNCH_CHECK();
   XC_TRY(vcycle_p<T>(H, cfg, l + 1, s));
-  p_prolong_kernel<T><<<nblk(n), 256, 0, s>>>(Nzc, Nxc, H.px[l + 1], H.px[l]); xc_count_launch();
+  pdl(PDL_ON, p_prolong_kernel<T>, nblk(n), 256, s, Nzc, Nxc, H.px[l + 1], H.px[l]);
   a = H.px[l];
   o = H.px2[l];
   for (int q = 0; q < cfg.nu_p; ++q) {
-    p_jacobi_kernel<T><<<nblk(n), 256, 0, s>>>(Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
-                                               om, 0); xc_count_launch();
+    pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                               om, 0);
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.px[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.px[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
@@ -1678,22 +1744,22 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   const long long n = (long long)g.NW + g.NU + g.NP;
   const long long nvv = (long long)g.NW + g.NU;
   // physical residual r = S^-1 v -> velocity part into vb[0], pressure into rp
-  div_kernel<T><<<nblk(nvv), 256, 0, s>>>(nvv, v, H.scl, H.vb[0]); xc_count_launch();
-  div_kernel<T><<<nblk(g.NP), 256, 0, s>>>(g.NP, v + nvv, H.scl + nvv, H.rp); xc_count_launch();
+  pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, v, H.scl, H.vb[0]);
+  pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, v + nvv, H.scl + nvv, H.rp);
   // pressure: interior solve with ghost elimination
-  p_gather_kernel<T><<<nblk(g.Nz * g.Nx), 256, 0, s>>>(g, H.kx[0], H.kr, H.rp, H.pb[0]); xc_count_launch();
+  pdl(PDL_ON, p_gather_kernel<T>, nblk(g.Nz * g.Nx), 256, s, g, H.kx[0], H.kr, H.rp, H.pb[0]);
   XC_LAUNCH_CHECK();
   XC_TRY(vcycle_p<T>(H, cfg, 0, s));
   T* zp = out + nvv;   // physical z_p written directly into out, rescaled below
-  p_scatter_kernel<T><<<nblk((long long)g.Nz * g.Nx), 256, 0, s>>>(g, H.px[0], H.rp, H.etarho, (T)cfg.cmass, zp); xc_count_launch();
-  p_scatter_cols_kernel<T><<<nblk(g.Nz + 1), 256, 0, s>>>(g, H.rp, zp); xc_count_launch();
-  p_scatter_rows_kernel<T><<<nblk(g.Nx + 2), 256, 0, s>>>(g, H.rp, zp); xc_count_launch();
+  pdl(PDL_ON, p_scatter_kernel<T>, nblk((long long)g.Nz * g.Nx), 256, s, g, H.px[0], H.rp, H.etarho, (T)cfg.cmass, zp);
+  pdl(PDL_ON, p_scatter_cols_kernel<T>, nblk(g.Nz + 1), 256, s, g, H.rp, zp);
+  pdl(PDL_ON, p_scatter_rows_kernel<T>, nblk(g.Nx + 2), 256, s, g, H.rp, zp);
   // velocity: rhs r_v - GG z_p, one V-cycle
-  sub_grad_kernel<T><<<nblk(nvv), 256, 0, s>>>(g, zp, H.vb[0]); xc_count_launch();
+  pdl(PDL_ON, sub_grad_kernel<T>, nblk(nvv), 256, s, g, zp, H.vb[0]);
   XC_LAUNCH_CHECK();
   XC_TRY(vcycle_vel<T>(H, k, cfg, 0, s));
-  div_kernel<T><<<nblk(nvv), 256, 0, s>>>(nvv, H.vx[0], H.scl, out); xc_count_launch();
-  div_kernel<T><<<nblk(g.NP), 256, 0, s>>>(g.NP, zp, H.scl + nvv, zp); xc_count_launch();
+  pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, H.vx[0], H.scl, out);
+  pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, zp, H.scl + nvv, zp);
   XC_LAUNCH_CHECK();
   (void)n;
   return XC_OK;
@@ -1704,8 +1770,8 @@ template <typename T>
 int apply_scaled(StokesWork* w, Hier<T>& H, const OpConst& k, const T* v, const T* b, T* y, cudaStream_t s) {
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
-  mul_kernel<T><<<nblk(n), 256, 0, s>>>(n, v, H.scl, H.t); xc_count_launch();
-  stokes_apply_kernel<T><<<grid2(g), blk2(), 0, s>>>(g, k, vop(H, 0), H.cp, H.scl, H.t, b, y); xc_count_launch();
+  pdl(PDL_ON, mul_kernel<T>, nblk(n), 256, s, n, v, H.scl, H.t);
+  pdl(PDL_ON, stokes_apply_kernel<T>, grid2(g), blk2(), s, g, k, vop(H, 0), H.cp, H.scl, H.t, b, y);
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -1737,10 +1803,9 @@ template <typename T>
 int launch_multidot(long long n, int m, const T* V, long long ldv, const T* wv, double* part, cudaStream_t s) {
   const int* gr = g_md_grid[std::is_same<T, float>::value ? 0 : 1];
   int nb;
-  if (m <= 8) multidot_kernel<T, 8><<<(nb = gr[0]), KB, 0, s>>>(n, m, V, ldv, wv, part);
-  else if (m <= 16) multidot_kernel<T, 16><<<(nb = gr[1]), KB, 0, s>>>(n, m, V, ldv, wv, part);
-  else multidot_kernel<T, 32><<<(nb = gr[2]), KB, 0, s>>>(n, m, V, ldv, wv, part);
-  xc_count_launch();
+  if (m <= 8) pdl(PDL_ON, multidot_kernel<T, 8>, (nb = gr[0]), KB, s, n, m, V, ldv, wv, part);
+  else if (m <= 16) pdl(PDL_ON, multidot_kernel<T, 16>, (nb = gr[1]), KB, s, n, m, V, ldv, wv, part);
+  else pdl(PDL_ON, multidot_kernel<T, 32>, (nb = gr[2]), KB, s, n, m, V, ldv, wv, part);
   return nb;
 }
 
@@ -1748,7 +1813,7 @@ int launch_multidot(long long n, int m, const T* V, long long ldv, const T* wv, 
 template <typename T>
 int dot_self(StokesWork* w, Hier<T>& H, const T* v, long long n, int slot, cudaStream_t s) {
   const int nb = launch_multidot<T>(n, 1, v, n, v, w->part, s);
-  norm_final_kernel<<<1, KB, 0, s>>>(nb, w->part, w->hdev + slot, w->hdev + 6); xc_count_launch();
+  pdl(PDL_ON, norm_final_kernel, 1, KB, s, nb, w->part, w->hdev + slot, w->hdev + 6);
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -1769,11 +1834,11 @@ int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg
   double* hd = w->hdev + 8;
   for (int pass = 0; pass < cfg.gs_passes; ++pass) {
     const int nb = launch_multidot<T>(n, kk + 1, H.V, n, wv, w->part, s);
-    multidot_final_kernel<<<kk + 1, KB, 0, s>>>(kk + 1, nb, w->part, hd + pass * kMaxRestart); xc_count_launch();
-    multiaxpy_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv); xc_count_launch();
+    pdl(PDL_ON, multidot_final_kernel, kk + 1, KB, s, kk + 1, nb, w->part, hd + pass * kMaxRestart);
+    pdl(PDL_ON, multiaxpy_kernel<T>, nblk(n), 256, s, n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv);
   }
   XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
-  normalize_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, wv); xc_count_launch();
+  pdl(PDL_ON, normalize_kernel<T>, nblk(n), 256, s, n, w->hdev + 6, wv);
   XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
   XC_LAUNCH_CHECK();
   return XC_OK;
@@ -1786,7 +1851,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.cmass); mix(cfg.kplane);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -2122,6 +2187,8 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.coarse_sweeps > 0) cfg.coarse_sweeps = o.coarse_sweeps;
   if (o.small_cells != 0) cfg.small_cells = o.small_cells;
   if (o.pressure_sweeps > 0) cfg.nu_p = o.pressure_sweeps;
+  cfg.pdl = !o.serial_launch;
+  g_xc_pdl = cfg.pdl;
   // the FP32 inner solve only has to reduce its residual by inner_rtol (1e-2
   // to 3e-2 with at most ~30 basis vectors), so one Gram-Schmidt pass does;
   // the FP64 solve keeps two
