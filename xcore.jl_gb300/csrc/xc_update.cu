@@ -28,6 +28,7 @@ __device__ __forceinline__ double clampd(double x, double lo, double hi) {
 
 struct Rheo {
   double A11, A12, A21, A22, B11, B12, B21, B22, iC11, iC12, iC21, iC22, ex, em;
+  double lmx, lxm;   // log(em / ex), log(ex / em)
 };
 
 // compute_volfrac_kernel! (update.jl:18-35) fused with compute_rheology_kernel!
@@ -48,8 +49,13 @@ __global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rho
   size_t o = (size_t)i * Nz + j;
   hasx[o] = xc >= XC_SQRT_EPS;
   hasm[o] = mc >= XC_SQRT_EPS;
-  double s11 = pow(f1 / r.B11, r.iC11), s12 = pow(f2 / r.B12, r.iC12);
-  double s21 = pow(f1 / r.B21, r.iC21), s22 = pow(f2 / r.B22, r.iC22);
+  // The powers of update.jl:153-171 as exp(y log x): pow carries its log in
+  // extra precision, which costs about twice the FP64 work; the relative error
+  // of exp(y log x) is |y log x| eps, below 2e-14 for these operands (f >= eps,
+  // 1/C and the fractions Xf of order one), far inside the 1e-12 bound of
+  // these fields.
+  double s11 = exp(r.iC11 * log(f1 / r.B11)), s12 = exp(r.iC12 * log(f2 / r.B12));
+  double s21 = exp(r.iC21 * log(f1 / r.B21)), s22 = exp(r.iC22 * log(f2 / r.B22));
   double n1 = s11 + s12, n2 = s21 + s22;
   double Sf11 = s11 / n1, Sf12 = s12 / n1, Sf21 = s21 / n2, Sf22 = s22 / n2;
   double a1 = r.A11 * Sf11 + r.A12 * Sf12;
@@ -61,8 +67,8 @@ __global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rho
   // update.jl:170-171 multiply by pow(ex/ex, Xf11) and pow(em/em, Xf22): with
   // positive finite ex, em those are pow(1, y) = 1 exactly, and x * 1 = x, so
   // the two FP64 pow calls are left out without changing a bit
-  double thtv1 = pow(r.em / r.ex, Xf12);
-  double thtv2 = pow(r.ex / r.em, Xf21);
+  double thtv1 = exp(Xf12 * r.lmx);
+  double thtv2 = exp(Xf21 * r.lxm);
   double etaf1 = r.ex * thtv1, etaf2 = r.em * thtv2;
   AT(etamix, j, i) = f1 * etaf1 + f2 * etaf2;
 }
@@ -105,16 +111,28 @@ __global__ void interp_kernel(int Nz, int Nx, int xBC, int zBC, double rhom0, do
 }
 
 // mean(rhow, dims=2) (sequential over columns, as Julia reduces a
-// non-leading dimension) and the lithostatic z-scan of update_pressure!
-// (update.jl:119-131).  One CTA; rhoref and Pl_col go to scratch.
-__global__ void rowmean_scan_kernel(int Nz, int Nx, CView rhow, double g0, double h, double Ptop,
-                                    double* rhoref, double* plcol) {
-  for (int j = threadIdx.x; j <= Nz; j += blockDim.x) {
-    double acc = 0.0;
-    for (int i = 0; i < Nx; ++i) acc = acc + AT(rhow, j, i);
-    rhoref[j] = acc / (double)Nx;
+// non-leading dimension) and, below, the lithostatic z-scan of
+// update_pressure! (update.jl:119-131); rhoref and Pl_col go to scratch.
+// One thread per row j sums the row in column order; the columns are loaded
+// 16 at a time ahead of the additions, so the order (and the bits) of the sum
+// stay sequential while many loads are in flight.
+__global__ void rowmean_kernel(int Nz, int Nx, CView rhow, double* rhoref) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > Nz) return;
+  double acc = 0.0;
+  int i = 0;
+  for (; i + 16 <= Nx; i += 16) {
+    double v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = AT(rhow, j, i + q);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc = acc + v[q];
   }
-  __syncthreads();
+  for (; i < Nx; ++i) acc = acc + AT(rhow, j, i);
+  rhoref[j] = acc / (double)Nx;
+}
+__global__ void pressure_scan_kernel(int Nz, double g0, double h, double Ptop, const double* rhoref,
+                                     double* plcol) {
   if (threadIdx.x == 0) {
     double p = ((rhoref[0] * g0) * h) / 2.0 + Ptop;
     plcol[0] = p;
@@ -351,7 +369,8 @@ int update_impl(xc_ctx* c) {
   cudaStream_t s = c->stream;
   dim3 blk(32, 8);
   Rheo r{p.AA[0], p.AA[1], p.AA[2], p.AA[3], p.BB[0], p.BB[1], p.BB[2], p.BB[3],
-         1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0};
+         1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0,
+         std::log(p.etam0 / p.etax0), std::log(p.etax0 / p.etam0)};
   volfrac_rheology_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
       Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
       F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix)); xc_count_launch();
@@ -364,7 +383,8 @@ int update_impl(xc_ctx* c) {
   XC_LAUNCH_CHECK();
   double* rhoref = c->tmp[6];
   double* plcol = c->tmp[6] + (Nz + 8);
-  rowmean_scan_kernel<<<1, 1024, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
+  rowmean_kernel<<<(Nz + 1 + 31) / 32, 32, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), rhoref); xc_count_launch();
+  pressure_scan_kernel<<<1, 32, 0, s>>>(Nz, p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
   XC_LAUNCH_CHECK();
   drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, s>>>(
       Nz, Nx, p.Ptop, rhoref, plcol, CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
