@@ -499,7 +499,8 @@ __global__ void refine_update_kernel(long long n, const T* __restrict__ dy, cons
 // ghost / boundary rows are relaxed exactly (w = 1)
 template <typename T, int MODE>
 __device__ __forceinline__ void vel_update_w(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi,
-                                             const T* b, T* out, T omega, long long t, int j, int i) {
+                                             const T* b, T* out, T omega, long long t, int j, int i,
+                                             const T* dscl = nullptr) {
   const bool exact = i == 0 || i == g.Nx + 1 || j == 0 || j == g.Nz;
   if (MODE == 0) {
     out[t] = sdiv<T>((exact ? (T)1 : omega) * b[t], vel_diag_w<T>(g, op, t, j, i));
@@ -508,11 +509,13 @@ __device__ __forceinline__ void vel_update_w(const Geo& g, const OpConst& k, con
   T d;
   const T ax = vel_row_w<T, false>(g, k, op, xi, xi + g.NW, nullptr, t, j, i, &d);
   if (MODE == 2) out[t] = b[t] - ax;
+  else if (MODE == 3) out[t] = (xi[t] + sdiv<T>((exact ? (T)1 : omega) * (b[t] - ax), d)) / dscl[t];
   else out[t] = xi[t] + sdiv<T>((exact ? (T)1 : omega) * (b[t] - ax), d);
 }
 template <typename T, int MODE>
 __device__ __forceinline__ void vel_update_u(const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi,
-                                             const T* b, T* out, T omega, long long u, int j, int i) {
+                                             const T* b, T* out, T omega, long long u, int j, int i,
+                                             const T* dscl = nullptr) {
   const bool exact = j == 0 || j == g.Nz + 1 || (k.mms && (int)u == k.pin_u);
   const long long t = g.NW + u;
   if (MODE == 0) {
@@ -522,20 +525,24 @@ __device__ __forceinline__ void vel_update_u(const Geo& g, const OpConst& k, con
   T d;
   const T ax = vel_row_u<T, false>(g, k, op, xi, xi + g.NW, nullptr, u, j, i, &d);
   if (MODE == 2) out[t] = b[t] - ax;
+  else if (MODE == 3) out[t] = (xi[t] + sdiv<T>((exact ? (T)1 : omega) * (b[t] - ax), d)) / dscl[t];
   else out[t] = xi[t] + sdiv<T>((exact ? (T)1 : omega) * (b[t] - ax), d);
 }
 // a level's rows on a 2-D grid: thread (j, i) takes W row (j, i) and U row
-// (j, i) -- no index division, and the two rows share viscosity loads
+// (j, i) -- no index division, and the two rows share viscosity loads.
+// MODE 3 is a sweep whose result is written divided by dscl (the last sweep
+// of the fine level, returning the preconditioned vector in scaled form).
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) vel_sweep2d_kernel(Geo g, OpConst k, VOp<T> op, const T* __restrict__ xi,
-                                                          const T* __restrict__ b, T* out, T omega) {
+                                                          const T* __restrict__ b, T* out, T omega,
+                                                          const T* __restrict__ dscl) {
   XC_PDL_WAIT();
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int i = blockIdx.y * 8 + threadIdx.y;
   if (j <= g.Nz && i <= g.Nx + 1)
-    vel_update_w<T, MODE>(g, k, op, xi, b, out, omega, (long long)i * (g.Nz + 1) + j, j, i);
+    vel_update_w<T, MODE>(g, k, op, xi, b, out, omega, (long long)i * (g.Nz + 1) + j, j, i, dscl);
   if (j <= g.Nz + 1 && i <= g.Nx)
-    vel_update_u<T, MODE>(g, k, op, xi, b, out, omega, (long long)i * (g.Nz + 2) + j, j, i);
+    vel_update_u<T, MODE>(g, k, op, xi, b, out, omega, (long long)i * (g.Nz + 2) + j, j, i, dscl);
 }
 
 
@@ -1146,22 +1153,25 @@ __global__ void p_scatter_rows_kernel(Geo g, const T* __restrict__ rp, T* zp) {
   zp[o + Nz + 1] = rp[o + Nz + 1] + zp[o + Nz];
 }
 
-// r_v' = r_v - GG z_p on interior velocity rows (fluidmech.jl:343-356)
+// velocity right-hand side of the preconditioner: rv = S^-1 v - GG z_p on the
+// interior velocity rows (fluidmech.jl:343-356), S^-1 v elsewhere -- the
+// unscaling of the residual fused with the gradient of the pressure part
 template <typename T>
-__global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, T* rv) {
+__global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, const T* __restrict__ v,
+                                const T* __restrict__ scl, T* rv) {
   XC_PDL_WAIT();
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
+  if (t >= g.NW + g.NU) return;
+  T r = v[t] / scl[t];
   if (t < g.NW) {
-    int j = (int)(t % lw), i = (int)(t / lw);
-    if (j >= 1 && j <= Nz - 1 && i >= 1 && i <= Nx)
-      rv[t] -= (T)g.invh * (zp[(size_t)i * lu + j + 1] - zp[(size_t)i * lu + j]);
-    return;
+    const int j = t % lw, i = t / lw;
+    if (j >= 1 && j <= Nz - 1 && i >= 1 && i <= Nx) r -= (T)g.invh * (zp[i * lu + j + 1] - zp[i * lu + j]);
+  } else {
+    const int u = t - g.NW, j = u % lu, i = u / lu;
+    if (j >= 1 && j <= Nz) r -= (T)g.invh * (zp[(i + 1) * lu + j] - zp[i * lu + j]);
   }
-  long long u = t - g.NW;
-  if (u >= g.NU) return;
-  int j = (int)(u % lu), i = (int)(u / lu);
-  if (j >= 1 && j <= Nz) rv[t] -= (T)g.invh * (zp[(size_t)(i + 1) * lu + j] - zp[(size_t)i * lu + j]);
+  rv[t] = r;
 }
 
 // ---------------------------------------------------------------------------
@@ -1632,7 +1642,8 @@ static int coarse_threads(long long n) { return n > 512 ? 1024 : (n > 128 ? 256 
 
 // ---- velocity V-cycle on level l: solve A x = vb[l] approximately (x := vx[l])
 template <typename T>
-int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaStream_t s) {
+int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaStream_t s, T* final_out = nullptr,
+               const T* final_scl = nullptr, bool* final_done = nullptr) {
   const Geo& g = H.vg[l];
   const long long n = (long long)g.NW + g.NU;
   const T om = (T)cfg.omega_v;
@@ -1656,17 +1667,18 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
-  // pre-smoothing (first sweep from zero)
+  // pre-smoothing (first sweep from zero, into the buffer that makes the last
+  // sweep land in vx)
   const VOp<T> op = vop(H, l);
-  pdl(PDL_ON, vel_sweep2d_kernel<T, 0>, grid2(g), blk2(), s, g, k, op, H.vx[l], H.vb[l], H.vx[l], om);
-  T* a = H.vx[l];
-  T* o = H.vx2[l];
+  const T* no = nullptr;
+  T* a = (cfg.nu - 1) % 2 ? H.vx2[l] : H.vx[l];
+  T* o = (cfg.nu - 1) % 2 ? H.vx[l] : H.vx2[l];
+  pdl(PDL_ON, vel_sweep2d_kernel<T, 0>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], a, om, no);
   for (int q = 1; q < cfg.nu; ++q) {
-    pdl(PDL_ON, vel_sweep2d_kernel<T, 1>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], o, om);
+    pdl(PDL_ON, vel_sweep2d_kernel<T, 1>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], o, om, no);
     T* tmp = a; a = o; o = tmp;
   }
-  if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-  pdl(PDL_ON, vel_sweep2d_kernel<T, 2>, grid2(g), blk2(), s, g, k, op, H.vx[l], H.vb[l], H.vr[l], om);
+  pdl(PDL_ON, vel_sweep2d_kernel<T, 2>, grid2(g), blk2(), s, g, k, op, H.vx[l], H.vb[l], H.vr[l], om, no);
   const Geo& c = H.vg[l + 1];
   pdl(PDL_ON, vel_restrict2d_kernel<T>, grid2(c), blk2(), s, g, c, H.vr[l], H.vb[l + 1]);
   XC_LAUNCH_CHECK();
@@ -1675,7 +1687,13 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   a = H.vx[l];
   o = H.vx2[l];
   for (int q = 0; q < cfg.nu; ++q) {
-    pdl(PDL_ON, vel_sweep2d_kernel<T, 1>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], o, om);
+    if (final_out && q == cfg.nu - 1) {   // last sweep of the fine level straight into the scaled output
+      pdl(PDL_ON, vel_sweep2d_kernel<T, 3>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], final_out, om, final_scl);
+      *final_done = true;
+      XC_LAUNCH_CHECK();
+      return XC_OK;
+    }
+    pdl(PDL_ON, vel_sweep2d_kernel<T, 1>, grid2(g), blk2(), s, g, k, op, a, H.vb[l], o, om, no);
     T* tmp = a; a = o; o = tmp;
   }
   if (a != H.vx[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.vx[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
@@ -1743,8 +1761,8 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   const long long nvv = (long long)g.NW + g.NU;
-  // physical residual r = S^-1 v -> velocity part into vb[0], pressure into rp
-  pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, v, H.scl, H.vb[0]);
+  // physical residual r = S^-1 v: pressure part into rp here, velocity part
+  // into vb[0] by sub_grad_kernel below
   pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, v + nvv, H.scl + nvv, H.rp);
   // pressure: interior solve with ghost elimination
   pdl(PDL_ON, p_gather_kernel<T>, nblk(g.Nz * g.Nx), 256, s, g, H.kx[0], H.kr, H.rp, H.pb[0]);
@@ -1755,10 +1773,11 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   pdl(PDL_ON, p_scatter_cols_kernel<T>, nblk(g.Nz + 1), 256, s, g, H.rp, zp);
   pdl(PDL_ON, p_scatter_rows_kernel<T>, nblk(g.Nx + 2), 256, s, g, H.rp, zp);
   // velocity: rhs r_v - GG z_p, one V-cycle
-  pdl(PDL_ON, sub_grad_kernel<T>, nblk(nvv), 256, s, g, zp, H.vb[0]);
+  pdl(PDL_ON, sub_grad_kernel<T>, nblk(nvv), 256, s, g, zp, v, H.scl, H.vb[0]);
   XC_LAUNCH_CHECK();
-  XC_TRY(vcycle_vel<T>(H, k, cfg, 0, s));
-  pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, H.vx[0], H.scl, out);
+  bool done = false;
+  XC_TRY(vcycle_vel<T>(H, k, cfg, 0, s, out, H.scl, &done));
+  if (!done) pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, H.vx[0], H.scl, out);
   pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, zp, H.scl + nvv, zp);
   XC_LAUNCH_CHECK();
   (void)n;
@@ -2329,7 +2348,8 @@ int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H
       if (it == 0) cudaEventRecord(e0, s);
       const int q = ((it % nc) + nc) % nc;
       vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op_of(q), (const T*)cp[q][xo],
-                                                           (const T*)cp[q][xo + 1], (T*)cp[q][xo + 2], (T)0.7);
+                                                           (const T*)cp[q][xo + 1], (T*)cp[q][xo + 2], (T)0.7,
+                                                           (const T*)nullptr);
       xc_count_launch();
     }
     cudaEventRecord(e1, s);
