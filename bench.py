@@ -205,7 +205,7 @@ def main():
             pair.append(t.numpy().T)   # F-contiguous [z, x] view of the pinned buffer
         draws.append(pair)
     st.initialize(x0, draws[0][0], draws[0][1])
-    sopt = dict(solver=a.solver, rtol=a.rtol, maxit=400, inner_rtol=3e-2, inner_maxit=30, pressure_sweeps=1)
+    sopt = dict(solver=a.solver, rtol=a.rtol, maxit=400, inner_rtol=5e-2, inner_maxit=30, pressure_sweeps=1)
     for kv in a.knob:
         key, val = kv.split("=", 1)
         sopt[key] = float(val) if any(ch in val for ch in ".e") else int(val)
