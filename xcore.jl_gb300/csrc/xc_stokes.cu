@@ -1910,9 +1910,9 @@ int arnoldi_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cf
   return XC_OK;
 }
 
-// FGMRES(m) on S LL S y = rhs (rhs already in H.w on entry is NOT assumed):
-// solves from the initial guess in H.y; rhs = rhs_dev (scaled).
-// Returns iterations used; sets *relres = ||rhs - A y|| / ||rhs||.
+// Right-preconditioned FGMRES(m) on the scaled system S LL S y = rhs, from the
+// initial guess in H.y (updated in place).  *its_out = iterations used,
+// *relres_out = ||rhs - A y|| / ||rhs|| of the true residual at the last restart.
 template <typename T>
 int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* rhs, double rtol,
            int maxit, int* its_out, double* relres_out, cudaStream_t s) {
@@ -2249,14 +2249,14 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       if (!std::isfinite(relres)) { xc_set_error("mixed solver: non-finite residual"); status = XC_NAN; break; }
       if (relres <= o.rtol || its >= o.maxit) break;
       ++refinements;
-      // inner FP32 solve of S LL S dy = res
+      // inner FP32 solve of S LL S dy = res from dy = 0.  Its right-hand side
+      // lives in f.w, which the FP32 Krylov and multigrid code never writes
+      // (f.t is the operator's scratch, f.V / f.Z the basis).
       convert_kernel<double, float><<<nblk(n), 256, 0, s>>>(n, res, w->f.w); xc_count_launch();
       XC_CUDA_TRY(cudaMemsetAsync(w->f.y, 0, sizeof(float) * n, s));
-      // the inner rhs must not alias the Krylov buffers: keep it in f.rv..? use a dedicated copy in f.t? use f.w
-      float* frhs = w->f.w;
+      const float* frhs = w->f.w;
       int iits = 0;
       double irr = 1.0;
-      // fgmres uses H.w only through its rhs pointer; H.t is scratch for apply
       XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s));
       its += iits;
       refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
