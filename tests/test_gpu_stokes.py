@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import xcore_oracle as O
-from gpu_helpers import assert_fields, device_state, realistic_state, rel_err
+from gpu_helpers import assert_fields, device_state, product_params, realistic_state, rel_err, upload_all
 from mms import mms_sources
 
 pytestmark = pytest.mark.gpu
@@ -36,6 +36,24 @@ def test_fluidmech_matches_lu(shape, solver, rtol, tol):
         e = _maxrel(ds[k], getattr(st, k))
         assert e <= tol, (k, e, info)
     assert_fields(ds, st, ["MFS", "drhodt"], exact=True)
+
+
+@pytest.mark.parametrize("bc", [dict(sds=-1, top_cnv=-1, bot_cnv=-1), dict(sds=-1, top_cnv=-1, bot_cnv=1),
+                                dict(sds=1, top_cnv=1, bot_cnv=1)])
+def test_fluidmech_boundary_variants_match_lu(bc):
+    """The velocity boundary rows of fluidmech.jl:145-162 (sds) and 245-262
+    (top_cnv, bot_cnv): free slip at one or both walls and the mirrored W side
+    columns, FP64 FGMRES against the sparse LU of the same assembled system."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=32, Nx=32, steps=2)
+    ds = xc.State(product_params(par), grid=xc.Grid(Nx=g.Nx, Nz=g.Nz, h=g.h, D=g.D, L=g.L), scales=sc, **bc)
+    upload_all(ds, st)
+    coefs = O.time_coefs("bd2im", 3)
+    O.fluidmech(st, g, par, coefs, dt, **bc)
+    info = ds.fluidmech(coefs, dt, solver="fgmres64", rtol=1e-10)
+    assert info["converged"] and info["rel_residual"] <= 1e-10, info
+    for k in ("W", "U", "P"):
+        e = _maxrel(ds[k], getattr(st, k))
+        assert e <= 1e-8, (k, e, info)
 
 
 def _mms_device(N):
