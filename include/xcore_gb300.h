@@ -104,6 +104,8 @@ typedef struct xc_solver_opts {
   int inner_gs_passes;     /* mixed: Gram-Schmidt passes of the FP32 inner solve (1; 1 or 2) */
   int serial_launch;       /* 1: plain stream order inside the solver's CUDA graphs instead of
                               programmatic dependent launch (same results) */
+  int coarse_viscosity_mean; /* cell viscosity of a coarse multigrid level from its four fine
+                                cells: 0 arithmetic (default), 1 geometric, 2 harmonic */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

@@ -706,7 +706,7 @@ __global__ void coarsen_fields_kernel(int Nzc, int Nxc, const double* __restrict
                                       const double* __restrict__ etaco, const double* __restrict__ rho,
                                       const double* __restrict__ rhow, const double* __restrict__ rhou,
                                       double* etac, double* etacoc, double* rhoc, double* rhowc,
-                                      double* rhouc) {
+                                      double* rhouc, int mean) {
   XC_PDL_WAIT();
   int J = blockIdx.x * blockDim.x + threadIdx.x;
   int I = blockIdx.y * blockDim.y + threadIdx.y;
@@ -722,7 +722,12 @@ __global__ void coarsen_fields_kernel(int Nzc, int Nxc, const double* __restrict
   }
   if (J < Nzc && I < Nxc) {
     size_t a = (size_t)(2 * I) * Nz + 2 * J, b = (size_t)(2 * I + 1) * Nz + 2 * J;
-    etac[(size_t)I * Nzc + J] = 0.25 * (eta[a] + eta[a + 1] + eta[b] + eta[b + 1]);
+    if (mean == 1)        // geometric
+      etac[(size_t)I * Nzc + J] = exp(0.25 * (log(eta[a]) + log(eta[a + 1]) + log(eta[b]) + log(eta[b + 1])));
+    else if (mean == 2)   // harmonic
+      etac[(size_t)I * Nzc + J] = 4.0 / (1.0 / eta[a] + 1.0 / eta[a + 1] + 1.0 / eta[b] + 1.0 / eta[b + 1]);
+    else
+      etac[(size_t)I * Nzc + J] = 0.25 * (eta[a] + eta[a + 1] + eta[b] + eta[b + 1]);
     rhoc[(size_t)I * Nzc + J] = 0.25 * (rho[a] + rho[a + 1] + rho[b] + rho[b + 1]);
   }
 }
@@ -2189,7 +2194,8 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     const double* rhow = l > 1 ? w->rhow[l - 1] : (const double*)c->field[FLD_rhow];
     const double* rhou = l > 1 ? w->rhou[l - 1] : (const double*)c->field[FLD_rhou];
     coarsen_fields_kernel<<<grid2d(lg.Nz + 1, lg.Nx + 1, blk), blk, 0, s>>>(
-        lg.Nz, lg.Nx, eta, etaco, rho, rhow, rhou, w->eta[l], w->etaco[l], w->rho[l], w->rhow[l], w->rhou[l]); xc_count_launch();
+        lg.Nz, lg.Nx, eta, etaco, rho, rhow, rhou, w->eta[l], w->etaco[l], w->rho[l], w->rhow[l], w->rhou[l],
+        o.coarse_viscosity_mean); xc_count_launch();
     XC_LAUNCH_CHECK();
   }
   SolveCfg cfg;

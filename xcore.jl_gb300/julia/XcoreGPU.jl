@@ -40,10 +40,10 @@ struct SolverOpts
     kind::Cint; rtol::Cdouble; maxit::Cint; restart::Cint; inner_rtol::Cdouble; inner_maxit::Cint
     smooth_sweeps::Cint; omega_velocity::Cdouble; schur_mass::Cdouble; schur_full_diagonal::Cint
     coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint; pressure_sweeps::Cint; inner_gs_passes::Cint
-    serial_launch::Cint
+    serial_launch::Cint; coarse_viscosity_mean::Cint
 end
 SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
-    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0)
+    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0)
 
 struct SolverStats
     iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
@@ -171,6 +171,25 @@ function compute_resnorm(ctx::Context, dt)
 end
 
 # one outer step of run! with `sweeps` Picard sweeps; returns the next dt
+# ---- values record_history! pushes (src/history.jl:121-145, 183-222) ---------------
+# {sumB, sumM, sumX, sumGx, top_aX, bot_aX, top_aM, bot_aM, top_dX, bot_dX, top_dM, bot_dM}
+function conservation_sums(ctx::Context)
+    out = Vector{Cdouble}(undef, 12)
+    check(ccall((:xc_conservation_sums, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), ctx.h, out))
+    return out
+end
+
+const HISTORY_KEYS = vcat(["x_min", "x_mean", "x_max", "x_std"],
+                          ["$(f)_$(s)" for f in ("V", "vx", "vm", "xie", "xix", "xis") for s in ("min", "rms", "max")],
+                          ["$(f)_$(s)" for f in ("Ra", "Rc", "ReD", "Red", "ks", "ke", "kx", "eta", "etamix", "etae",
+                                                 "etas", "etat") for s in ("min", "gm", "max")])
+
+function history_stats(ctx::Context)
+    out = Vector{Cdouble}(undef, 58)
+    check(ccall((:xc_history_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), ctx.h, out))
+    return Dict(zip(HISTORY_KEYS, out))
+end
+
 function step!(ctx::Context, step::Integer, dt, re, rs; sweeps = 3, solver::Symbol = :mixed, rtol = 1e-9)
     o = SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 1e-3, 40)
     st = Ref{NTuple{19,UInt64}}()   # xc_step_stats storage (152 bytes; dt_next is the last word)
