@@ -106,6 +106,8 @@ typedef struct xc_solver_opts {
                               programmatic dependent launch (same results) */
   int coarse_viscosity_mean; /* cell viscosity of a coarse multigrid level from its four fine
                                 cells: 0 arithmetic (default), 1 geometric, 2 harmonic */
+  int tiled_sweep;         /* 1: FP32 velocity sweeps from shared-memory tiles instead of per-row
+                              reads (same results; measured 5% slower at 1024^2) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {
