@@ -167,7 +167,7 @@ def compute_scales(p: Params, g: Grid, tol: float = 1e-9, maxiter: int = 200) ->
     return dict(h0=h0, D0=D0, d0=d0, L0=L0, L0h=L0h, l0=l0, l0h=l0h, bnd_w=bnd_w,
                 rho0=rho0, Drho0=Drho0, chi0=chi0, Dchi0=Dchi0, eta0=eta0, W0=W0, w0=w0,
                 ReL0=ReL0, Rel0=Rel0, fReL0=fReL0, fRel0=fRel0, ke0=ke0, ks0=ks0, kx0=kx0,
-                txi0=txi0, t0=t0, dt0=dt0, G0=G0)
+                txi0=txi0, t0=t0, dt0=dt0, G0=G0, Ri0=Ri0, W0l=W0l)
 
 
 def time_coefs(TINT: str, step: int):

@@ -307,3 +307,52 @@ def test_flux_form_equals_literal_cell_kernel(scheme):
     w = rng.standard_normal((Nz + 1, Nx))
     qx, qz = O.advect_fluxes(fh, u, w, scheme, g)
     assert np.array_equal(O.divergence(qx, qz, 1.0 / h), _literal_cell_kernel(fh, u, w, h, scheme, g))
+
+
+def test_grid_sizes_and_ghost_maps():
+    """test/test_grid.jl:1-29: sizes, spacing and the ghost index vectors
+    (0-based here: Julia's icx = [Nx; 1:Nx; 1] is [Nx-1, 0..Nx-1, 0])."""
+    g = O.make_grid(O.Params(D=10.0, N=100, L=10.0))
+    assert (g.Nz, g.Nx, g.h) == (100, 100, 0.1)
+    icx, icz = O.icx_of(g.Nx, "periodic"), O.icz_of(g.Nz, "closed")
+    assert icx[0] == g.Nx - 1 and icx[-1] == 0 and len(icx) == g.Nx + 2
+    assert icz[0] == 0 and icz[-1] == g.Nz - 1
+    assert O.make_grid(O.Params(D=10.0, N=50, L=15.0)).Nx == 75
+
+
+def test_scales_fixed_point_and_ordering():
+    """test/test_scales.jl:1-30: the convection speed is the fixed point of its
+    defining relation to 1e-12, and the derived scales have the stated signs
+    and ranges; the package's host restatement gives the same numbers."""
+    import xcore_gb300 as xc
+    par = O.Params(D=10.0, N=200, L=15.0, d0=1e-2, etam0=1e1, rhom0=2700, rhox0=3200, g0=10.0, L0=10.0 / 100,
+                   l0=1e-2 * 10, Da=0.01, Xi=0.5, x0=float(np.finfo(np.float64).eps))
+    g = O.make_grid(par)
+    s = O.compute_scales(par, g)
+    Ri2 = s["Ri0"] ** 2
+    W0 = (math.sqrt(4 / Ri2 * s["Dchi0"] * s["Drho0"] * par.g0 * s["rho0"] * s["fReL0"] * s["L0"] ** 2 * s["D0"]
+                    + s["eta0"] ** 2) - s["eta0"]) * s["D0"] / (2 * s["fReL0"] * s["L0"] ** 2 * s["rho0"] / Ri2)
+    assert W0 == pytest.approx(s["W0"], rel=1e-12)
+    assert s["W0l"] > 0 and s["W0"] > 0 and s["w0"] > 0
+    assert 0 < s["fReL0"] <= 1 and 0 < s["fRel0"] <= 1
+    pp = xc.Parameters(**{k: getattr(par, k) for k in xc.Parameters.__dataclass_fields__ if hasattr(par, k)})
+    ps = xc.compute_scales(pp, xc.Grid(Nx=g.Nx, Nz=g.Nz, h=g.h, D=g.D, L=g.L))
+    common = [k for k in ps if k in s]
+    assert len(common) >= 10
+    for k in common:
+        assert ps[k] == pytest.approx(s[k], rel=1e-14), k
+
+
+def test_resnorm_positive_after_change():
+    """test/test_diagnose.jl:65-78: after a field changes, compute_resnorm is
+    positive."""
+    par = O.Params(D=10.0, N=16, L=10.0, x0=0.05, Da=0.0)
+    g = O.make_grid(par)
+    sc = O.compute_scales(par, g)
+    ns = O.NoiseStatic(g, sc)
+    rng = np.random.default_rng(3)
+    x0 = np.clip(rng.uniform(0.02, 0.1, (g.Nz, g.Nx)), 0, 1)
+    st = O.initialize(g, par, sc, ns, x0, rng.standard_normal((g.Nz, g.Nx)), rng.standard_normal((g.Nz, g.Nx)))
+    snap = O.snapshot(st)
+    st.X = st.X * 1.01
+    assert O.resnorm(st, snap, sc["dt0"])[0] > 0
