@@ -173,7 +173,8 @@ int xc_phsevo(xc_ctx* ctx, int scheme, const double coefs[6], double dt, double 
 int xc_fluidmech(xc_ctx* ctx, const double coefs[6], double dt,
                  const xc_solver_opts* opts, xc_solver_stats* stats);
 /* fluidmech! in MMS mode (bnchm_data != nothing): src_* and *_exact arrays are
-   host arrays sized like W (Nz+1,Nx+2), U (Nz+2,Nx+1), P (Nz+2,Nx+2).
+   host arrays sized like W (Nz+1,Nx+2), U (Nz+2,Nx+1), P (Nz+2,Nx+2); a context
+   with open_cnv set returns XC_BAD_ARG here.
                                                          src/fluidmech.jl:115,218,243,320,421-476 */
 int xc_fluidmech_mms(xc_ctx* ctx, const double* src_W, const double* src_U, const double* src_P,
                      const double* W_exact, const double* U_exact, const double* P_exact,

@@ -56,6 +56,24 @@ def test_fluidmech_boundary_variants_match_lu(bc):
         assert e <= 1e-8, (k, e, info)
 
 
+@pytest.mark.parametrize("solver,rtol,tol", [("fgmres64", 1e-10, 1e-8), ("mixed", 1e-9, 1e-7)])
+def test_open_bottom_matches_lu(solver, rtol, tol):
+    """open_cnv = true (fluidmech.jl:169-190, 426-429, 478-487): the bottom W
+    row becomes rho-weighted continuity with the MFS source and the bottom
+    ghost row of P is held at zero instead of one interior pin."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=32, Nx=40, steps=2)
+    ds = xc.State(product_params(par), grid=xc.Grid(Nx=g.Nx, Nz=g.Nz, h=g.h, D=g.D, L=g.L), scales=sc,
+                  open_cnv=True)
+    upload_all(ds, st)
+    coefs = O.time_coefs("bd2im", 3)
+    O.fluidmech(st, g, par, coefs, dt, open_cnv=True)
+    info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol, maxit=2000)
+    assert info["converged"] and info["rel_residual"] <= rtol, info
+    for k in ("W", "U", "P"):
+        e = _maxrel(ds[k], getattr(st, k))
+        assert e <= tol, (k, e, info)
+
+
 def test_tiled_fp32_sweep_gives_the_per_row_results():
     """The shared-memory tiled FP32 velocity sweep performs the per-row
     kernel's operations in the same order: a mixed solve with either kernel

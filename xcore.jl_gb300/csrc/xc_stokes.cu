@@ -83,6 +83,7 @@ struct OpConst {
   int pin_p;           // flat P index (0..NP-1) of the pressure pin
   int mms;             // 1: MMS pins (P row and U row are identity rows)
   int pin_u;           // flat U index of the MMS velocity pin
+  int open_cnv;        // 1: open bottom (fluidmech.jl:169-190, 426-429, 478-487)
 };
 
 // ---------------------------------------------------------------------------
@@ -111,7 +112,14 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
     if (i == 0 || i == Nx + 1 || j == 0) {
       c[0] = 1.0;
     } else if (j == Nz) {
+      // bottom row: closed (W = MFSmean D / h) or open, a continuity row
+      // rho1 W(Nz) - rho2 W(Nz-1) + rho3 U(Nz, i) - rho4 U(Nz, i-1) (fluidmech.jl:169-190)
       c[0] = rhow[(size_t)(i - 1) * (Nz + 1) + Nz] * invh;
+      if (k.open_cnv) {
+        c[1] = -rhow[(size_t)(i - 1) * (Nz + 1) + Nz - 1] * invh;
+        c[7] = +rhou[(size_t)i * Nz + Nz - 1] * invh;
+        c[5] = -rhou[(size_t)(i - 1) * Nz + Nz - 1] * invh;
+      }
     } else {
       double C1 = etaco[(size_t)(i - 1) * (Nz + 1) + j], C2 = etaco[(size_t)i * (Nz + 1) + j];
       double P1 = eta[(size_t)(i - 1) * Nz + (j - 1)], P2 = eta[(size_t)(i - 1) * Nz + j];
@@ -187,6 +195,8 @@ struct VOp {
   const T* etaco;   //   corner viscosity (Nz+1, Nx+1)
   const T* dw;      //   W rows: inertia + drunken-sailor term; bottom row: its diagonal
   const T* du;      //   U rows: inertia + drunken-sailor term
+  const T* dbot;    //   open bottom: the W(Nz-1), U(Nz, i-1), U(Nz, i) weights of the bottom W row,
+                    //   three per column
 };
 template <typename T>
 constexpr bool kFly = std::is_same<T, float>::value;
@@ -205,7 +215,7 @@ template <typename T>
 __global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta,
                                 const double* __restrict__ etaco, const double* __restrict__ rho,
                                 const double* __restrict__ rhow, const double* __restrict__ rhou,
-                                T* feta, T* fetaco, T* dw, T* du) {
+                                T* feta, T* fetaco, T* dw, T* du, T* dbot) {
   XC_PDL_WAIT();
   const int Nz = g.Nz, Nx = g.Nx;
   const double invh = g.invh;
@@ -222,6 +232,11 @@ __global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
       if (k.sailor) v += (rho[(size_t)(i - 1) * Nz + j] - rho[(size_t)(i - 1) * Nz + j - 1]) * invh * k.g0 * k.dt;
     }
     dw[t] = (T)v;
+    if (k.open_cnv && j == Nz && i >= 1 && i <= Nx) {
+      dbot[3 * i + 0] = (T)(-rhow[(size_t)(i - 1) * (Nz + 1) + Nz - 1] * invh);
+      dbot[3 * i + 1] = (T)(-rhou[(size_t)(i - 1) * Nz + Nz - 1] * invh);
+      dbot[3 * i + 2] = (T)(+rhou[(size_t)i * Nz + Nz - 1] * invh);
+    }
   }
   if (t < g.NU) {
     int j = (int)(t % (Nz + 2)), i = (int)(t / (Nz + 2));
@@ -301,6 +316,19 @@ __device__ __forceinline__ T vel_row_w(const Geo& g, const OpConst& k, const VOp
     if constexpr (kFly<T>) d = j == 0 ? (T)1 : op.dw[t];
     else d = op.cw[t];
     *dg = d;
+    if (j == Nz && k.open_cnv) {   // open bottom: the continuity-like row, no pressure gradient
+      T c1, c5, c7;
+      if constexpr (kFly<T>) {
+        c1 = op.dbot[3 * i]; c5 = op.dbot[3 * i + 1]; c7 = op.dbot[3 * i + 2];
+      } else {
+        c1 = op.cw[g.NW + t]; c5 = op.cw[5 * (size_t)g.NW + t]; c7 = op.cw[7 * (size_t)g.NW + t];
+      }
+      T s = d * xw[t];
+      s += c1 * xw[t - 1];
+      s += c5 * xu[(i - 1) * lu + j];
+      s += c7 * xu[i * lu + j];
+      return s;
+    }
     return d * xw[t];
   }
   const RowW<T> c = w_row<T>(g, op, t, j, i);
@@ -400,13 +428,17 @@ __device__ __forceinline__ T p_row(const Geo& g, const OpConst& k, const T* __re
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2, lw = Nz + 1;
   if (j == 0) return xp[t] - xp[t + 1];
   if (j == Nz + 1) return xp[t] - xp[t - 1];
-  if (i == 0) return xp[t] - xp[(size_t)Nx * lp + j];
-  if (i == Nx + 1) return xp[t] - xp[(size_t)1 * lp + j];
+  // open bottom: the whole last interior row of P is pinned like the single
+  // interior cell otherwise (its KP row becomes the identity, DM stays), and
+  // its two ghost-column cells become P = 0 rows (fluidmech.jl:426-429, 478-487)
+  const bool open_row = k.open_cnv && j == Nz;
+  if (i == 0) return open_row ? xp[t] : xp[t] - xp[(size_t)Nx * lp + j];
+  if (i == Nx + 1) return open_row ? xp[t] : xp[t] - xp[(size_t)1 * lp + j];
   if (k.mms && t == k.pin_p) return xp[t];
   const size_t NP = g.NP;
   T s = cp[t] * xu[(size_t)(i - 1) * lp + j] + cp[NP + t] * xu[(size_t)i * lp + j] +
         cp[2 * NP + t] * xw[(size_t)i * lw + j - 1] + cp[3 * NP + t] * xw[(size_t)i * lw + j];
-  if (t == k.pin_p) s += xp[t];
+  if (t == k.pin_p || open_row) s += xp[t];
   return s;
 }
 
@@ -577,7 +609,7 @@ __global__ void __launch_bounds__(kTJ * kTI) vel_sweep_tiled_kernel(Geo g, OpCon
   const int j0 = blockIdx.x * kTJ, i0 = blockIdx.y * kTI;
   const int j = j0 + tx, i = i0 + ty;
   const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
-  if (i0 < 1 || i0 + kTI > Nx) {
+  if (i0 < 1 || i0 + kTI > Nx || (k.open_cnv && j0 <= Nz && Nz < j0 + kTJ)) {
     if (j <= Nz && i <= Nx + 1) vel_update_w<float, MODE>(g, k, op, xi, b, out, omega, (long long)i * lw + j, j, i, dscl);
     if (j <= Nz + 1 && i <= Nx) vel_update_u<float, MODE>(g, k, op, xi, b, out, omega, (long long)i * lu + j, j, i, dscl);
     return;
@@ -1237,13 +1269,15 @@ __global__ void p_scatter_kernel(Geo g, const T* __restrict__ z, const T* __rest
 }
 // ghost columns then ghost rows: P_g = r_g + P_neighbour (fluidmech.jl:403-417)
 template <typename T>
-__global__ void p_scatter_cols_kernel(Geo g, const T* __restrict__ rp, T* zp) {
+__global__ void p_scatter_cols_kernel(Geo g, const T* __restrict__ rp, T* zp, int open_bottom) {
   XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
   if (j < 1 || j > Nz) return;
-  zp[j] = rp[j] + zp[(size_t)Nx * lp + j];
-  zp[(size_t)(Nx + 1) * lp + j] = rp[(size_t)(Nx + 1) * lp + j] + zp[(size_t)lp + j];
+  const bool id = open_bottom && j == Nz;   // P = 0 rows of the open bottom
+  zp[j] = id ? rp[j] : rp[j] + zp[(size_t)Nx * lp + j];
+  zp[(size_t)(Nx + 1) * lp + j] = id ? rp[(size_t)(Nx + 1) * lp + j]
+                                     : rp[(size_t)(Nx + 1) * lp + j] + zp[(size_t)lp + j];
 }
 template <typename T>
 __global__ void p_scatter_rows_kernel(Geo g, const T* __restrict__ rp, T* zp) {
@@ -1517,7 +1551,7 @@ __global__ void scl_kernel(Geo g, OpConst k, const double* __restrict__ cw, cons
     int j = p % (g.Nz + 2), i = p / (g.Nz + 2);
     bool interior = j >= 1 && j <= g.Nz && i >= 1 && i <= g.Nx;
     d = interior ? 0.0 : 1.0;
-    if (p == k.pin_p) d = 1.0;
+    if (p == k.pin_p || (k.open_cnv && j == g.Nz)) d = 1.0;
     double sp = interior ? AT(rho, j - 1, i - 1) / AT(eta, j - 1, i - 1) : 1.0;
     extra = sqrt(1.0 / sp);
     if (interior) etarho[(size_t)(i - 1) * g.Nz + j - 1] = 1.0 / sp;
@@ -1565,6 +1599,7 @@ struct Hier {
   T* fetaco[kMaxLevels];
   T* fdw[kMaxLevels];
   T* fdu[kMaxLevels];
+  T* fdbot[kMaxLevels];        //   open-bottom row weights, 3 per column
   T* vx[kMaxLevels];
   T* vx2[kMaxLevels];
   T* vb[kMaxLevels];
@@ -1639,6 +1674,7 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
       XC_CUDA_TRY(cudaMalloc(&H.fetaco[H.nv], sizeof(T) * (lg.Nz + 1) * (lg.Nx + 1)));
       XC_CUDA_TRY(cudaMalloc(&H.fdw[H.nv], sizeof(T) * lg.NW));
       XC_CUDA_TRY(cudaMalloc(&H.fdu[H.nv], sizeof(T) * lg.NU));
+      XC_CUDA_TRY(cudaMalloc(&H.fdbot[H.nv], sizeof(T) * 3 * (lg.Nx + 2)));
     } else {
       XC_CUDA_TRY(cudaMalloc(&H.cw[H.nv], sizeof(T) * 10 * lg.NW));
       XC_CUDA_TRY(cudaMalloc(&H.cu[H.nv], sizeof(T) * 10 * lg.NU));
@@ -1689,7 +1725,7 @@ void free_hier(Hier<T>& H) {
     if (H.gexec[q]) { cudaGraphExecDestroy(H.gexec[q]); H.gexec[q] = nullptr; }
   for (int l = 0; l < H.nv; ++l) {
     cudaFree(H.cw[l]); cudaFree(H.cu[l]); cudaFree(H.vx[l]); cudaFree(H.vx2[l]); cudaFree(H.vb[l]); cudaFree(H.vr[l]);
-    cudaFree(H.feta[l]); cudaFree(H.fetaco[l]); cudaFree(H.fdw[l]); cudaFree(H.fdu[l]);
+    cudaFree(H.feta[l]); cudaFree(H.fetaco[l]); cudaFree(H.fdw[l]); cudaFree(H.fdu[l]); cudaFree(H.fdbot[l]);
   }
   for (int l = 0; l < H.np_lv; ++l) {
     cudaFree(H.kx[l]); cudaFree(H.kz[l]); cudaFree(H.px[l]); cudaFree(H.px2[l]); cudaFree(H.pb[l]); cudaFree(H.pr[l]);
@@ -1703,7 +1739,7 @@ template <typename T>
 VOp<T> vop(const Hier<T>& H, int l) {
   VOp<T> o;
   o.cw = H.cw[l]; o.cu = H.cu[l];
-  o.eta = H.feta[l]; o.etaco = H.fetaco[l]; o.dw = H.fdw[l]; o.du = H.fdu[l];
+  o.eta = H.feta[l]; o.etaco = H.fetaco[l]; o.dw = H.fdw[l]; o.du = H.fdu[l]; o.dbot = H.fdbot[l];
   return o;
 }
 
@@ -1889,7 +1925,7 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   XC_TRY(vcycle_p<T>(H, cfg, 0, s));
   T* zp = out + nvv;   // physical z_p written directly into out, rescaled below
   pdl(PDL_ON, p_scatter_kernel<T>, nblk((long long)g.Nz * g.Nx), 256, s, g, H.px[0], H.rp, H.etarho, (T)cfg.cmass, zp);
-  pdl(PDL_ON, p_scatter_cols_kernel<T>, nblk(g.Nz + 1), 256, s, g, H.rp, zp);
+  pdl(PDL_ON, p_scatter_cols_kernel<T>, nblk(g.Nz + 1), 256, s, g, H.rp, zp, k.open_cnv);
   pdl(PDL_ON, p_scatter_rows_kernel<T>, nblk(g.Nx + 2), 256, s, g, H.rp, zp);
   // velocity: rhs r_v - GG z_p, one V-cycle
   pdl(PDL_ON, sub_grad_kernel<T>, nblk(nvv), 256, s, g, zp, v, H.scl, H.vb[0]);
@@ -1990,7 +2026,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     h = (h ^ b) * 1099511628211ULL;
   };
   mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane);
-  mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
+  mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
 
@@ -2122,7 +2158,7 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
     if (kFly<T>) {
       const long long nt = std::max((long long)lg.NW + lg.NU, (long long)(lg.Nz + 1) * (lg.Nx + 1));
       fly_coef_kernel<T><<<nblk(nt), 256, 0, s>>>(lg, kl, eta, etaco, rho, rhow, rhou, H.feta[l], H.fetaco[l],
-                                                  H.fdw[l], H.fdu[l]); xc_count_launch();
+                                                  H.fdw[l], H.fdu[l], H.fdbot[l]); xc_count_launch();
     } else {
       vel_coef_kernel<T><<<nblk((long long)lg.NW + lg.NU), 256, 0, s>>>(lg, kl, eta, etaco, rho, rhow, rhou,
                                                                         H.cw[l], H.cu[l]); xc_count_launch();
@@ -2227,7 +2263,6 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
                    xc_solver_stats* stats, const MmsData* mms) {
   StokesWork* w = c->stokes;
   if (!w || !w->ok) { xc_set_error("fluidmech: grid too small for the Stokes solver (need Nz, Nx >= 4)"); return XC_BAD_ARG; }
-  if (c->p.open_cnv) { xc_set_error("fluidmech: open_cnv = true is not supported"); return XC_BAD_ARG; }
   xc_solver_opts o;
   if (opts) o = *opts;
   else {
@@ -2268,6 +2303,11 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   k.sds = p.sds; k.top_cnv = p.top_cnv; k.bot_cnv = p.bot_cnv;
   k.sailor = mms ? 0 : 1;
   k.mms = mms ? 1 : 0;
+  k.open_cnv = c->p.open_cnv ? 1 : 0;
+  if (mms && k.open_cnv) {
+    xc_set_error("fluidmech: the MMS branch with open_cnv = true is not supported");
+    return XC_BAD_ARG;
+  }
   int pin_z, pin_x;
   double pin_p_val = 0, pin_u_val = 0;
   k.pin_u = -1;
@@ -2282,7 +2322,10 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     pin_z = (int)std::nearbyint(Nz / 2.0) - 1;
     pin_x = (int)std::nearbyint(Nx / 2.0) - 1;
   }
-  k.pin_p = pin_x * (Nz + 2) + pin_z;
+  // the pressure pin: one interior cell, or (open bottom) the whole last
+  // interior row of P, which p_row and scl_kernel handle (fluidmech.jl:426-429,
+  // 478-487)
+  k.pin_p = k.open_cnv ? -1 : pin_x * (Nz + 2) + pin_z;
   // RHS
   if (mms) {
     if (!w->srcw) {
@@ -2294,7 +2337,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     XC_CUDA_TRY(cudaMemcpyAsync(w->srcu, mms->src_U, sizeof(double) * g.NU, cudaMemcpyHostToDevice, s));
     XC_CUDA_TRY(cudaMemcpyAsync(w->srcp, mms->src_P, sizeof(double) * g.NP, cudaMemcpyHostToDevice, s));
   }
-  RhsArgs ra{coefs[0], coefs[1], coefs[2], dt, p.g0, p.D, p.h, 0.0, mms ? 1 : 0, k.pin_p, k.pin_u};
+  RhsArgs ra{coefs[0], coefs[1], coefs[2], dt, p.g0, p.D, p.h, k.open_cnv ? 1.0 : 0.0, mms ? 1 : 0, k.pin_p, k.pin_u};
   rhs_kernel<<<nblk(n), 256, 0, s>>>(g, ra, CF(c, FLD_Drho), CF(c, FLD_rhoWo), CF(c, FLD_rhoWoo), CF(c, FLD_rhoUo),
                                      CF(c, FLD_rhoUoo), CF(c, FLD_MFS), w->advz, w->advx, c->dscal + SC_MFS_MEAN,
                                      w->srcw, w->srcu, w->srcp, pin_p_val, pin_u_val, w->RR); xc_count_launch();
@@ -2456,6 +2499,7 @@ int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H
     const auto& v = cp[q];
     if (kFly<T>) {
       o.eta = (const T*)v[0]; o.etaco = (const T*)v[1]; o.dw = (const T*)v[2]; o.du = (const T*)v[3];
+      o.dbot = H.fdbot[0];
     } else {
       o.cw = (const T*)v[0]; o.cu = (const T*)v[1];
     }
