@@ -108,6 +108,7 @@ typedef struct xc_solver_opts {
                                 cells: 0 arithmetic (default), 1 geometric, 2 harmonic */
   int tiled_sweep;         /* 1: FP32 velocity sweeps from shared-memory tiles instead of per-row
                               reads (same results; measured 5% slower at 1024^2) */
+  int post_sweeps;         /* velocity post-smoothing sweeps on the large levels (smooth_sweeps) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

@@ -1746,6 +1746,7 @@ VOp<T> vop(const Hier<T>& H, int l) {
 struct SolveCfg {
   double omega_v = 0.7, omega_p = 0.8;
   int nu = 2;
+  int nu_post = 0;         // velocity post-smoothing sweeps (0: nu)
   int coarse_sweeps = 0;   // 0: 4 * (Nz + Nx) of the coarsest level, at least 32
   int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
                            // solved by Jacobi sweeps
@@ -1841,8 +1842,9 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   pdl(PDL_ON, vel_prolong2d_kernel<T>, grid2(g), blk2(), s, g, c, k, H.vx[l + 1], H.vx[l]);
   a = H.vx[l];
   o = H.vx2[l];
-  for (int q = 0; q < cfg.nu; ++q) {
-    if (final_out && q == cfg.nu - 1) {   // last sweep of the fine level straight into the scaled output
+  const int npost = cfg.nu_post > 0 ? cfg.nu_post : cfg.nu;
+  for (int q = 0; q < npost; ++q) {
+    if (final_out && q == npost - 1) {   // last sweep of the fine level straight into the scaled output
       launch_sweep<T, 3>(cfg, g, k, op, a, H.vb[l], final_out, om, final_scl, s);
       *final_done = true;
       XC_LAUNCH_CHECK();
@@ -2025,7 +2027,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -2362,6 +2364,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   // third of the iterations of the defaults there.
   if (mms) { cfg.nu = 4; cfg.coarse_cells = 256; cfg.coarse_sweeps = 200; }
   if (o.smooth_sweeps > 0) cfg.nu = o.smooth_sweeps;
+  if (o.post_sweeps > 0) cfg.nu_post = o.post_sweeps;
   if (o.omega_velocity > 0) cfg.omega_v = o.omega_velocity;
   if (o.schur_full_diagonal) { cfg.kplane = 0; cfg.cmass = 0.0; }
   if (o.schur_mass > 0) cfg.cmass = o.schur_mass;
