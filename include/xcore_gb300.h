@@ -109,6 +109,18 @@ typedef struct xc_solver_opts {
   int tiled_sweep;         /* 1: FP32 velocity sweeps from shared-memory tiles instead of per-row
                               reads (same results; measured 5% slower at 1024^2) */
   int post_sweeps;         /* velocity post-smoothing sweeps on the large levels (smooth_sweeps) */
+  int outer_solver;        /* mixed: 2 plain iterative refinement x += S dy per inner solve (default),
+                              1 FP64 FGMRES whose preconditioner is the FP32 inner solve (measured
+                              4% slower at 1024^2: the inner solves' corrections are nearly
+                              independent, so keeping them gains no iterations) */
+  int fused_pressure_cells; /* pressure-multigrid levels of at most this many cells fuse the first
+                               sweep, residual and restriction (descent) and the prolongation and
+                               first post sweep (ascent) into one launch each; larger levels launch
+                               each operation (same results either way; default and -1: none,
+                               measured no faster) */
+  int stage_small_levels;  /* 1: the one-CTA V-cycles of the small levels stage them in shared
+                              memory instead of reading global memory (same results; measured
+                              1.5% slower at 1024^2) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

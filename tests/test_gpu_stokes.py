@@ -91,6 +91,60 @@ def test_tiled_fp32_sweep_gives_the_per_row_results():
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("solver,psweeps", [("mixed", 1), ("mixed", 2), ("fgmres64", 1)])
+def test_fused_pressure_multigrid_gives_the_split_results(solver, psweeps):
+    """The fused descent (sweep from zero + residual + restriction) and ascent
+    (prolongation + sweep) kernels of the pressure multigrid form the same
+    values as one launch per operation: same bits, same iteration count."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=48, Nx=40, steps=2)
+    coefs = O.time_coefs("bd2im", 3)
+    out = []
+    for fuse in (1 << 30, -1):
+        ds = device_state(par, g, sc, st)
+        info = ds.fluidmech(coefs, dt, solver=solver, rtol=1e-9, pressure_sweeps=psweeps,
+                           fused_pressure_cells=fuse)
+        out.append((info["iterations"], [ds[k] for k in ("W", "U", "P")]))
+        ds.close()
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("solver", ["mixed", "fgmres64"])
+def test_staged_small_levels_give_the_global_memory_results(solver):
+    """The one-CTA V-cycles of the small multigrid levels run the same
+    operations whether their levels are staged in shared memory or read from
+    global memory: same bits, same iteration count."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=48, Nx=40, steps=2)
+    coefs = O.time_coefs("bd2im", 3)
+    out = []
+    for stage in (True, False):
+        ds = device_state(par, g, sc, st)
+        info = ds.fluidmech(coefs, dt, solver=solver, rtol=1e-9, stage_small_levels=stage)
+        out.append((info["iterations"], [ds[k] for k in ("W", "U", "P")]))
+        ds.close()
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("outer", [1, 2])
+def test_mixed_outer_solvers_match_lu(outer):
+    """Both outer loops of the mixed solver (FP64 FGMRES over FP32 inner solves,
+    and plain iterative refinement) reach the FP64 residual target and the
+    sparse-LU solution within the mixed tolerance."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=32, Nx=40, steps=2)
+    ds = device_state(par, g, sc, st)
+    coefs = O.time_coefs("bd2im", 3)
+    O.fluidmech(st, g, par, coefs, dt)
+    info = ds.fluidmech(coefs, dt, solver="mixed", rtol=1e-9, maxit=2000, outer_solver=outer)
+    assert info["converged"] and info["rel_residual"] <= 1e-9, info
+    for k in ("W", "U", "P"):
+        e = _maxrel(ds[k], getattr(st, k))
+        assert e <= 1e-7, (k, e, info)
+    ds.close()
+
+
 def _mms_device(N):
     m = mms_sources(N, 10.0)
     # x0 only feeds the host-side scales, which the Stokes solve does not read

@@ -43,11 +43,12 @@ thread_local bool g_xc_pdl = true;
 #define PDL_ON g_xc_pdl
 
 template <typename... KArgs, typename... Args>
-void pdl(bool on, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
+void pdl_smem(bool on, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+              Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -56,6 +57,10 @@ void pdl(bool on, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t 
   cfg.numAttrs = on ? 1 : 0;
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
   xc_count_launch();
+}
+template <typename... KArgs, typename... Args>
+void pdl(bool on, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
+  pdl_smem(on, kernel, grid, block, 0, s, std::forward<Args>(args)...);
 }
 
 constexpr int kMaxLevels = 12;
@@ -208,6 +213,19 @@ template <typename T>
 __device__ __forceinline__ T sdiv(T r, T d) {
   if constexpr (kFly<T>) return __fdividef(r, d);
   else return r / d;
+}
+// rounded products and sums the compiler may not contract into FMAs: the
+// pressure multigrid forms the same values in its fused and split kernels,
+// whose inlined contexts would otherwise contract differently
+template <typename T>
+__device__ __forceinline__ T mul_rn(T a, T b) {
+  if constexpr (kFly<T>) return __fmul_rn(a, b);
+  else return __dmul_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b) {
+  if constexpr (kFly<T>) return __fadd_rn(a, b);
+  else return __dadd_rn(a, b);
 }
 
 // dw / du and the FP32 viscosity copies of one level (terms as vel_coef_kernel)
@@ -929,21 +947,37 @@ __global__ void vel_coarse_kernel(Geo g, OpConst k, VOp<T> op, T* x, T* x2, cons
 // (L p)_c = sum_faces k_f (p_c - p_n) + dpin p_pin
 // kx[j,i]: face left of cell (j,i) (periodic); kz[j,i]: face above (kz[0]=kz[Nz]=0)
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ T p_apply_at(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
-                                        int pin, T dpin, const T* p, int j, int i, T* diag) {
+// (L p)(j, i) with p(j', i') supplied by pv -- a stored array or values formed
+// on the fly by the fused kernels below; one body, so both give the same bits
+template <typename T, typename PV>
+__device__ __forceinline__ T p_apply_fn(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
+                                        int pin, T dpin, PV pv, int j, int i, T* diag) {
   size_t c = (size_t)i * Nz + j;
   int il = i == 0 ? Nx - 1 : i - 1, ir = i == Nx - 1 ? 0 : i + 1;
   T kl = kx[c], kr = kx[(size_t)ir * Nz + j];
   T kt = kz[(size_t)i * (Nz + 1) + j], kb = kz[(size_t)i * (Nz + 1) + j + 1];
-  T pc = p[c];
-  T s = kl * (pc - p[(size_t)il * Nz + j]) + kr * (pc - p[(size_t)ir * Nz + j]);
-  if (j > 0) s += kt * (pc - p[c - 1]);
-  if (j < Nz - 1) s += kb * (pc - p[c + 1]);
+  T pc = pv(j, i);
+  T s = add_rn<T>(mul_rn<T>(kl, pc - pv(j, il)), mul_rn<T>(kr, pc - pv(j, ir)));
+  if (j > 0) s = add_rn<T>(s, mul_rn<T>(kt, pc - pv(j - 1, i)));
+  if (j < Nz - 1) s = add_rn<T>(s, mul_rn<T>(kb, pc - pv(j + 1, i)));
   T d = kl + kr + (j > 0 ? kt : (T)0) + (j < Nz - 1 ? kb : (T)0);
-  if ((int)c == pin) { s += dpin * pc; d += dpin; }
+  if ((int)c == pin) { s = add_rn<T>(s, mul_rn<T>(dpin, pc)); d += dpin; }
   *diag = d;
   return s;
+}
+template <typename T>
+__device__ __forceinline__ T p_apply_at(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
+                                        int pin, T dpin, const T* p, int j, int i, T* diag) {
+  return p_apply_fn<T>(Nz, Nx, kx, kz, pin, dpin, [=](int jj, int ii) { return p[(size_t)ii * Nz + jj]; }, j, i,
+                       diag);
+}
+// the first Jacobi sweep from zero at one cell: omega b / d
+template <typename T>
+__device__ __forceinline__ T p_jacobi0_val(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz,
+                                           int pin, T dpin, const T* b, T omega, int j, int i) {
+  T d;
+  p_apply_fn<T>(Nz, Nx, kx, kz, pin, dpin, [](int, int) { return (T)0; }, j, i, &d);   // only the diagonal
+  return d > (T)0 ? sdiv<T>(omega * b[(size_t)i * Nz + j], d) : (T)0;
 }
 
 template <typename T>
@@ -953,8 +987,7 @@ __device__ __forceinline__ void p_jacobi_at(int Nz, int Nx, const T* __restrict_
   int j = t % Nz, i = t / Nz;
   T d;
   if (zero_init) {
-    p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, b, j, i, &d);   // only the diagonal is used
-    xo[t] = d > (T)0 ? sdiv<T>(omega * b[t], d) : (T)0;
+    xo[t] = p_jacobi0_val<T>(Nz, Nx, kx, kz, pin, dpin, b, omega, j, i);
     return;
   }
   T ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xi, j, i, &d);
@@ -1000,16 +1033,21 @@ __global__ void p_restrict_kernel(int Nzc, int Nxc, const T* __restrict__ r, T* 
   p_restrict_at<T>(Nzc, Nxc, r, bc, t);
 }
 
+// bilinear prolongation of the coarse correction to fine cell (j, i)
 template <typename T>
-__device__ __forceinline__ void p_prolong_at(int Nzc, int Nxc, const T* xc, T* xf, int t) {
-  const int Nz = 2 * Nzc;
-  int j = t % Nz, i = t / Nz;
+__device__ __forceinline__ T p_prolong_val(int Nzc, int Nxc, const T* xc, int j, int i) {
   int J = j / 2, I = i / 2;
   int Jn = (j % 2 == 0) ? (J > 0 ? J - 1 : 0) : (J < Nzc - 1 ? J + 1 : Nzc - 1);
   int In = (i % 2 == 0) ? (I - 1 + Nxc) % Nxc : (I + 1) % Nxc;
-  T v = (T)9 * xc[(size_t)I * Nzc + J] + (T)3 * xc[(size_t)I * Nzc + Jn] + (T)3 * xc[(size_t)In * Nzc + J] +
-        xc[(size_t)In * Nzc + Jn];
-  xf[t] += v / (T)16;
+  T v = add_rn<T>(add_rn<T>(add_rn<T>(mul_rn<T>((T)9, xc[(size_t)I * Nzc + J]), mul_rn<T>((T)3, xc[(size_t)I * Nzc + Jn])),
+                            mul_rn<T>((T)3, xc[(size_t)In * Nzc + J])),
+                  xc[(size_t)In * Nzc + Jn]);
+  return mul_rn<T>(v, (T)0.0625);
+}
+template <typename T>
+__device__ __forceinline__ void p_prolong_at(int Nzc, int Nxc, const T* xc, T* xf, int t) {
+  const int Nz = 2 * Nzc;
+  xf[t] = add_rn<T>(xf[t], p_prolong_val<T>(Nzc, Nxc, xc, t % Nz, t / Nz));
 }
 template <typename T>
 __global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* xf) {
@@ -1017,6 +1055,61 @@ __global__ void p_prolong_kernel(int Nzc, int Nxc, const T* __restrict__ xc, T* 
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 4 * Nzc * Nxc) return;
   p_prolong_at<T>(Nzc, Nxc, xc, xf, t);
+}
+
+// Fused descent of one pressure level (one thread per coarse cell): the
+// residual b - L x of its four fine cells, restricted.  zero_init: x is the
+// first Jacobi sweep from zero, formed on the fly at the cells the stencils
+// read and stored at the thread's own four cells (pre-smoothing of one sweep).
+// Same values as p_jacobi (from zero) + p_residual + p_restrict.
+template <typename T>
+__global__ void p_down_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin, T dpin,
+                              T* x, const T* __restrict__ b, T* bc, T omega, int zero_init) {
+  XC_PDL_WAIT();
+  const int Nzc = Nz / 2, Nxc = Nx / 2;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nzc * Nxc) return;
+  const int J = t % Nzc, I = t / Nzc;
+  T r[4];
+  for (int q = 0; q < 4; ++q) {
+    const int j = 2 * J + (q & 1), i = 2 * I + (q >> 1);
+    T d;
+    T ax;
+    if (zero_init)
+      ax = p_apply_fn<T>(Nz, Nx, kx, kz, pin, dpin,
+                         [=](int jj, int ii) { return p_jacobi0_val<T>(Nz, Nx, kx, kz, pin, dpin, b, omega, jj, ii); },
+                         j, i, &d);
+    else
+      ax = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, x, j, i, &d);
+    r[q] = b[(size_t)i * Nz + j] - ax;
+  }
+  if (zero_init)
+    for (int q = 0; q < 4; ++q) {
+      const int j = 2 * J + (q & 1), i = 2 * I + (q >> 1);
+      x[(size_t)i * Nz + j] = p_jacobi0_val<T>(Nz, Nx, kx, kz, pin, dpin, b, omega, j, i);
+    }
+  // p_restrict_at's order: (2J, 2I), (2J+1, 2I), (2J, 2I+1), (2J+1, 2I+1)
+  bc[t] = (T)0.25 * (r[0] + r[1] + r[2] + r[3]);
+}
+
+// Fused ascent (one thread per fine cell): the first post-smoothing Jacobi
+// sweep of x + P xc, the coarse correction added on the fly at the cells the
+// stencil reads; xo != x.  Same values as p_prolong + p_jacobi.
+template <typename T>
+__global__ void p_up_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin, T dpin,
+                            const T* __restrict__ xc, const T* __restrict__ x, const T* __restrict__ b, T* xo,
+                            T omega) {
+  XC_PDL_WAIT();
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Nz * Nx) return;
+  const int Nzc = Nz / 2, Nxc = Nx / 2;
+  const int j = t % Nz, i = t / Nz;
+  auto xv = [=](int jj, int ii) {
+    return add_rn<T>(x[(size_t)ii * Nz + jj], p_prolong_val<T>(Nzc, Nxc, xc, jj, ii));
+  };
+  T d;
+  T ax = p_apply_fn<T>(Nz, Nx, kx, kz, pin, dpin, xv, j, i, &d);
+  xo[t] = d > (T)0 ? xv(j, i) + sdiv<T>(omega * (b[t] - ax), d) : (T)0;
 }
 
 template <typename T>
@@ -1112,10 +1205,84 @@ __host__ __device__ __forceinline__ OpConst level_const(const OpConst& k, int l)
   return c;
 }
 
+// Shared-memory staging of the one-CTA V-cycles.  The small levels are a few
+// hundred unknowns each, and every sweep of them is a chain of dependent loads
+// separated by CTA barriers: from shared memory instead of L2 each sweep costs
+// a fraction of the latency.  Arrays are carved in a fixed order, each rounded
+// up to 16 bytes; the host sizes the dynamic allocation with the same counts.
 template <typename T>
-__global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> L, OpConst kf, int l0, int lc, int nu,
-                                                                T om, int csweeps) {
+__host__ __device__ __forceinline__ long long smem_round(long long c) {
+  constexpr long long q = 16 / sizeof(T);
+  return (c + q - 1) / q * q;
+}
+template <typename T>
+__host__ __device__ inline long long vel_stage_elems(const Geo* gs, int l0, int lc) {
+  long long e = 0;
+  for (int q = l0; q <= lc; ++q) {
+    const Geo& g = gs[q];
+    if (kFly<T>)
+      e += smem_round<T>((long long)g.Nz * g.Nx) + smem_round<T>((long long)(g.Nz + 1) * (g.Nx + 1)) +
+           smem_round<T>(g.NW) + smem_round<T>(g.NU) + smem_round<T>(3LL * (g.Nx + 2));
+    else
+      e += smem_round<T>(10LL * g.NW) + smem_round<T>(10LL * g.NU);
+    e += 4 * smem_round<T>((long long)g.NW + g.NU);
+  }
+  return e;
+}
+template <typename T>
+__device__ __forceinline__ void cta_copy(T* dst, const T* src, long long n) {
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) dst[t] = src[t];
+}
+constexpr size_t kStageMaxBytes = 160 * 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> Lg, OpConst kf, int l0, int lc, int nu,
+                                                                T om, int csweeps, int staged) {
   XC_PDL_WAIT();
+  extern __shared__ __align__(16) unsigned char xc_stage[];
+  __shared__ VelLevels<T> L;
+  if (threadIdx.x == 0) {
+    T* p = reinterpret_cast<T*>(xc_stage);
+    for (int q = l0; q <= lc; ++q) {
+      const Geo& g = Lg.g[q];
+      L.g[q] = g; L.op[q] = Lg.op[q];
+      L.x[q] = Lg.x[q]; L.x2[q] = Lg.x2[q]; L.b[q] = Lg.b[q]; L.r[q] = Lg.r[q];
+      if (!staged) continue;
+      if constexpr (kFly<T>) {
+        L.op[q].eta = p; p += smem_round<T>((long long)g.Nz * g.Nx);
+        L.op[q].etaco = p; p += smem_round<T>((long long)(g.Nz + 1) * (g.Nx + 1));
+        L.op[q].dw = p; p += smem_round<T>(g.NW);
+        L.op[q].du = p; p += smem_round<T>(g.NU);
+        L.op[q].dbot = p; p += smem_round<T>(3LL * (g.Nx + 2));
+      } else {
+        L.op[q].cw = p; p += smem_round<T>(10LL * g.NW);
+        L.op[q].cu = p; p += smem_round<T>(10LL * g.NU);
+      }
+      const long long nvv = (long long)g.NW + g.NU;
+      L.x[q] = p; p += smem_round<T>(nvv);
+      L.x2[q] = p; p += smem_round<T>(nvv);
+      L.b[q] = p; p += smem_round<T>(nvv);
+      L.r[q] = p; p += smem_round<T>(nvv);
+    }
+  }
+  __syncthreads();
+  if (staged) {
+    for (int q = l0; q <= lc; ++q) {
+      const Geo& g = L.g[q];
+      if constexpr (kFly<T>) {
+        cta_copy<T>(const_cast<T*>(L.op[q].eta), Lg.op[q].eta, (long long)g.Nz * g.Nx);
+        cta_copy<T>(const_cast<T*>(L.op[q].etaco), Lg.op[q].etaco, (long long)(g.Nz + 1) * (g.Nx + 1));
+        cta_copy<T>(const_cast<T*>(L.op[q].dw), Lg.op[q].dw, g.NW);
+        cta_copy<T>(const_cast<T*>(L.op[q].du), Lg.op[q].du, g.NU);
+        cta_copy<T>(const_cast<T*>(L.op[q].dbot), Lg.op[q].dbot, 3LL * (g.Nx + 2));
+      } else {
+        cta_copy<T>(const_cast<T*>(L.op[q].cw), Lg.op[q].cw, 10LL * g.NW);
+        cta_copy<T>(const_cast<T*>(L.op[q].cu), Lg.op[q].cu, 10LL * g.NU);
+      }
+    }
+    cta_copy<T>(L.b[l0], Lg.b[l0], (long long)L.g[l0].NW + L.g[l0].NU);
+    __syncthreads();
+  }
   for (int l = l0; l < lc; ++l) {
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
@@ -1138,6 +1305,7 @@ __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> L, 
     __syncthreads();
     vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, false);
   }
+  if (staged) cta_copy<T>(Lg.x[l0], L.x[l0], (long long)L.g[l0].NW + L.g[l0].NU);
 }
 
 template <typename T>
@@ -1178,9 +1346,45 @@ __device__ void p_smooth_cta(const PLevels<T>& L, int l, T om, int sweeps, bool 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> L, int l0, int lc, int nu, T om,
-                                                              int csweeps) {
+__host__ __device__ inline long long p_stage_elems(const int* Nzs, const int* Nxs, int l0, int lc) {
+  long long e = 0;
+  for (int q = l0; q <= lc; ++q) {
+    const long long n = (long long)Nzs[q] * Nxs[q];
+    e += 5 * smem_round<T>(n) + smem_round<T>((long long)(Nzs[q] + 1) * Nxs[q]);
+  }
+  return e;
+}
+template <typename T>
+__global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> Lg, int l0, int lc, int nu, T om,
+                                                              int csweeps, int staged) {
   XC_PDL_WAIT();
+  extern __shared__ __align__(16) unsigned char xc_stage[];
+  __shared__ PLevels<T> L;
+  if (threadIdx.x == 0) {
+    T* p = reinterpret_cast<T*>(xc_stage);
+    for (int q = l0; q <= lc; ++q) {
+      L.Nz[q] = Lg.Nz[q]; L.Nx[q] = Lg.Nx[q]; L.pin[q] = Lg.pin[q]; L.dpin[q] = Lg.dpin[q];
+      L.kx[q] = Lg.kx[q]; L.kz[q] = Lg.kz[q];
+      L.x[q] = Lg.x[q]; L.x2[q] = Lg.x2[q]; L.b[q] = Lg.b[q]; L.r[q] = Lg.r[q];
+      if (!staged) continue;
+      const long long n = (long long)Lg.Nz[q] * Lg.Nx[q];
+      L.kx[q] = p; p += smem_round<T>(n);
+      L.kz[q] = p; p += smem_round<T>((long long)(Lg.Nz[q] + 1) * Lg.Nx[q]);
+      L.x[q] = p; p += smem_round<T>(n);
+      L.x2[q] = p; p += smem_round<T>(n);
+      L.b[q] = p; p += smem_round<T>(n);
+      L.r[q] = p; p += smem_round<T>(n);
+    }
+  }
+  __syncthreads();
+  if (staged) {
+    for (int q = l0; q <= lc; ++q) {
+      cta_copy<T>(const_cast<T*>(L.kx[q]), Lg.kx[q], (long long)L.Nz[q] * L.Nx[q]);
+      cta_copy<T>(const_cast<T*>(L.kz[q]), Lg.kz[q], (long long)(L.Nz[q] + 1) * L.Nx[q]);
+    }
+    cta_copy<T>(L.b[l0], Lg.b[l0], (long long)L.Nz[l0] * L.Nx[l0]);
+    __syncthreads();
+  }
   for (int l = l0; l < lc; ++l) {
     const int Nz = L.Nz[l], Nx = L.Nx[l], n = Nz * Nx;
     p_smooth_cta<T>(L, l, om, nu, true);
@@ -1199,6 +1403,7 @@ __global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> L, int 
     __syncthreads();
     p_smooth_cta<T>(L, l, om, nu, false);
   }
+  if (staged) cta_copy<T>(Lg.x[l0], L.x[l0], (long long)L.Nz[l0] * L.Nx[l0]);
 }
 
 // fine-level pressure coefficients from the velocity diagonal (plane 0: full,
@@ -1760,6 +1965,15 @@ struct SolveCfg {
   // velocity diagonal instead (cmass then defaults to 0)
   double cmass = 0.5;
   int kplane = 9;
+  // pressure levels of at most this many cells use the fused descent /
+  // ascent kernels, larger ones one launch per operation (none by default:
+  // measured no faster at any level size, programmatic launch already hides
+  // the launches they save, and 1% slower on the fine levels)
+  long long pfuse_cells = 0;
+  // one-CTA levels staged in shared memory (off by default: measured 1.5%
+  // slower at 1024^2 -- the small levels' sweeps are bound by instruction
+  // latency on one SM, and their L1-resident loads gain nothing from it)
+  bool stage_small = false;
 };
 
 // Jacobi sweeps on a coarsest level of Nz x Nx cells: a few times the grid's
@@ -1812,8 +2026,10 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
       L.g[q] = H.vg[q]; L.op[q] = vop(H, q);
       L.x[q] = H.vx[q]; L.x2[q] = H.vx2[q]; L.b[q] = H.vb[q]; L.r[q] = H.vr[q];
     }
-    pdl(PDL_ON, vel_vcycle_small_kernel<T>, 1, coarse_threads(n), s, L, kf, l, lc, cfg.nu, om,
-                                                              coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx));
+    const size_t bytes = sizeof(T) * (size_t)vel_stage_elems<T>(H.vg, l, lc);
+    const int staged = cfg.stage_small && bytes <= kStageMaxBytes;
+    pdl_smem(PDL_ON, vel_vcycle_small_kernel<T>, 1, coarse_threads(n), staged ? bytes : 0, s, L, kf, l, lc, cfg.nu,
+             om, coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx), staged);
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
@@ -1858,10 +2074,14 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   return XC_OK;
 }
 
+// ---- pressure V-cycle on level l: solve L x = pb[l] approximately; *res is
+// the buffer holding x (px[l] or px2[l]: the sweeps alternate between the two
+// and no copy is made)
 template <typename T>
-int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
+int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s, T** res) {
   const int Nz = H.pNz[l], Nx = H.pNx[l], n = Nz * Nx;
   const T om = (T)cfg.omega_p;
+  *res = H.px[l];
   if (!p_coarsest(H, cfg, l) && (long long)n <= cfg.small_cells) {
     int lc = l;
     while (!p_coarsest(H, cfg, lc)) ++lc;
@@ -1871,8 +2091,10 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
       L.kx[q] = H.kx[q]; L.kz[q] = H.kz[q];
       L.x[q] = H.px[q]; L.x2[q] = H.px2[q]; L.b[q] = H.pb[q]; L.r[q] = H.pr[q];
     }
-    pdl(PDL_ON, p_vcycle_small_kernel<T>, 1, coarse_threads(n), s, L, l, lc, cfg.nu_p, om,
-                                                            coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]));
+    const size_t bytes = sizeof(T) * (size_t)p_stage_elems<T>(H.pNz, H.pNx, l, lc);
+    const int staged = cfg.stage_small && bytes <= kStageMaxBytes;
+    pdl_smem(PDL_ON, p_vcycle_small_kernel<T>, 1, coarse_threads(n), staged ? bytes : 0, s, L, l, lc, cfg.nu_p, om,
+             coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]), staged);
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
@@ -1882,31 +2104,60 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s) {
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
-  pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
-                                             H.px[l], om, 1);
+  const int Nzc = H.pNz[l + 1], Nxc = H.pNx[l + 1];
+  T* ec = nullptr;
+  if ((long long)n > cfg.pfuse_cells) {
+    // one launch per operation (same values as the fused path below)
+    pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
+                                               H.px[l], om, 1);
+    T* a = H.px[l];
+    T* o = H.px2[l];
+    for (int q = 1; q < cfg.nu_p; ++q) {
+      pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                                 om, 0);
+      T* tmp = a; a = o; o = tmp;
+    }
+    pdl(PDL_ON, p_residual_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l],
+                                                 H.pr[l]);
+    pdl(PDL_ON, p_restrict_kernel<T>, nblk(Nzc * Nxc), 256, s, Nzc, Nxc, H.pr[l], H.pb[l + 1]);
+    XC_LAUNCH_CHECK();
+    XC_TRY(vcycle_p<T>(H, cfg, l + 1, s, &ec));
+    pdl(PDL_ON, p_prolong_kernel<T>, nblk(n), 256, s, Nzc, Nxc, ec, a);
+    for (int q = 0; q < cfg.nu_p; ++q) {
+      pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                                 om, 0);
+      T* tmp = a; a = o; o = tmp;
+    }
+    *res = a;
+    XC_LAUNCH_CHECK();
+    return XC_OK;
+  }
+  // pre-smoothing: with one sweep, the sweep from zero, the residual and the
+  // restriction are one launch; otherwise the last of them fuses the last two
   T* a = H.px[l];
   T* o = H.px2[l];
+  if (cfg.nu_p > 1) {
+    pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], a,
+                                               om, 1);
+    for (int q = 1; q < cfg.nu_p; ++q) {
+      pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
+                                                 om, 0);
+      T* tmp = a; a = o; o = tmp;
+    }
+  }
+  pdl(PDL_ON, p_down_kernel<T>, nblk(Nzc * Nxc), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l],
+                                             H.pb[l + 1], om, cfg.nu_p > 1 ? 0 : 1);
+  XC_LAUNCH_CHECK();
+  XC_TRY(vcycle_p<T>(H, cfg, l + 1, s, &ec));
+  // post-smoothing: the first sweep takes the prolongation along
+  pdl(PDL_ON, p_up_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], ec, a, H.pb[l], o, om);
+  { T* tmp = a; a = o; o = tmp; }
   for (int q = 1; q < cfg.nu_p; ++q) {
     pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
                                                om, 0);
     T* tmp = a; a = o; o = tmp;
   }
-  if (a != H.px[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.px[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-  pdl(PDL_ON, p_residual_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l], H.pb[l],
-                                               H.pr[l]);
-  const int Nzc = H.pNz[l + 1], Nxc = H.pNx[l + 1];
-  pdl(PDL_ON, p_restrict_kernel<T>, nblk(Nzc * Nxc), 256, s, Nzc, Nxc, H.pr[l], H.pb[l + 1]);
-  XC_LAUNCH_CHECK();
-  XC_TRY(vcycle_p<T>(H, cfg, l + 1, s));
-  pdl(PDL_ON, p_prolong_kernel<T>, nblk(n), 256, s, Nzc, Nxc, H.px[l + 1], H.px[l]);
-  a = H.px[l];
-  o = H.px2[l];
-  for (int q = 0; q < cfg.nu_p; ++q) {
-    pdl(PDL_ON, p_jacobi_kernel<T>, nblk(n), 256, s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], a, H.pb[l], o,
-                                               om, 0);
-    T* tmp = a; a = o; o = tmp;
-  }
-  if (a != H.px[l]) XC_CUDA_TRY(cudaMemcpyAsync(H.px[l], a, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+  *res = a;
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -1924,9 +2175,10 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   // pressure: interior solve with ghost elimination
   pdl(PDL_ON, p_gather_kernel<T>, nblk(g.Nz * g.Nx), 256, s, g, H.kx[0], H.kr, H.rp, H.pb[0]);
   XC_LAUNCH_CHECK();
-  XC_TRY(vcycle_p<T>(H, cfg, 0, s));
+  T* px0 = nullptr;
+  XC_TRY(vcycle_p<T>(H, cfg, 0, s, &px0));
   T* zp = out + nvv;   // physical z_p written directly into out, rescaled below
-  pdl(PDL_ON, p_scatter_kernel<T>, nblk((long long)g.Nz * g.Nx), 256, s, g, H.px[0], H.rp, H.etarho, (T)cfg.cmass, zp);
+  pdl(PDL_ON, p_scatter_kernel<T>, nblk((long long)g.Nz * g.Nx), 256, s, g, px0, H.rp, H.etarho, (T)cfg.cmass, zp);
   pdl(PDL_ON, p_scatter_cols_kernel<T>, nblk(g.Nz + 1), 256, s, g, H.rp, zp, k.open_cnv);
   pdl(PDL_ON, p_scatter_rows_kernel<T>, nblk(g.Nx + 2), 256, s, g, H.rp, zp);
   // velocity: rhs r_v - GG z_p, one V-cycle
@@ -1998,14 +2250,15 @@ int dot_self(StokesWork* w, Hier<T>& H, const T* v, long long n, int slot, cudaS
 // Gram-Schmidt passes against v_0..v_k (coefficients to hdev[8..]); ||w||^2 to
 // hdev[2]; v_{k+1} = w / ||w||; the H column to the pinned host mirror.
 template <typename T>
-int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s) {
+int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s,
+                     bool with_precond = true) {
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   T* vk = H.V + (size_t)kk * n;
   T* zk = H.Z + (size_t)kk * n;
   T* wv = H.V + (size_t)(kk + 1) * n;
   if (kk + 1 > 32) { xc_set_error("fgmres: restart above 32 basis vectors"); return XC_BAD_ARG; }
-  XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
+  if (with_precond) XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
   XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
   double* hd = w->hdev + 8;
   for (int pass = 0; pass < cfg.gs_passes; ++pass) {
@@ -2027,7 +2280,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -2067,38 +2320,97 @@ int arnoldi_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cf
   return XC_OK;
 }
 
+// Hessenberg least-squares problem of (F)GMRES, on the host: one Givens
+// rotation per new column, the residual estimate |g_{k+1}|, back substitution.
+struct HessLS {
+  int m;
+  std::vector<double> Hm, cs, sn, gv, yv;
+  explicit HessLS(int m_) : m(m_), Hm((size_t)(m_ + 1) * m_), cs(m_), sn(m_), gv(m_ + 1), yv(m_) {}
+  void start(double beta) {
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+  }
+  // column kk from the Gram-Schmidt coefficients (one or two passes, summed)
+  // and ||w||; returns the new residual estimate |g_{kk+1}|
+  double add(int kk, const double* h1, const double* h2, double hn) {
+    double* col = &Hm[(size_t)kk * (m + 1)];
+    for (int i = 0; i <= kk; ++i) col[i] = h1[i] + (h2 ? h2[i] : 0.0);
+    col[kk + 1] = hn;
+    for (int i = 0; i < kk; ++i) {
+      double a = col[i], b = col[i + 1];
+      col[i] = cs[i] * a + sn[i] * b;
+      col[i + 1] = -sn[i] * a + cs[i] * b;
+    }
+    double a = col[kk], b = col[kk + 1];
+    double r = std::hypot(a, b);
+    cs[kk] = r > 0 ? a / r : 1.0;
+    sn[kk] = r > 0 ? b / r : 0.0;
+    col[kk] = r;
+    col[kk + 1] = 0.0;
+    gv[kk + 1] = -sn[kk] * gv[kk];
+    gv[kk] = cs[kk] * gv[kk];
+    return std::fabs(gv[kk + 1]);
+  }
+  // coefficients of the first kk basis vectors -> yv
+  void solve(int kk) {
+    for (int i = kk - 1; i >= 0; --i) {
+      double sacc = gv[i];
+      for (int j = i + 1; j < kk; ++j) sacc -= Hm[(size_t)j * (m + 1) + i] * yv[j];
+      yv[i] = sacc / Hm[(size_t)i * (m + 1) + i];
+    }
+  }
+};
+
+// fgmres flags.  FG_ZERO_GUESS: start from y = 0 (set here), so the first
+// residual is rhs itself and no operator application is needed.  FG_TRUST_EST:
+// stop on the Givens estimate without recomputing the true residual (an inner
+// solve whose caller forms the exact FP64 residual anyway).
+constexpr int FG_ZERO_GUESS = 1;
+constexpr int FG_TRUST_EST = 2;
+
 // Right-preconditioned FGMRES(m) on the scaled system S LL S y = rhs, from the
 // initial guess in H.y (updated in place).  *its_out = iterations used,
-// *relres_out = ||rhs - A y|| / ||rhs|| of the true residual at the last restart.
+// *relres_out = ||rhs - A y|| / ||rhs|| of the true residual at the last restart
+// (the estimate under FG_TRUST_EST).
 template <typename T>
 int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* rhs, double rtol,
-           int maxit, int* its_out, double* relres_out, cudaStream_t s) {
+           int maxit, int* its_out, double* relres_out, cudaStream_t s, int flags = 0) {
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   const int m = H.m;
   double* hh = w->hhost;
+  const bool zero = (flags & FG_ZERO_GUESS) != 0;
   XC_TRY(dot_self<T>(w, H, rhs, n, 0, s));
+  if (zero) {
+    XC_CUDA_TRY(cudaMemsetAsync(H.y, 0, sizeof(T) * n, s));
+    // V[0] = rhs / ||rhs|| with the reciprocal dot_self left on the device
+    scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, rhs, H.V); xc_count_launch();
+  }
   XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
   XC_CUDA_TRY(cudaStreamSynchronize(s));
   const double bnorm = std::sqrt(hh[0]) > 0 ? std::sqrt(hh[0]) : 1.0;
   int its = 0;
   double relres = 1.0;
-  std::vector<double> Hm((size_t)(m + 1) * m), cs(m), sn(m), gv(m + 1), yv(m);
-  while (true) {
-    // r = rhs - A y  -> V[0]
-    XC_TRY(apply_scaled<T>(w, H, k, H.y, rhs, H.V, s));
-    XC_TRY(dot_self<T>(w, H, H.V, n, 0, s));
-    XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
-    XC_CUDA_TRY(cudaStreamSynchronize(s));
-    double beta = std::sqrt(hh[0]);
-    relres = beta / bnorm;
-    if (!(relres > rtol) || its >= maxit) break;
-    if (!std::isfinite(beta)) { *its_out = its; *relres_out = relres; xc_set_error("fgmres: non-finite residual"); return XC_NAN; }
-    hh[0] = 1.0 / beta;
-    XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 1, hh, sizeof(double), cudaMemcpyHostToDevice, s));
-    scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 1, H.V, H.V); xc_count_launch();
-    std::fill(gv.begin(), gv.end(), 0.0);
-    gv[0] = beta;
+  HessLS ls(m);
+  for (int cycle = 0;; ++cycle) {
+    double beta;
+    if (zero && cycle == 0) {
+      beta = std::sqrt(hh[0]);
+      relres = beta > 0 ? 1.0 : 0.0;
+      if (!(relres > rtol) || its >= maxit) break;
+    } else {
+      // r = rhs - A y  -> V[0]
+      XC_TRY(apply_scaled<T>(w, H, k, H.y, rhs, H.V, s));
+      XC_TRY(dot_self<T>(w, H, H.V, n, 0, s));
+      XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+      XC_CUDA_TRY(cudaStreamSynchronize(s));
+      beta = std::sqrt(hh[0]);
+      relres = beta / bnorm;
+      if (!(relres > rtol) || its >= maxit) break;
+      if (!std::isfinite(beta)) { *its_out = its; *relres_out = relres; xc_set_error("fgmres: non-finite residual"); return XC_NAN; }
+      scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, H.V, H.V); xc_count_launch();
+    }
+    ls.start(beta);
     int kk = 0;
     for (; kk < m && its < maxit; ++kk) {
       // z_k = M v_k, v_{k+1} = A z_k orthogonalised and normalised, H column
@@ -2106,43 +2418,89 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
       XC_TRY(arnoldi_step<T>(w, H, k, cfg, kk, s));
       XC_CUDA_TRY(cudaStreamSynchronize(s));
       XC_LAUNCH_CHECK();
-      for (int i = 0; i <= kk; ++i)
-        Hm[(size_t)kk * (m + 1) + i] = hh[8 + i] + (cfg.gs_passes > 1 ? hh[8 + kMaxRestart + i] : 0.0);
-      double hn = std::sqrt(hh[2]);
-      Hm[(size_t)kk * (m + 1) + kk + 1] = hn;
-      // Givens rotations on column kk
-      double* col = &Hm[(size_t)kk * (m + 1)];
-      for (int i = 0; i < kk; ++i) {
-        double a = col[i], b = col[i + 1];
-        col[i] = cs[i] * a + sn[i] * b;
-        col[i + 1] = -sn[i] * a + cs[i] * b;
-      }
-      double a = col[kk], b = col[kk + 1];
-      double r = std::hypot(a, b);
-      cs[kk] = r > 0 ? a / r : 1.0;
-      sn[kk] = r > 0 ? b / r : 0.0;
-      col[kk] = r;
-      col[kk + 1] = 0.0;
-      gv[kk + 1] = -sn[kk] * gv[kk];
-      gv[kk] = cs[kk] * gv[kk];
+      const double hn = std::sqrt(hh[2]);
       ++its;
-      relres = std::fabs(gv[kk + 1]) / bnorm;
+      relres = ls.add(kk, hh + 8, cfg.gs_passes > 1 ? hh + 8 + kMaxRestart : nullptr, hn) / bnorm;
       if (!std::isfinite(relres)) { xc_set_error("fgmres: breakdown"); return XC_NAN; }
       if (relres <= rtol * 0.5 || hn == 0.0) { ++kk; break; }
     }
     // back substitution and update y += Z yv
-    for (int i = kk - 1; i >= 0; --i) {
-      double sacc = gv[i];
-      for (int j = i + 1; j < kk; ++j) sacc -= Hm[(size_t)j * (m + 1) + i] * yv[j];
-      yv[i] = sacc / Hm[(size_t)i * (m + 1) + i];
-    }
-    XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 8, yv.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
+    ls.solve(kk);
+    XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 8, ls.yv.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
     combine_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
     XC_LAUNCH_CHECK();
+    if ((flags & FG_TRUST_EST) && (relres <= rtol || its >= maxit)) break;
   }
   *its_out = its;
   *relres_out = relres;
   return XC_OK;
+}
+
+// The mixed solver's outer loop as FGMRES(m) in FP64 on S LL S y = rhs (from
+// the initial guess in d.y), preconditioned by the whole FP32 inner solve:
+// z_k = inner FGMRES on v_k to a reduction of inner_rtol, then w = A z_k
+// orthogonalised in FP64.  Unlike plain refinement (y += inner(r) per pass)
+// it keeps every correction and combines them by the FP64 least-squares
+// problem.  *its_out counts FP32 inner iterations, *outer_out inner solves.
+int fgmres_outer(StokesWork* w, const OpConst& k, const SolveCfg& cfg, const SolveCfg& icfg, const double* rhs,
+                 double rtol, int maxit, double inner_rtol, int inner_maxit, int* its_out, int* outer_out,
+                 double* relres_out, cudaStream_t s) {
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  Hier<double>& H = w->d;
+  const int m = H.m;
+  double* hh = w->hhost;
+  XC_TRY(dot_self<double>(w, H, rhs, n, 0, s));
+  XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  const double bnorm = std::sqrt(hh[0]) > 0 ? std::sqrt(hh[0]) : 1.0;
+  int its = 0, outer = 0;
+  double relres = 1.0;
+  HessLS ls(m);
+  int status = XC_OK;
+  while (status == XC_OK) {
+    XC_TRY(apply_scaled<double>(w, H, k, H.y, rhs, H.V, s));
+    XC_TRY(dot_self<double>(w, H, H.V, n, 0, s));
+    XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    XC_CUDA_TRY(cudaStreamSynchronize(s));
+    const double beta = std::sqrt(hh[0]);
+    relres = beta / bnorm;
+    if (!std::isfinite(relres)) { xc_set_error("mixed solver: non-finite residual"); status = XC_NAN; break; }
+    if (relres <= rtol || its >= maxit || outer >= 50) break;
+    scale_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, H.V, H.V); xc_count_launch();
+    ls.start(beta);
+    int kk = 0;
+    for (; kk < m && its < maxit && outer < 50; ++kk) {
+      double* vk = H.V + (size_t)kk * n;
+      double* zk = H.Z + (size_t)kk * n;
+      convert_kernel<double, float><<<nblk(n), 256, 0, s>>>(n, vk, w->f.w); xc_count_launch();
+      int iits = 0;
+      double irr = 1.0;
+      XC_TRY(fgmres<float>(w, w->f, k, icfg, w->f.w, inner_rtol, inner_maxit, &iits, &irr, s,
+                           FG_ZERO_GUESS | FG_TRUST_EST));
+      its += iits;
+      ++outer;
+      convert_kernel<float, double><<<nblk(n), 256, 0, s>>>(n, w->f.y, zk); xc_count_launch();
+      XC_TRY(arnoldi_launches<double>(w, H, k, cfg, kk, s, false));
+      XC_CUDA_TRY(cudaStreamSynchronize(s));
+      XC_LAUNCH_CHECK();
+      const double hn = std::sqrt(hh[2]);
+      relres = ls.add(kk, hh + 8, cfg.gs_passes > 1 ? hh + 8 + kMaxRestart : nullptr, hn) / bnorm;
+      if (!std::isfinite(relres)) { xc_set_error("mixed solver: breakdown"); status = XC_NAN; ++kk; break; }
+      // the FP64 Arnoldi relation makes the estimate accurate far below rtol;
+      // the true residual above confirms it
+      if (relres <= rtol * 0.9 || hn == 0.0) { ++kk; break; }
+    }
+    if (status != XC_OK) break;
+    ls.solve(kk);
+    XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 8, ls.yv.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
+    combine_kernel<double><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
+    XC_LAUNCH_CHECK();
+  }
+  *its_out = its;
+  *outer_out = outer;
+  *relres_out = relres;
+  return status;
 }
 
 // build the operator coefficients and both multigrid hierarchies for one solve
@@ -2207,6 +2565,12 @@ int stokes_create(xc_ctx* c) {
     return XC_BAD_ARG;
   }
   std::call_once(g_md_once, md_grid_init);
+  // the one-CTA V-cycles stage their levels in up to kStageMaxBytes of shared memory
+  cudaFuncSetAttribute(vel_vcycle_small_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageMaxBytes);
+  cudaFuncSetAttribute(vel_vcycle_small_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageMaxBytes);
+  cudaFuncSetAttribute(p_vcycle_small_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageMaxBytes);
+  cudaFuncSetAttribute(p_vcycle_small_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageMaxBytes);
+  XC_CUDA_TRY(cudaGetLastError());
   StokesWork* w = new StokesWork();
   std::memset((void*)w, 0, sizeof(StokesWork));
   c->stokes = w;
@@ -2374,6 +2738,8 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.pressure_sweeps > 0) cfg.nu_p = o.pressure_sweeps;
   cfg.pdl = !o.serial_launch;
   cfg.tiled = o.tiled_sweep != 0;
+  cfg.stage_small = o.stage_small_levels != 0;
+  if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;
   g_xc_pdl = cfg.pdl;
   // the FP32 inner solve only has to reduce its residual by inner_rtol (1e-2
   // to 3e-2 with at most ~30 basis vectors), so one Gram-Schmidt pass does;
@@ -2397,7 +2763,14 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.kind == XC_SOLVER_MIXED) {
     if (!w->f_alloc) { XC_TRY(alloc_hier<float>(w, w->f, 30)); w->f_alloc = true; }
     XC_TRY(setup_hier<float>(w, w->f, k, cfg, c, s));
-    // FP64 norm of the scaled rhs
+    if (o.outer_solver == 1) {
+      div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, w->d.y); xc_count_launch();
+      status = fgmres_outer(w, k, cfg, icfg, w->r, o.rtol, o.maxit, o.inner_rtol, o.inner_maxit, &its,
+                            &refinements, &relres, s);
+      mul_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->d.y, w->d.scl, w->x); xc_count_launch();
+      XC_LAUNCH_CHECK();
+    } else {
+    // plain refinement: FP64 norm of the scaled rhs
     XC_TRY(dot_self<double>(w, w->d, w->r, n, 3, s));
     XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
     XC_CUDA_TRY(cudaStreamSynchronize(s));
@@ -2420,14 +2793,15 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       // lives in f.w, which the FP32 Krylov and multigrid code never writes
       // (f.t is the operator's scratch, f.V / f.Z the basis).
       convert_kernel<double, float><<<nblk(n), 256, 0, s>>>(n, res, w->f.w); xc_count_launch();
-      XC_CUDA_TRY(cudaMemsetAsync(w->f.y, 0, sizeof(float) * n, s));
       const float* frhs = w->f.w;
       int iits = 0;
       double irr = 1.0;
-      XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s));
+      XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
+                           FG_ZERO_GUESS | FG_TRUST_EST));
       its += iits;
       refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
       XC_LAUNCH_CHECK();
+    }
     }
   } else {
     div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, w->d.y); xc_count_launch();
