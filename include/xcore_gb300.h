@@ -121,6 +121,9 @@ typedef struct xc_solver_opts {
   int stage_small_levels;  /* 1: the one-CTA V-cycles of the small levels stage them in shared
                               memory instead of reading global memory (same results; measured
                               1.5% slower at 1024^2) */
+  int jacobi_coarse;       /* 1: Jacobi sweeps (coarse_sweeps) on the coarsest levels even where they
+                              have at most 64 unknowns, which by default are solved with their
+                              dense inverse (formed and inverted on the device once per solve) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

@@ -38,6 +38,24 @@ def test_fluidmech_matches_lu(shape, solver, rtol, tol):
     assert_fields(ds, st, ["MFS", "drhodt"], exact=True)
 
 
+@pytest.mark.parametrize("solver,rtol,tol", [("fgmres64", 1e-10, 1e-8), ("mixed", 1e-9, 1e-7)])
+@pytest.mark.parametrize("jacobi", [False, True])
+def test_coarse_solves_match_lu(solver, rtol, tol, jacobi):
+    """At 32x32 the coarsest levels (4x4 velocity cells, 60 unknowns; 2x2
+    pressure cells) are solved with their dense inverse by default, or by
+    Jacobi sweeps: both preconditioners give the sparse-LU solution."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=32, Nx=32, steps=2)
+    ds = device_state(par, g, sc, st)
+    coefs = O.time_coefs("bd2im", 3)
+    O.fluidmech(st, g, par, coefs, dt)
+    info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol, jacobi_coarse=jacobi)
+    assert info["converged"] and info["rel_residual"] <= rtol, info
+    for k in ("W", "U", "P"):
+        e = _maxrel(ds[k], getattr(st, k))
+        assert e <= tol, (k, e, info)
+    ds.close()
+
+
 @pytest.mark.parametrize("bc", [dict(sds=-1, top_cnv=-1, bot_cnv=-1), dict(sds=-1, top_cnv=-1, bot_cnv=1),
                                 dict(sds=1, top_cnv=1, bot_cnv=1)])
 def test_fluidmech_boundary_variants_match_lu(bc):

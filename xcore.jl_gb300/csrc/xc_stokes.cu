@@ -892,6 +892,99 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
   return s;
 }
 
+__device__ __forceinline__ double cta_max(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double m = 0;
+  for (int q = 0; q < nw; ++q) m = fmax(m, red[q]);
+  return m;
+}
+
+// ---- direct solve of a small coarsest level -------------------------------
+// A coarsest level of at most kDenseMax unknowns is solved with its inverse:
+// the dense matrix is formed once per solve by applying the level's rows to
+// unit vectors (kDenseBatch at a time), inverted in FP64 by Gauss-Jordan
+// elimination with partial pivoting, and each V-cycle's coarse solve becomes
+// one matrix-vector product by one CTA instead of tens of CTA-wide Jacobi
+// sweeps.  ok = 0 (the sweeps are used instead) on a pivot below 1e-12 of the
+// largest entry, or where the velocity level has the unlifted uniform-U mode.
+constexpr int kDenseMax = 64;
+constexpr int kDenseBatch = 16;
+
+// in-place inverse of the n x n row-major FP64 matrix M in shared memory
+__device__ void gj_invert_cta(double* M, int n, int* piv, int* ok, double* fcol, double* red, int* sprow) {
+  double amax = 0;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) amax = fmax(amax, fabs(M[e]));
+  amax = cta_max(amax, red);
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x < 32) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + (int)threadIdx.x; i < n; i += 32) {
+        const double v = fabs(M[i * n + k]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (threadIdx.x == 0) {
+        *sprow = bi;
+        piv[k] = bi;
+        if (!(best > 1e-12 * amax)) *ok = 0;
+      }
+    }
+    __syncthreads();
+    const int p = *sprow;
+    if (p != k)
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const double t = M[k * n + c];
+        M[k * n + c] = M[p * n + c];
+        M[p * n + c] = t;
+      }
+    __syncthreads();
+    const double pv = M[k * n + k];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = M[i * n + k];
+    __syncthreads();
+    // row k scaled; its pivot entry becomes 1 / pv
+    for (int c = threadIdx.x; c < n; c += blockDim.x) M[k * n + c] = (c == k ? 1.0 : M[k * n + c]) / pv;
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e / n, c = e - i * n;
+      if (i != k) M[e] = (c == k ? 0.0 : M[e]) - fcol[i] * M[k * n + c];
+    }
+    __syncthreads();
+  }
+  // A^-1 = (P A)^-1 P: the row interchanges undone as column interchanges, last first
+  for (int k = n - 1; k >= 0; --k) {
+    const int p = piv[k];
+    if (p != k)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double t = M[i * n + k];
+        M[i * n + k] = M[i * n + p];
+        M[i * n + p] = t;
+      }
+    __syncthreads();
+  }
+}
+
+// x = inv b by one CTA (a warp per row); ends with a barrier
+template <typename T>
+__device__ void dense_apply_cta(const T* __restrict__ inv, int n, const T* b, T* x) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = warp; r < n; r += nw) {
+    T acc = 0;
+    for (int c = lane; c < n; c += 32) acc += inv[r * n + c] * b[c];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[r] = acc;
+  }
+  __syncthreads();
+}
+
 // many damped-Jacobi sweeps on the coarsest velocity level, by one whole CTA.
 // With free slip at top and bottom (top_cnv = bot_cnv = -1) and periodic x, a
 // uniform U shift is a null mode of the viscous rows; where inertia does not
@@ -900,8 +993,12 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
 // coarse correction and left to the pinned fine level and the Krylov method.
 template <typename T>
 __device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const VOp<T>& op, T* x, T* x2, const T* b,
-                               int sweeps, T omega) {
+                               int sweeps, T omega, const T* inv = nullptr, const int* inv_ok = nullptr) {
   const long long n = (long long)g.NW + g.NU;
+  if (inv && *inv_ok) {
+    dense_apply_cta<T>(inv, (int)n, b, x);
+    return;
+  }
   for (long long t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
   __syncthreads();
   T* a = x;
@@ -937,9 +1034,61 @@ __device__ void vel_coarse_cta(const Geo& g, const OpConst& k, const VOp<T>& op,
 }
 template <typename T>
 __global__ void vel_coarse_kernel(Geo g, OpConst k, VOp<T> op, T* x, T* x2, const T* __restrict__ b, int sweeps,
-                                  T omega) {
+                                  T omega, const T* inv, const int* inv_ok) {
   XC_PDL_WAIT();
-  vel_coarse_cta<T>(g, k, op, x, x2, b, sweeps, omega);
+  vel_coarse_cta<T>(g, k, op, x, x2, b, sweeps, omega, inv, inv_ok);
+}
+
+// the inverse of the coarsest velocity level (NW + NU <= kDenseMax), one CTA
+template <typename T>
+__global__ void __launch_bounds__(1024) vel_dense_inv_kernel(Geo g, OpConst k, VOp<T> op, T* inv, int* ok) {
+  XC_PDL_WAIT();
+  __shared__ double M[kDenseMax * kDenseMax];
+  __shared__ T xb[kDenseBatch][kDenseMax];
+  __shared__ double fcol[kDenseMax];
+  __shared__ double red[32];
+  __shared__ int piv[kDenseMax];
+  __shared__ int sprow, sok;
+  const int n = g.NW + g.NU;
+  if (threadIdx.x == 0) sok = 1;
+  for (int c0 = 0; c0 < n; c0 += kDenseBatch) {
+    for (int e = threadIdx.x; e < kDenseBatch * kDenseMax; e += blockDim.x) {
+      const int bq = e / kDenseMax, r = e - bq * kDenseMax;
+      xb[bq][r] = (T)(r == c0 + bq ? 1 : 0);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kDenseBatch * n; e += blockDim.x) {
+      const int bq = e / n, r = e - bq * n, c = c0 + bq;
+      if (c >= n) continue;
+      const T* xv = xb[bq];
+      T d, v;
+      if (r < g.NW) {
+        v = vel_row_w<T, false>(g, k, op, xv, xv + g.NW, nullptr, r, r % (g.Nz + 1), r / (g.Nz + 1), &d);
+      } else {
+        const int u = r - g.NW;
+        v = vel_row_u<T, false>(g, k, op, xv, xv + g.NW, nullptr, u, u % (g.Nz + 2), u / (g.Nz + 2), &d);
+      }
+      M[r * n + c] = (double)v;
+    }
+    __syncthreads();
+  }
+  if (k.top_cnv == -1 && k.bot_cnv == -1 && !k.mms) {
+    double si = 0, sd = 0;
+    for (int u = threadIdx.x; u < g.NU; u += blockDim.x) {
+      const int j = u % (g.Nz + 2);
+      if (j >= 1 && j <= g.Nz) {
+        si += (double)vel_inertia_u<T>(g, op, u);
+        sd += (double)vel_diag<T>(g, k, op, g.NW + u);
+      }
+    }
+    si = cta_sum(si, red);
+    sd = cta_sum(sd, red);
+    if (threadIdx.x == 0 && si <= 1e-6 * sd) sok = 0;
+  }
+  __syncthreads();
+  gj_invert_cta(M, n, piv, &sok, fcol, red, &sprow);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = (T)M[e];
+  if (threadIdx.x == 0) *ok = sok;
 }
 
 // ---------------------------------------------------------------------------
@@ -1128,8 +1277,13 @@ __global__ void p_coarsen_kernel(int Nzc, int Nxc, const T* __restrict__ kx, con
 
 template <typename T>
 __device__ void p_coarse_cta(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
-                             T dpin, T* x, T* x2, const T* b, int sweeps, T omega) {
+                             T dpin, T* x, T* x2, const T* b, int sweeps, T omega, const T* inv = nullptr,
+                             const int* inv_ok = nullptr) {
   const int n = Nz * Nx;
+  if (inv && *inv_ok) {
+    dense_apply_cta<T>(inv, n, b, x);
+    return;
+  }
   for (int t = threadIdx.x; t < n; t += blockDim.x) x[t] = 0;
   __syncthreads();
   T* a = x;
@@ -1149,9 +1303,42 @@ __device__ void p_coarse_cta(int Nz, int Nx, const T* __restrict__ kx, const T* 
 }
 template <typename T>
 __global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const T* __restrict__ kz, int pin,
-                                T dpin, T* x, T* x2, const T* __restrict__ b, int sweeps, T omega) {
+                                T dpin, T* x, T* x2, const T* __restrict__ b, int sweeps, T omega, const T* inv,
+                                const int* inv_ok) {
   XC_PDL_WAIT();
-  p_coarse_cta<T>(Nz, Nx, kx, kz, pin, dpin, x, x2, b, sweeps, omega);
+  p_coarse_cta<T>(Nz, Nx, kx, kz, pin, dpin, x, x2, b, sweeps, omega, inv, inv_ok);
+}
+
+// the inverse of the coarsest pressure level (Nz Nx <= kDenseMax), one CTA
+template <typename T>
+__global__ void __launch_bounds__(1024) p_dense_inv_kernel(int Nz, int Nx, const T* __restrict__ kx,
+                                                           const T* __restrict__ kz, int pin, T dpin, T* inv, int* ok) {
+  XC_PDL_WAIT();
+  __shared__ double M[kDenseMax * kDenseMax];
+  __shared__ T xb[kDenseBatch][kDenseMax];
+  __shared__ double fcol[kDenseMax];
+  __shared__ double red[32];
+  __shared__ int piv[kDenseMax];
+  __shared__ int sprow, sok;
+  const int n = Nz * Nx;
+  if (threadIdx.x == 0) sok = 1;
+  for (int c0 = 0; c0 < n; c0 += kDenseBatch) {
+    for (int e = threadIdx.x; e < kDenseBatch * kDenseMax; e += blockDim.x) {
+      const int bq = e / kDenseMax, r = e - bq * kDenseMax;
+      xb[bq][r] = (T)(r == c0 + bq ? 1 : 0);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kDenseBatch * n; e += blockDim.x) {
+      const int bq = e / n, r = e - bq * n, c = c0 + bq;
+      if (c >= n) continue;
+      T d;
+      M[r * n + c] = (double)p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xb[bq], r % Nz, r / Nz, &d);
+    }
+    __syncthreads();
+  }
+  gj_invert_cta(M, n, piv, &sok, fcol, red, &sprow);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = (T)M[e];
+  if (threadIdx.x == 0) *ok = sok;
 }
 
 // ---------------------------------------------------------------------------
@@ -1237,7 +1424,8 @@ constexpr size_t kStageMaxBytes = 160 * 1024;
 
 template <typename T>
 __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> Lg, OpConst kf, int l0, int lc, int nu,
-                                                                T om, int csweeps, int staged) {
+                                                                T om, int csweeps, int staged, const T* inv,
+                                                                const int* inv_ok) {
   XC_PDL_WAIT();
   extern __shared__ __align__(16) unsigned char xc_stage[];
   __shared__ VelLevels<T> L;
@@ -1296,7 +1484,7 @@ __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> Lg,
     for (long long t = threadIdx.x; t < nc; t += blockDim.x) vel_restrict_at<T>(g, c, L.r[l], L.b[l + 1], t);
     __syncthreads();
   }
-  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.op[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om);
+  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.op[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om, inv, inv_ok);
   for (int l = lc - 1; l >= l0; --l) {
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
@@ -1356,7 +1544,8 @@ __host__ __device__ inline long long p_stage_elems(const int* Nzs, const int* Nx
 }
 template <typename T>
 __global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> Lg, int l0, int lc, int nu, T om,
-                                                              int csweeps, int staged) {
+                                                              int csweeps, int staged, const T* inv,
+                                                              const int* inv_ok) {
   XC_PDL_WAIT();
   extern __shared__ __align__(16) unsigned char xc_stage[];
   __shared__ PLevels<T> L;
@@ -1396,7 +1585,7 @@ __global__ void __launch_bounds__(1024) p_vcycle_small_kernel(PLevels<T> Lg, int
     __syncthreads();
   }
   p_coarse_cta<T>(L.Nz[lc], L.Nx[lc], L.kx[lc], L.kz[lc], L.pin[lc], L.dpin[lc], L.x[lc], L.x2[lc], L.b[lc],
-                  csweeps, om);
+                  csweeps, om, inv, inv_ok);
   for (int l = lc - 1; l >= l0; --l) {
     const int n = L.Nz[l] * L.Nx[l];
     for (int t = threadIdx.x; t < n; t += blockDim.x) p_prolong_at<T>(L.Nz[l + 1], L.Nx[l + 1], L.x[l + 1], L.x[l], t);
@@ -1818,6 +2007,12 @@ struct Hier {
   T* pb[kMaxLevels];
   T* pr[kMaxLevels];
   T* kr;          // right-face coefficient of the last column (fine level)
+  // dense inverses of the coarsest velocity and pressure levels (direct
+  // coarse solves) and their validity flags dok[0], dok[1] (device)
+  T* vinv;
+  T* pinv;
+  int* dok;
+  bool vdirect, pdirect;
   T* cp;          // DM coefficient planes (fine level)
   T* scl;         // scaling vector
   T* etarho;      // eta/rho on interior cells
@@ -1892,6 +2087,10 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
     if (Nz % 2 || Nx % 2 || Nz / 2 < 4 || Nx / 2 < 4) break;
     Nz /= 2; Nx /= 2; h *= 2;
   }
+  XC_CUDA_TRY(cudaMalloc(&H.vinv, sizeof(T) * kDenseMax * kDenseMax));
+  XC_CUDA_TRY(cudaMalloc(&H.pinv, sizeof(T) * kDenseMax * kDenseMax));
+  XC_CUDA_TRY(cudaMalloc(&H.dok, sizeof(int) * 2));
+  XC_CUDA_TRY(cudaMemset(H.dok, 0, sizeof(int) * 2));
   // pressure levels
   Nz = g.Nz; Nx = g.Nx;
   int pz = (int)std::nearbyint(g.Nz / 2.0) - 2, px = (int)std::nearbyint(g.Nx / 2.0) - 2;
@@ -1937,6 +2136,7 @@ void free_hier(Hier<T>& H) {
   }
   cudaFree(H.kr); cudaFree(H.cp); cudaFree(H.scl); cudaFree(H.etarho); cudaFree(H.V); cudaFree(H.Z);
   cudaFree(H.w); cudaFree(H.t); cudaFree(H.y); cudaFree(H.rv); cudaFree(H.rp); cudaFree(H.rin);
+  cudaFree(H.vinv); cudaFree(H.pinv); cudaFree(H.dok);
   H.nv = H.np_lv = 0;
 }
 
@@ -1974,6 +2174,8 @@ struct SolveCfg {
   // slower at 1024^2 -- the small levels' sweeps are bound by instruction
   // latency on one SM, and their L1-resident loads gain nothing from it)
   bool stage_small = false;
+  // coarsest levels of at most kDenseMax unknowns solved by their inverse
+  bool direct_coarse = true;
 };
 
 // Jacobi sweeps on a coarsest level of Nz x Nx cells: a few times the grid's
@@ -2029,13 +2231,14 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
     const size_t bytes = sizeof(T) * (size_t)vel_stage_elems<T>(H.vg, l, lc);
     const int staged = cfg.stage_small && bytes <= kStageMaxBytes;
     pdl_smem(PDL_ON, vel_vcycle_small_kernel<T>, 1, coarse_threads(n), staged ? bytes : 0, s, L, kf, l, lc, cfg.nu,
-             om, coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx), staged);
+             om, coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx), staged, H.vdirect ? H.vinv : nullptr, H.dok);
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
   if (vel_coarsest(H, cfg, l)) {
     pdl(PDL_ON, vel_coarse_kernel<T>, 1, coarse_threads(n), s, g, k, vop(H, l), H.vx[l], H.vx2[l], H.vb[l],
-                                                        coarse_sweeps(cfg, g.Nz, g.Nx), om);
+                                                        coarse_sweeps(cfg, g.Nz, g.Nx), om,
+                                                        (const T*)(H.vdirect ? H.vinv : nullptr), (const int*)H.dok);
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
@@ -2094,13 +2297,14 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s, T** res) {
     const size_t bytes = sizeof(T) * (size_t)p_stage_elems<T>(H.pNz, H.pNx, l, lc);
     const int staged = cfg.stage_small && bytes <= kStageMaxBytes;
     pdl_smem(PDL_ON, p_vcycle_small_kernel<T>, 1, coarse_threads(n), staged ? bytes : 0, s, L, l, lc, cfg.nu_p, om,
-             coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]), staged);
+             coarse_sweeps(cfg, H.pNz[lc], H.pNx[lc]), staged, H.pdirect ? H.pinv : nullptr, H.dok + 1);
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
   if (p_coarsest(H, cfg, l)) {
     pdl(PDL_ON, p_coarse_kernel<T>, 1, coarse_threads(n), s, Nz, Nx, H.kx[l], H.kz[l], H.ppin[l], H.pdpin[l], H.px[l],
-                                                      H.px2[l], H.pb[l], coarse_sweeps(cfg, Nz, Nx), om);
+                                                      H.px2[l], H.pb[l], coarse_sweeps(cfg, Nz, Nx), om,
+                                                      (const T*)(H.pdirect ? H.pinv : nullptr), (const int*)(H.dok + 1));
     XC_LAUNCH_CHECK();
     return XC_OK;
   }
@@ -2280,7 +2484,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -2504,9 +2708,12 @@ int fgmres_outer(StokesWork* w, const OpConst& k, const SolveCfg& cfg, const Sol
 }
 
 // build the operator coefficients and both multigrid hierarchies for one solve
+// (mg = false: the fine-level operator only -- the FP64 hierarchy of a mixed
+// solve, whose multigrid is not used)
 template <typename T>
-int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, xc_ctx* c, cudaStream_t s) {
-  for (int l = 0; l < H.nv; ++l) {
+int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, xc_ctx* c, cudaStream_t s,
+               bool mg = true) {
+  for (int l = 0; l < (mg ? H.nv : 1); ++l) {
     const Geo& lg = H.vg[l];
     const double* eta = l ? w->eta[l] : (const double*)c->field[FLD_eta];
     const double* etaco = l ? w->etaco[l] : (const double*)c->field[FLD_etaco];
@@ -2538,6 +2745,7 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
     convert_kernel<double, T><<<nblk((long long)g.Nz * g.Nx), 256, 0, s>>>((long long)g.Nz * g.Nx, w->d.etarho,
                                                                           H.etarho); xc_count_launch();
   }
+  if (!mg) return XC_OK;
   // pressure hierarchy
   p_kcoef_kernel<T><<<nblk((long long)(g.Nz + 1) * g.Nx), 256, 0, s>>>(
       g, (const double*)c->field[FLD_rhow], (const double*)c->field[FLD_rhou], w->d.cw[0], w->d.cu[0], cfg.kplane,
@@ -2551,6 +2759,22 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
     H.pdpin[l] = H.pdpin[l - 1] / (T)4;
     XC_LAUNCH_CHECK();
   }
+  // inverses of small coarsest levels
+  int lv = 0, lp = 0;
+  while (!vel_coarsest(H, cfg, lv)) ++lv;
+  while (!p_coarsest(H, cfg, lp)) ++lp;
+  H.vdirect = cfg.direct_coarse && (long long)H.vg[lv].NW + H.vg[lv].NU <= kDenseMax;
+  H.pdirect = cfg.direct_coarse && (long long)H.pNz[lp] * H.pNx[lp] <= kDenseMax;
+  if (H.vdirect) {
+    vel_dense_inv_kernel<T><<<1, 1024, 0, s>>>(H.vg[lv], level_const(k, lv), vop(H, lv), H.vinv, H.dok);
+    xc_count_launch();
+  }
+  if (H.pdirect) {
+    p_dense_inv_kernel<T><<<1, 1024, 0, s>>>(H.pNz[lp], H.pNx[lp], H.kx[lp], H.kz[lp], H.ppin[lp], H.pdpin[lp],
+                                             H.pinv, H.dok + 1);
+    xc_count_launch();
+  }
+  XC_LAUNCH_CHECK();
   return XC_OK;
 }
 
@@ -2739,6 +2963,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   cfg.pdl = !o.serial_launch;
   cfg.tiled = o.tiled_sweep != 0;
   cfg.stage_small = o.stage_small_levels != 0;
+  cfg.direct_coarse = !o.jacobi_coarse;
   if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;
   g_xc_pdl = cfg.pdl;
   // the FP32 inner solve only has to reduce its residual by inner_rtol (1e-2
@@ -2748,7 +2973,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   icfg.gs_passes = o.inner_gs_passes >= 2 ? 2 : 1;
   w->last_k = k;
   w->have_k = true;
-  XC_TRY(setup_hier<double>(w, w->d, k, cfg, c, s));
+  XC_TRY(setup_hier<double>(w, w->d, k, cfg, c, s, o.kind != XC_SOLVER_MIXED));
   scl_kernel<<<nblk(n), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], CF(c, FLD_rho), CF(c, FLD_eta), w->d.scl,
                                      w->d.etarho); xc_count_launch();
   XC_LAUNCH_CHECK();
