@@ -90,7 +90,8 @@ typedef struct xc_solver_opts {
   double inner_rtol; /* mixed: relative reduction per FP32 inner solve */
   int inner_maxit;   /* mixed: FP32 FGMRES iterations per refinement pass */
   /* preconditioner knobs (0 selects the default) */
-  int smooth_sweeps;       /* Jacobi sweeps before and after each coarse correction (2; 4 for MMS) */
+  int smooth_sweeps;       /* velocity Jacobi sweeps before each coarse correction, and after it
+                              unless post_sweeps is given (default 1 before, 2 after; 4 and 4 for MMS) */
   double omega_velocity;   /* damping of the velocity Jacobi smoother (0.7) */
   double schur_mass;       /* weight c of the c*eta/rho term added to the Schur inverse (0.5) */
   int schur_full_diagonal; /* 1: pressure Laplacian from the full velocity diagonal, no mass term */
@@ -108,7 +109,7 @@ typedef struct xc_solver_opts {
                                 cells: 0 arithmetic (default), 1 geometric, 2 harmonic */
   int tiled_sweep;         /* 1: FP32 velocity sweeps from shared-memory tiles instead of per-row
                               reads (same results; measured 5% slower at 1024^2) */
-  int post_sweeps;         /* velocity post-smoothing sweeps on the large levels (smooth_sweeps) */
+  int post_sweeps;         /* velocity post-smoothing sweeps on the large levels (2) */
   int outer_solver;        /* mixed: 2 plain iterative refinement x += S dy per inner solve (default),
                               1 FP64 FGMRES whose preconditioner is the FP32 inner solve (measured
                               4% slower at 1024^2: the inner solves' corrections are nearly

@@ -2150,8 +2150,8 @@ VOp<T> vop(const Hier<T>& H, int l) {
 
 struct SolveCfg {
   double omega_v = 0.7, omega_p = 0.8;
-  int nu = 2;
-  int nu_post = 0;         // velocity post-smoothing sweeps (0: nu)
+  int nu = 1;              // velocity pre-smoothing sweeps (and both on the one-CTA levels)
+  int nu_post = 2;         // velocity post-smoothing sweeps on the large levels
   int coarse_sweeps = 0;   // 0: 4 * (Nz + Nx) of the coarsest level, at least 32
   int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
                            // solved by Jacobi sweeps
@@ -2261,7 +2261,7 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   pdl(PDL_ON, vel_prolong2d_kernel<T>, grid2(g), blk2(), s, g, c, k, H.vx[l + 1], H.vx[l]);
   a = H.vx[l];
   o = H.vx2[l];
-  const int npost = cfg.nu_post > 0 ? cfg.nu_post : cfg.nu;
+  const int npost = cfg.nu_post;
   for (int q = 0; q < npost; ++q) {
     if (final_out && q == npost - 1) {   // last sweep of the fine level straight into the scaled output
       launch_sweep<T, 3>(cfg, g, k, op, a, H.vb[l], final_out, om, final_scl, s);
@@ -2950,8 +2950,8 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   // Jacobi smooths the grad-div coupled viscous rows poorly: four sweeps per
   // level and long Jacobi runs on a 16x16 coarsest level converge in about a
   // third of the iterations of the defaults there.
-  if (mms) { cfg.nu = 4; cfg.coarse_cells = 256; cfg.coarse_sweeps = 200; }
-  if (o.smooth_sweeps > 0) cfg.nu = o.smooth_sweeps;
+  if (mms) { cfg.nu = 4; cfg.nu_post = 4; cfg.coarse_cells = 256; cfg.coarse_sweeps = 200; }
+  if (o.smooth_sweeps > 0) cfg.nu = cfg.nu_post = o.smooth_sweeps;
   if (o.post_sweeps > 0) cfg.nu_post = o.post_sweeps;
   if (o.omega_velocity > 0) cfg.omega_v = o.omega_velocity;
   if (o.schur_full_diagonal) { cfg.kplane = 0; cfg.cmass = 0.0; }
