@@ -906,70 +906,77 @@ __device__ __forceinline__ double cta_max(double v, double* red) {
 // ---- direct solve of a small coarsest level -------------------------------
 // A coarsest level of at most kDenseMax unknowns is solved with its inverse:
 // the dense matrix is formed once per solve by applying the level's rows to
-// unit vectors (kDenseBatch at a time), inverted in FP64 by Gauss-Jordan
-// elimination with partial pivoting, and each V-cycle's coarse solve becomes
-// one matrix-vector product by one CTA instead of tens of CTA-wide Jacobi
-// sweeps.  ok = 0 (the sweeps are used instead) on a pivot below 1e-12 of the
-// largest entry, or where the velocity level has the unlifted uniform-U mode.
+// unit vectors (kDenseBatch at a time), inverted by Gauss-Jordan elimination
+// with partial pivoting in the hierarchy's precision, and each V-cycle's
+// coarse solve becomes one matrix-vector product by one CTA instead of tens of
+// CTA-wide Jacobi sweeps.  ok = 0 (the sweeps are used instead) on a pivot
+// below 1e-6 (FP32) or 1e-12 (FP64) of the largest entry, or where the
+// velocity level has the unlifted uniform-U mode.
 constexpr int kDenseMax = 64;
 constexpr int kDenseBatch = 16;
 
-// in-place inverse of the n x n row-major FP64 matrix M in shared memory
-__device__ void gj_invert_cta(double* M, int n, int* piv, int* ok, double* fcol, double* red, int* sprow) {
+// In-place inverse of the n x n row-major matrix M in shared memory, in the
+// working precision R of the hierarchy (the coarse matrix is far from
+// singular wherever ok stays 1; the FP64 pipe would make an FP64 inversion of
+// the FP32 hierarchy's matrix several times slower).  Per column k, warp 0
+// finds the pivot, swaps it into row k, scales that row and saves column k;
+// then every thread eliminates: two CTA barriers per column.
+template <typename R>
+__device__ void gj_invert_cta(R* M, int n, int* piv, int* ok, R* fcol, double* red) {
   double amax = 0;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) amax = fmax(amax, fabs(M[e]));
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) amax = fmax(amax, (double)fabs(M[e]));
   amax = cta_max(amax, red);
+  const double thr = (std::is_same<R, float>::value ? 1e-6 : 1e-12) * amax;
   for (int k = 0; k < n; ++k) {
     if (threadIdx.x < 32) {
-      double best = -1.0;
+      const int lane = threadIdx.x;
+      R best = (R)-1;
       int bi = k;
-      for (int i = k + (int)threadIdx.x; i < n; i += 32) {
-        const double v = fabs(M[i * n + k]);
+      for (int i = k + lane; i < n; i += 32) {
+        const R v = fabs(M[i * n + k]);
         if (v > best) { best = v; bi = i; }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const R ob = __shfl_xor_sync(0xffffffffu, best, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
       }
-      if (threadIdx.x == 0) {
-        *sprow = bi;
+      if (lane == 0) {
         piv[k] = bi;
-        if (!(best > 1e-12 * amax)) *ok = 0;
+        if (!((double)best > thr)) *ok = 0;
       }
+      if (bi != k)
+        for (int c = lane; c < n; c += 32) {
+          const R t = M[k * n + c];
+          M[k * n + c] = M[bi * n + c];
+          M[bi * n + c] = t;
+        }
+      __syncwarp();
+      const R pv = M[k * n + k];
+      __syncwarp();
+      // row k scaled, its pivot entry becoming 1 / pv; column k of the others saved
+      for (int c = lane; c < n; c += 32) M[k * n + c] = (c == k ? (R)1 : M[k * n + c]) / pv;
+      for (int i = lane; i < n; i += 32) fcol[i] = M[i * n + k];
     }
-    __syncthreads();
-    const int p = *sprow;
-    if (p != k)
-      for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        const double t = M[k * n + c];
-        M[k * n + c] = M[p * n + c];
-        M[p * n + c] = t;
-      }
-    __syncthreads();
-    const double pv = M[k * n + k];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = M[i * n + k];
-    __syncthreads();
-    // row k scaled; its pivot entry becomes 1 / pv
-    for (int c = threadIdx.x; c < n; c += blockDim.x) M[k * n + c] = (c == k ? 1.0 : M[k * n + c]) / pv;
     __syncthreads();
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       const int i = e / n, c = e - i * n;
-      if (i != k) M[e] = (c == k ? 0.0 : M[e]) - fcol[i] * M[k * n + c];
+      if (i != k) M[e] = (c == k ? (R)0 : M[e]) - fcol[i] * M[k * n + c];
     }
     __syncthreads();
   }
-  // A^-1 = (P A)^-1 P: the row interchanges undone as column interchanges, last first
-  for (int k = n - 1; k >= 0; --k) {
-    const int p = piv[k];
-    if (p != k)
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double t = M[i * n + k];
+  // A^-1 = (P A)^-1 P: the row interchanges undone as column interchanges,
+  // last first, each thread on its own rows
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = piv[k];
+      if (p != k) {
+        const R t = M[i * n + k];
         M[i * n + k] = M[i * n + p];
         M[i * n + p] = t;
       }
-    __syncthreads();
-  }
+    }
+  __syncthreads();
 }
 
 // x = inv b by one CTA (a warp per row); ends with a barrier
@@ -1041,14 +1048,14 @@ __global__ void vel_coarse_kernel(Geo g, OpConst k, VOp<T> op, T* x, T* x2, cons
 
 // the inverse of the coarsest velocity level (NW + NU <= kDenseMax), one CTA
 template <typename T>
-__global__ void __launch_bounds__(1024) vel_dense_inv_kernel(Geo g, OpConst k, VOp<T> op, T* inv, int* ok) {
+__global__ void __launch_bounds__(256) vel_dense_inv_kernel(Geo g, OpConst k, VOp<T> op, T* inv, int* ok) {
   XC_PDL_WAIT();
-  __shared__ double M[kDenseMax * kDenseMax];
+  __shared__ T M[kDenseMax * kDenseMax];
   __shared__ T xb[kDenseBatch][kDenseMax];
-  __shared__ double fcol[kDenseMax];
+  __shared__ T fcol[kDenseMax];
   __shared__ double red[32];
   __shared__ int piv[kDenseMax];
-  __shared__ int sprow, sok;
+  __shared__ int sok;
   const int n = g.NW + g.NU;
   if (threadIdx.x == 0) sok = 1;
   for (int c0 = 0; c0 < n; c0 += kDenseBatch) {
@@ -1068,7 +1075,7 @@ __global__ void __launch_bounds__(1024) vel_dense_inv_kernel(Geo g, OpConst k, V
         const int u = r - g.NW;
         v = vel_row_u<T, false>(g, k, op, xv, xv + g.NW, nullptr, u, u % (g.Nz + 2), u / (g.Nz + 2), &d);
       }
-      M[r * n + c] = (double)v;
+      M[r * n + c] = v;
     }
     __syncthreads();
   }
@@ -1086,8 +1093,8 @@ __global__ void __launch_bounds__(1024) vel_dense_inv_kernel(Geo g, OpConst k, V
     if (threadIdx.x == 0 && si <= 1e-6 * sd) sok = 0;
   }
   __syncthreads();
-  gj_invert_cta(M, n, piv, &sok, fcol, red, &sprow);
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = (T)M[e];
+  gj_invert_cta<T>(M, n, piv, &sok, fcol, red);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = M[e];
   if (threadIdx.x == 0) *ok = sok;
 }
 
@@ -1311,15 +1318,15 @@ __global__ void p_coarse_kernel(int Nz, int Nx, const T* __restrict__ kx, const 
 
 // the inverse of the coarsest pressure level (Nz Nx <= kDenseMax), one CTA
 template <typename T>
-__global__ void __launch_bounds__(1024) p_dense_inv_kernel(int Nz, int Nx, const T* __restrict__ kx,
+__global__ void __launch_bounds__(256) p_dense_inv_kernel(int Nz, int Nx, const T* __restrict__ kx,
                                                            const T* __restrict__ kz, int pin, T dpin, T* inv, int* ok) {
   XC_PDL_WAIT();
-  __shared__ double M[kDenseMax * kDenseMax];
+  __shared__ T M[kDenseMax * kDenseMax];
   __shared__ T xb[kDenseBatch][kDenseMax];
-  __shared__ double fcol[kDenseMax];
+  __shared__ T fcol[kDenseMax];
   __shared__ double red[32];
   __shared__ int piv[kDenseMax];
-  __shared__ int sprow, sok;
+  __shared__ int sok;
   const int n = Nz * Nx;
   if (threadIdx.x == 0) sok = 1;
   for (int c0 = 0; c0 < n; c0 += kDenseBatch) {
@@ -1332,12 +1339,12 @@ __global__ void __launch_bounds__(1024) p_dense_inv_kernel(int Nz, int Nx, const
       const int bq = e / n, r = e - bq * n, c = c0 + bq;
       if (c >= n) continue;
       T d;
-      M[r * n + c] = (double)p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xb[bq], r % Nz, r / Nz, &d);
+      M[r * n + c] = p_apply_at<T>(Nz, Nx, kx, kz, pin, dpin, xb[bq], r % Nz, r / Nz, &d);
     }
     __syncthreads();
   }
-  gj_invert_cta(M, n, piv, &sok, fcol, red, &sprow);
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = (T)M[e];
+  gj_invert_cta<T>(M, n, piv, &sok, fcol, red);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = M[e];
   if (threadIdx.x == 0) *ok = sok;
 }
 
@@ -2766,11 +2773,11 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
   H.vdirect = cfg.direct_coarse && (long long)H.vg[lv].NW + H.vg[lv].NU <= kDenseMax;
   H.pdirect = cfg.direct_coarse && (long long)H.pNz[lp] * H.pNx[lp] <= kDenseMax;
   if (H.vdirect) {
-    vel_dense_inv_kernel<T><<<1, 1024, 0, s>>>(H.vg[lv], level_const(k, lv), vop(H, lv), H.vinv, H.dok);
+    vel_dense_inv_kernel<T><<<1, 256, 0, s>>>(H.vg[lv], level_const(k, lv), vop(H, lv), H.vinv, H.dok);
     xc_count_launch();
   }
   if (H.pdirect) {
-    p_dense_inv_kernel<T><<<1, 1024, 0, s>>>(H.pNz[lp], H.pNx[lp], H.kx[lp], H.kz[lp], H.ppin[lp], H.pdpin[lp],
+    p_dense_inv_kernel<T><<<1, 256, 0, s>>>(H.pNz[lp], H.pNx[lp], H.kx[lp], H.kz[lp], H.ppin[lp], H.pdpin[lp],
                                              H.pinv, H.dok + 1);
     xc_count_launch();
   }
