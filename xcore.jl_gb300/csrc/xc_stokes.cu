@@ -69,11 +69,14 @@ constexpr int kMaxRestart = 64;
 struct Geo {          // one grid level
   int Nz, Nx, NW, NU, NP;
   double h, invh;
+  float invhf, ih2f;  // FP32 1/h and 1/h^2, rounded once here: FP32 kernels do no FP64 arithmetic
 };
 
 Geo make_geo(int Nz, int Nx, double h) {
   Geo g;
   g.Nz = Nz; g.Nx = Nx; g.h = h; g.invh = 1.0 / h;
+  g.invhf = (float)g.invh;
+  g.ih2f = (float)(g.invh * g.invh);
   g.NW = (Nz + 1) * (Nx + 2);
   g.NU = (Nz + 2) * (Nx + 1);
   g.NP = (Nz + 2) * (Nx + 2);
@@ -205,6 +208,17 @@ struct VOp {
 };
 template <typename T>
 constexpr bool kFly = std::is_same<T, float>::value;
+// 1/h and 1/h^2 of a level in T (the same values as converting the FP64 ones)
+template <typename T>
+__host__ __device__ __forceinline__ T geo_invh(const Geo& g) {
+  if constexpr (kFly<T>) return g.invhf;
+  else return g.invh;
+}
+template <typename T>
+__host__ __device__ __forceinline__ T geo_ih2(const Geo& g) {
+  if constexpr (kFly<T>) return g.ih2f;
+  else return g.invh * g.invh;
+}
 
 // smoother update r / d: the FP32 preconditioner takes the fast approximate
 // division (2 ulp; d is a positive diagonal far inside its range), FP64 the
@@ -303,7 +317,7 @@ __device__ __forceinline__ RowW<T> w_row(const Geo& g, const VOp<T>& op, long lo
     const int Nz = g.Nz;
     const T* pc = op.etaco + ((i - 1) * (Nz + 1) + j);    // corners (j, i-1), (j, i)
     const T* pe = op.eta + ((i - 1) * Nz + j - 1);        // cells (j-1, i-1), (j, i-1)
-    return fly_row<T>(pc[0], pc[Nz + 1], pe[0], pe[1], op.dw[t], (T)(g.invh * g.invh));
+    return fly_row<T>(pc[0], pc[Nz + 1], pe[0], pe[1], op.dw[t], geo_ih2<T>(g));
   } else {
     return plane_row<T>(op.cw, (size_t)g.NW, t);
   }
@@ -315,7 +329,7 @@ __device__ __forceinline__ RowW<T> u_row(const Geo& g, const VOp<T>& op, long lo
     const int ia = (i == 0) ? Nx - 1 : i - 1, ib = (i == Nx) ? 0 : i;
     const T* pc = op.etaco + (i * (Nz + 1) + j - 1);      // corners (j-1, i), (j, i)
     return fly_row<T>(pc[0], pc[1], op.eta[ia * Nz + j - 1], op.eta[ib * Nz + j - 1], op.du[u],
-                      (T)(g.invh * g.invh));
+                      geo_ih2<T>(g));
   } else {
     return plane_row<T>(op.cu, (size_t)g.NU, u);
   }
@@ -364,7 +378,7 @@ __device__ __forceinline__ T vel_row_w(const Geo& g, const OpConst& k, const VOp
   s += c.c8 * pu[lu + 1];
   if (FULL) {
     const T* pp = xp + (i * lu + j);
-    s += (T)g.invh * (pp[1] - pp[0]);
+    s += geo_invh<T>(g) * (pp[1] - pp[0]);
   }
   return s;
 }
@@ -391,7 +405,7 @@ __device__ __forceinline__ T vel_row_u(const Geo& g, const OpConst& k, const VOp
   s += c.c8 * pw[lw + 1];
   if (FULL) {
     const T* pp = xp + (i * lu + j);
-    s += (T)g.invh * (pp[lu] - pp[0]);
+    s += geo_invh<T>(g) * (pp[lu] - pp[0]);
   }
   return s;
 }
@@ -644,7 +658,7 @@ __global__ void __launch_bounds__(kTJ * kTI) vel_sweep_tiled_kernel(Geo g, OpCon
     sC[ii][jj] = (gj >= 0 && gj <= Nz) ? op.etaco[gi * (Nz + 1) + gj] : 0.f;
   }
   __syncthreads();
-  const float ih2 = (float)(g.invh * g.invh);
+  const float ih2 = g.ih2f;
   const int a = ty + 1, c = tx + 1;    // this thread's (i, j) in the tiles
   if (j <= Nz) {                       // W row (j, i), 1 <= i <= Nx here
     const long long t = (long long)i * lw + j;
@@ -1704,10 +1718,10 @@ __global__ void sub_grad_kernel(Geo g, const T* __restrict__ zp, const T* __rest
   T r = v[t] / scl[t];
   if (t < g.NW) {
     const int j = t % lw, i = t / lw;
-    if (j >= 1 && j <= Nz - 1 && i >= 1 && i <= Nx) r -= (T)g.invh * (zp[i * lu + j + 1] - zp[i * lu + j]);
+    if (j >= 1 && j <= Nz - 1 && i >= 1 && i <= Nx) r -= geo_invh<T>(g) * (zp[i * lu + j + 1] - zp[i * lu + j]);
   } else {
     const int u = t - g.NW, j = u % lu, i = u / lu;
-    if (j >= 1 && j <= Nz) r -= (T)g.invh * (zp[(i + 1) * lu + j] - zp[i * lu + j]);
+    if (j >= 1 && j <= Nz) r -= geo_invh<T>(g) * (zp[(i + 1) * lu + j] - zp[i * lu + j]);
   }
   rv[t] = r;
 }
