@@ -100,7 +100,10 @@ extern "C" int xc_ctx_create(const xc_params* par, xc_ctx** out) {
   c->Nx = par->Nx;
   cudaGetDevice(&c->device);
   auto fail = [&](int st) { xc_ctx_destroy(c); return st; };
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     xc_set_error("xc_ctx_create: stream creation failed");
     return fail(XC_CUDA);
   }
@@ -125,6 +128,7 @@ extern "C" int xc_ctx_create(const xc_params* par, xc_ctx** out) {
   for (int k = 0; k < 8; ++k) c->tmp[k] = (double*)(c->arena + tmp_off + k * tmpn);
   c->red_partials_len = reduce_partials_len();
   if (cudaMalloc(&c->red_partials, sizeof(double) * c->red_partials_len) != cudaSuccess ||
+      cudaMalloc(&c->red_partials_side, sizeof(double) * c->red_partials_len) != cudaSuccess ||
       cudaMalloc(&c->dscal, sizeof(double) * 64) != cudaSuccess ||
       cudaMallocHost(&c->hscal, sizeof(double) * 64) != cudaSuccess) {
     xc_set_error("xc_ctx_create: scratch allocation failed");
@@ -146,13 +150,18 @@ extern "C" int xc_ctx_create(const xc_params* par, xc_ctx** out) {
 extern "C" int xc_ctx_destroy(xc_ctx* c) {
   if (!c) return XC_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->side) cudaStreamSynchronize(c->side);
   noise_plan_destroy(c);
   stokes_destroy(c);
   if (c->arena) cudaFree(c->arena);
   if (c->red_partials) cudaFree(c->red_partials);
+  if (c->red_partials_side) cudaFree(c->red_partials_side);
   if (c->dscal) cudaFree(c->dscal);
   if (c->hscal) cudaFreeHost(c->hscal);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   delete c;
   return XC_OK;
 }
@@ -334,16 +343,33 @@ extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double*
   XC_TRY(store_noise_impl(c));
   xc_step_stats local;
   std::memset(&local, 0, sizeof(local));
+  // the main stream waits for the side stream's noise! before it goes on
+  auto join = [&]() -> int {
+    XC_CUDA_TRY(cudaEventRecord(c->ev_join, c->side));
+    XC_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    return XC_OK;
+  };
   for (int it = 1; it <= sweeps; ++it) {
     XC_TRY(snapshot_impl(c));
-    XC_TRY(phsevo_impl(c, c->p.ADVN, coefs, dt, c->p.alpha));
+    // noise! (run.jl:240) reads only what the previous update! (or the
+    // initial state) left -- V, vx, fReL, ke, ks, chi, the face fractions and
+    // the stored noise -- none of which phsevo! or fluidmech! write, and
+    // neither of them reads its results: it runs on the side stream while
+    // they run, and update_phase_velocities! waits for it
+    XC_CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
+    XC_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    int nst = noise_impl(c, dt, it == 1, it == 1 ? re : nullptr, it == 1 ? rs : nullptr, c->side,
+                         c->red_partials_side);
+    if (nst != XC_OK) { join(); return nst; }
+    int st = phsevo_impl(c, c->p.ADVN, coefs, dt, c->p.alpha);
+    if (st != XC_OK) { join(); return st; }
     xc_solver_stats ss;
     std::memset(&ss, 0, sizeof(ss));
-    int st = fluidmech_impl(c, coefs, dt, opts, &ss, nullptr);
+    st = fluidmech_impl(c, coefs, dt, opts, &ss, nullptr);
+    XC_TRY(join());
     if (st != XC_OK && st != XC_NOT_CONVERGED) return st;
     local.solver_iterations += ss.iterations;
     if (ss.rel_residual > local.solver_rel_residual) local.solver_rel_residual = ss.rel_residual;
-    XC_TRY(noise_impl(c, dt, it == 1, it == 1 ? re : nullptr, it == 1 ? rs : nullptr));
     XC_TRY(phase_velocities_impl(c));
     XC_TRY(update_impl(c));
     double rn[3];

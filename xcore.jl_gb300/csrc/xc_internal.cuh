@@ -139,6 +139,12 @@ struct xc_ctx {
   int Nz, Nx;
   int device;
   cudaStream_t stream;
+  // noise! of a Picard sweep runs on `side` while phsevo! and fluidmech! run
+  // on `stream` (it reads only fields of the previous update!); ev_fork /
+  // ev_join order it, red_partials_side is its reduction scratch
+  cudaStream_t side;
+  cudaEvent_t ev_fork, ev_join;
+  double* red_partials_side;
   char* arena;
   size_t arena_bytes;
   void* field[FLD_COUNT];
@@ -185,7 +191,7 @@ enum RedOp : int { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2, RED_SUMSQ = 3, RED_MAX
 int reduce_view(xc_ctx* c, int op, CView a, CView b, int rows, int cols, int slot);
 // general form: optional center (sum of (a - *center)^2), result / divisor into *out
 int reduce_to(xc_ctx* c, int op, CView a, CView b, const double* center, int rows, int cols,
-              double* out, cudaStream_t s, double divisor = 1.0);
+              double* out, cudaStream_t s, double divisor = 1.0, double* partials = nullptr);
 int reduce_partials_len();
 // copy device scalars [first, first+n) to the pinned host mirror and wait
 int fetch_scalars(xc_ctx* c, int first, int n);
@@ -215,7 +221,9 @@ int history_impl(xc_ctx* c, double out[58]);
 
 int noise_plan_create(xc_ctx* c);
 void noise_plan_destroy(xc_ctx* c);
-int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const double* rs);
+// on stream s (c->stream when null) with reduction scratch partials (c->red_partials when null)
+int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const double* rs,
+               cudaStream_t s = nullptr, double* partials = nullptr);
 
 int stokes_create(xc_ctx* c);
 void stokes_destroy(xc_ctx* c);

@@ -356,10 +356,11 @@ void noise_plan_destroy(xc_ctx* c) {
   c->noise = nullptr;
 }
 
-int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const double* rs) {
+int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const double* rs, cudaStream_t s_in,
+               double* partials) {
   const int Nz = c->Nz, Nx = c->Nx;
   const xc_params& p = c->p;
-  cudaStream_t s = c->stream;
+  cudaStream_t s = s_in ? s_in : c->stream;
   NoisePlan* np = c->noise;
   const size_t nb = sizeof(double) * (size_t)Nz * Nx;
   if (first_iter) {
@@ -385,10 +386,10 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
     XC_TRY(run_line_filter(*zf[q], CF(c, src[q]), mid, Nz, Nx, 0, s));
     XC_TRY(run_line_filter(*xf[q], CView{mid.p, Nz}, flt[q], Nz, Nx, 1, s));
     CView raw = CF(c, src[q]), fv{flt[q].p, Nz};
-    XC_TRY(reduce_to(c, RED_SUM, raw, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 0, s, n));
-    XC_TRY(reduce_to(c, RED_SUM, raw, CView{nullptr, 0}, st + 4 * q + 0, Nz, Nx, st + 4 * q + 1, s));
-    XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 2, s, n));
-    XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, st + 4 * q + 2, Nz, Nx, st + 4 * q + 3, s));
+    XC_TRY(reduce_to(c, RED_SUM, raw, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 0, s, n, partials));
+    XC_TRY(reduce_to(c, RED_SUM, raw, CView{nullptr, 0}, st + 4 * q + 0, Nz, Nx, st + 4 * q + 1, s, 1.0, partials));
+    XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 2, s, n, partials));
+    XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, st + 4 * q + 2, Nz, Nx, st + 4 * q + 3, s, 1.0, partials));
   }
   rescale_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(Nz, Nx, flt[0], flt[1], flt[2], st); xc_count_launch();
   XC_LAUNCH_CHECK();

@@ -76,12 +76,13 @@ __global__ void __launch_bounds__(RB) final_kernel(int op, const double* partial
 }  // namespace
 
 int reduce_to(xc_ctx* c, int op, CView a, CView b, const double* center, int rows, int cols,
-              double* out, cudaStream_t s, double divisor) {
+              double* out, cudaStream_t s, double divisor, double* partials) {
+  double* part = partials ? partials : c->red_partials;
   int combine_op = (op == RED_SUMSQ || op == RED_SUMSQDIFF || op == RED_SUMLOG) ? RED_SUM : op;
   if (center) combine_op = RED_SUM;
-  partial_kernel<<<RG, RB, 0, s>>>(op, a, b, center, rows, cols, c->red_partials); xc_count_launch();
+  partial_kernel<<<RG, RB, 0, s>>>(op, a, b, center, rows, cols, part); xc_count_launch();
   XC_LAUNCH_CHECK();
-  final_kernel<<<1, RB, 0, s>>>(combine_op, c->red_partials, RG, out, divisor); xc_count_launch();
+  final_kernel<<<1, RB, 0, s>>>(combine_op, part, RG, out, divisor); xc_count_launch();
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
