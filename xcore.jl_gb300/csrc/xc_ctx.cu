@@ -351,18 +351,18 @@ extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double*
   };
   for (int it = 1; it <= sweeps; ++it) {
     XC_TRY(snapshot_impl(c));
+    int st = phsevo_impl(c, c->p.ADVN, coefs, dt, c->p.alpha);
+    if (st != XC_OK) return st;
     // noise! (run.jl:240) reads only what the previous update! (or the
     // initial state) left -- V, vx, fReL, ke, ks, chi, the face fractions and
     // the stored noise -- none of which phsevo! or fluidmech! write, and
-    // neither of them reads its results: it runs on the side stream while
-    // they run, and update_phase_velocities! waits for it
+    // neither of them reads its results: it runs on the side stream beside
+    // the latency-bound Stokes solve, and update_phase_velocities! waits for it
     XC_CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
     XC_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
     int nst = noise_impl(c, dt, it == 1, it == 1 ? re : nullptr, it == 1 ? rs : nullptr, c->side,
                          c->red_partials_side);
     if (nst != XC_OK) { join(); return nst; }
-    int st = phsevo_impl(c, c->p.ADVN, coefs, dt, c->p.alpha);
-    if (st != XC_OK) { join(); return st; }
     xc_solver_stats ss;
     std::memset(&ss, 0, sizeof(ss));
     st = fluidmech_impl(c, coefs, dt, opts, &ss, nullptr);
