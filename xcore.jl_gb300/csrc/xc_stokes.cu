@@ -2597,30 +2597,38 @@ constexpr int FG_TRUST_EST = 2;
 // initial guess in H.y (updated in place).  *its_out = iterations used,
 // *relres_out = ||rhs - A y|| / ||rhs|| of the true residual at the last restart
 // (the estimate under FG_TRUST_EST).
+// rhs_norm2 >= 0 (with FG_ZERO_GUESS): ||rhs||^2 is known on the host and its
+// reciprocal root already sits in hdev[6] (the FP64 norm of the residual the
+// FP32 rhs was rounded from), so no reduction or synchronisation is needed
 template <typename T>
 int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* rhs, double rtol,
-           int maxit, int* its_out, double* relres_out, cudaStream_t s, int flags = 0) {
+           int maxit, int* its_out, double* relres_out, cudaStream_t s, int flags = 0, double rhs_norm2 = -1.0) {
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   const int m = H.m;
   double* hh = w->hhost;
   const bool zero = (flags & FG_ZERO_GUESS) != 0;
-  XC_TRY(dot_self<T>(w, H, rhs, n, 0, s));
+  const bool known = zero && rhs_norm2 >= 0.0;
+  if (!known) XC_TRY(dot_self<T>(w, H, rhs, n, 0, s));
   if (zero) {
     XC_CUDA_TRY(cudaMemsetAsync(H.y, 0, sizeof(T) * n, s));
-    // V[0] = rhs / ||rhs|| with the reciprocal dot_self left on the device
+    // V[0] = rhs / ||rhs|| with the reciprocal left on the device
     scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, rhs, H.V); xc_count_launch();
   }
-  XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
-  XC_CUDA_TRY(cudaStreamSynchronize(s));
-  const double bnorm = std::sqrt(hh[0]) > 0 ? std::sqrt(hh[0]) : 1.0;
+  double rhs2 = rhs_norm2;
+  if (!known) {
+    XC_CUDA_TRY(cudaMemcpyAsync(hh, w->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    XC_CUDA_TRY(cudaStreamSynchronize(s));
+    rhs2 = hh[0];
+  }
+  const double bnorm = std::sqrt(rhs2) > 0 ? std::sqrt(rhs2) : 1.0;
   int its = 0;
   double relres = 1.0;
   HessLS ls(m);
   for (int cycle = 0;; ++cycle) {
     double beta;
     if (zero && cycle == 0) {
-      beta = std::sqrt(hh[0]);
+      beta = std::sqrt(rhs2);
       relres = beta > 0 ? 1.0 : 0.0;
       if (!(relres > rtol) || its >= maxit) break;
     } else {
@@ -3023,11 +3031,11 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     const double bn = std::sqrt(w->hhost[3]) > 0 ? std::sqrt(w->hhost[3]) : 1.0;
     // the FP64 operator reuses d.V[0] as residual storage
     double* res = w->d.V;
-    double* yd = w->d.y;
     for (int outer = 0; outer < 50; ++outer) {
-      // yd = x / scl; res = S RR - S LL S yd (FP64)
-      div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, yd); xc_count_launch();
-      XC_TRY(apply_scaled<double>(w, w->d, k, yd, w->r, res, s));
+      // res = S RR - S LL x (FP64), the operator applied to the physical x
+      pdl(PDL_ON, stokes_apply_kernel<double>, grid2(g), blk2(), s, g, k, vop(w->d, 0), w->d.cp, w->d.scl, w->x,
+          (const double*)w->r, res);
+      XC_LAUNCH_CHECK();
       XC_TRY(dot_self<double>(w, w->d, res, n, 3, s));
       XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
       XC_CUDA_TRY(cudaStreamSynchronize(s));
@@ -3043,7 +3051,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       int iits = 0;
       double irr = 1.0;
       XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
-                           FG_ZERO_GUESS | FG_TRUST_EST));
+                           FG_ZERO_GUESS | FG_TRUST_EST, w->hhost[3]));
       its += iits;
       refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
       XC_LAUNCH_CHECK();
