@@ -234,25 +234,39 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident: the step's draws already on the device -------------------
+    # Both timed loops below run the same K steps of the same trajectory: the
+    # state is saved here and restored before the end-to-end loop, and both use
+    # draws k, k+1, ... -- same work, same iteration counts, same bits.
+    snap = st.checkpoint()
+    step0, dt0, k0 = step, dt, k
+    # ---- device-resident: each step's draws uploaded to the device before its
+    # timed interval (CUDA events on the library stream around each step) ------------
     iters, resid = 0, 0.0
+    intervals = []
     barrier()
     launches0 = xc.launch_count()
     with ClockSampler(local) as clk:
-        ev0.record(stream)
         for _ in range(a.steps):
             step += 1
+            st["re"], st["rs"] = draws[k][0], draws[k][1]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             info = st.step(step, dt, None, None, sweeps=a.sweeps, **sopt)
+            e1.record(stream)
+            intervals.append((e0, e1))
             dt = info["dt_next"]
+            k += 1
             iters += info["solver_iterations"]
             resid = max(resid, info["solver_rel_residual"])
-        ev1.record(stream)
         barrier()
     launches = xc.launch_count() - launches0
-    ms = ev0.elapsed_time(ev1) / a.steps
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in intervals) / a.steps
     # ---- end to end: host draws in, crystal fraction out, every step ------------------
+    st.restore(snap)
+    step, dt, k = step0, dt0, k0
     xout = torch.empty((N, N), dtype=torch.float64).pin_memory()
     xout_np = xout.numpy().T
+    iters_e2e = 0
     barrier()
     ev0.record(stream)
     for _ in range(a.steps):
@@ -260,22 +274,31 @@ def main():
         info = st.step(step, dt, draws[k][0], draws[k][1], sweeps=a.sweeps, **sopt)
         dt = info["dt_next"]
         k += 1
+        iters_e2e += info["solver_iterations"]
         xc.lib().xc_field_download(st._h, st._ids["x"], xout_np.ctypes.data)
     ev1.record(stream)
     barrier()
     ms_e2e = ev0.elapsed_time(ev1) / a.steps
     # ---- plain FP64 GPU drop-in on the same state -------------------------------------
+    # from the same saved state with the same draws as the two loops above
     ms_plain = None
     if a.plain_steps > 0:
+        st.restore(snap)
+        step, dt, k = step0, dt0, k0
+        intervals = []
         barrier()
-        ev0.record(stream)
         for _ in range(a.plain_steps):
             step += 1
+            st["re"], st["rs"] = draws[k][0], draws[k][1]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             info = st.step(step, dt, None, None, sweeps=a.sweeps, solver="fgmres64", rtol=a.rtol, maxit=1500)
+            e1.record(stream)
+            intervals.append((e0, e1))
             dt = info["dt_next"]
-        ev1.record(stream)
+            k += 1
         barrier()
-        ms_plain = ev0.elapsed_time(ev1) / a.plain_steps
+        ms_plain = sum(e0.elapsed_time(e1) for e0, e1 in intervals) / a.plain_steps
     # ---- roofline of the dominant kernel (CUDA events on the library stream) ----------
     rk = st.bench_kernel(a.roofline_kernel, iters=20)
     peaks = {}
@@ -328,6 +351,10 @@ def main():
             "grid": f"{N}x{N}", "sweeps": a.sweeps, "solver": a.solver, "stokes_rtol": a.rtol,
             "solver_options": {k: v for k, v in sopt.items() if k not in ("solver", "rtol")},
             "solver_iterations_per_step": iters / a.steps, "worst_solver_rel_residual": resid,
+            "e2e_solver_iterations_per_step": iters_e2e / a.steps,
+            "timing": "value: sum of the K steps' device intervals, each step's draws uploaded before it; "
+                      "e2e: one interval over the same K steps from the same saved state, draws copied in "
+                      "and the crystal fraction copied out inside it",
             "plain_fp64_ms_per_step": ms_plain_max if ms_plain else None,
             "speedup_vs_plain_fp64": (ms_plain_max / ms) if ms_plain else None,
             "learned_preconditioner": "not built",
