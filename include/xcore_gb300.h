@@ -97,7 +97,9 @@ typedef struct xc_solver_opts {
   int schur_full_diagonal; /* 1: pressure Laplacian from the full velocity diagonal, no mass term */
   int coarse_cells;        /* a velocity level of at most this many cells is the coarsest, a pressure
                               level of a quarter of it (16; 256 for MMS) */
-  int coarse_sweeps;       /* Jacobi sweeps there (4 (Nz + Nx), at least 32; 200 for MMS) */
+  int coarse_sweeps;       /* Jacobi sweeps on a coarsest level that is not solved with its dense
+                              inverse (above 64 unknowns, or jacobi_coarse): 4 (Nz + Nx), at
+                              least 32; 200 for MMS */
   int small_cells;         /* levels of at most this many cells run their V-cycle in one CTA
                               (256; -1: none) */
   int pressure_sweeps;     /* pressure-multigrid Jacobi sweeps before and after each coarse
