@@ -56,6 +56,25 @@ def test_coarse_solves_match_lu(solver, rtol, tol, jacobi):
     ds.close()
 
 
+@pytest.mark.parametrize("N", [4, 6, 8])
+@pytest.mark.parametrize("solver,rtol,tol", [("fgmres64", 1e-10, 1e-8), ("mixed", 1e-9, 1e-7)])
+def test_smallest_grids_match_lu(N, solver, rtol, tol):
+    """Grids with a single or two multigrid levels: at 4x4 the fine level is
+    the coarsest and is solved with its dense inverse (60 unknowns), at 6x6 it
+    is the coarsest with 112 unknowns (Jacobi sweeps), at 8x8 the one-CTA
+    V-cycle starts on the fine level and ends in the 4x4 inverse."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=N, Nx=N, steps=2)
+    ds = device_state(par, g, sc, st)
+    coefs = O.time_coefs("bd2im", 3)
+    O.fluidmech(st, g, par, coefs, dt)
+    info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol, maxit=2000)
+    assert info["converged"] and info["rel_residual"] <= rtol, info
+    for k in ("W", "U", "P"):
+        e = _maxrel(ds[k], getattr(st, k))
+        assert e <= tol, (k, e, info)
+    ds.close()
+
+
 @pytest.mark.parametrize("bc", [dict(sds=-1, top_cnv=-1, bot_cnv=-1), dict(sds=-1, top_cnv=-1, bot_cnv=1),
                                 dict(sds=1, top_cnv=1, bot_cnv=1)])
 def test_fluidmech_boundary_variants_match_lu(bc):
