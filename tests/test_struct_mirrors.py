@@ -110,3 +110,15 @@ def test_julia_short_solver_opts_constructor_pads_every_field():
     assert m
     args = [a.strip() for a in m.group(1).split(",")]
     assert len(args) == len(c_fields("xc_solver_opts"))
+
+
+def test_julia_solver_opts_calls_have_six_or_all_arguments():
+    """Every SolverOpts(...) call of the binding passes the 6 leading fields
+    (the short constructor) or every field of xc_solver_opts."""
+    src = re.sub(r"#.*", "", open(JULIA).read())
+    n = len(c_fields("xc_solver_opts"))
+    calls = re.findall(r"SolverOpts\(([^()]*)\)", src)
+    assert calls
+    for args in calls:
+        k = len([a for a in args.split(",") if a.strip()])
+        assert k in (6, n), (k, args)

@@ -192,7 +192,10 @@ function history_stats(ctx::Context)
 end
 
 function step!(ctx::Context, step::Integer, dt, re, rs; sweeps = 3, solver::Symbol = :mixed, rtol = 1e-9)
-    o = SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 1e-3, 40)
+    # the measured optimum of the 1024^2 time step: FP32 inner solves to a 5e-2
+    # reduction in at most 30 iterations, one pressure-multigrid sweep
+    o = SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 5e-2, 30,
+                   0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     st = Ref{NTuple{19,UInt64}}()   # xc_step_stats storage (152 bytes; dt_next is the last word)
     check(ccall((:xc_step, LIB), Cint,
                 (Ptr{Cvoid}, Cint, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts}, Ptr{Cvoid}),
