@@ -356,3 +356,106 @@ def test_resnorm_positive_after_change():
     snap = O.snapshot(st)
     st.X = st.X * 1.01
     assert O.resnorm(st, snap, sc["dt0"])[0] > 0
+
+
+def _noise_setup(N=16, seed=42):
+    """test/test_noise.jl:8-19: Parameters(D = 10, N, L = 10, etam0 = 10,
+    x0 = 0.1, Da = 0, Xi = 0.5) after initialize! (the initial draw supplied)."""
+    par = O.Params(D=10.0, N=N, L=10.0, etam0=10.0, x0=0.1, Da=0.0, Xi=0.5)
+    g = O.make_grid(par)
+    sc = O.compute_scales(par, g)
+    ns = O.NoiseStatic(g, sc)
+    rng = np.random.default_rng(seed)
+    rp = rng.standard_normal((g.Nz, g.Nx))
+    rp = (rp - rp.mean()) / rp.std(ddof=1)
+    x0 = par.x0 * (1 + par.dxr * rp)
+    st = O.initialize(g, par, sc, ns, x0, rng.standard_normal((g.Nz, g.Nx)), rng.standard_normal((g.Nz, g.Nx)))
+    return par, g, sc, ns, st, rng
+
+
+def test_store_noise_snapshots_potentials():
+    """test/test_noise.jl:44-59."""
+    par, g, sc, ns, st, rng = _noise_setup()
+    st.psie[:] = 1.0
+    st.psix[:] = 2.0
+    st.psis[:] = 3.0
+    O.store_noise(st)
+    assert np.all(st.psieo == 1.0) and np.all(st.psixo == 2.0) and np.all(st.psiso == 3.0)
+    st.psie[:] = 7.0
+    O.store_noise(st)
+    assert np.all(st.psieo == 7.0)
+
+
+def test_noise_speeds_and_fluxes_finite_over_sweeps():
+    """test/test_noise.jl:61-76: three noise! calls, the first drawing; the
+    speed magnitudes are finite and non-negative, the fluxes finite."""
+    par, g, sc, ns, st, rng = _noise_setup()
+    for it in range(3):
+        first = it == 0
+        re = rng.standard_normal((g.Nz, g.Nx)) if first else None
+        rs = rng.standard_normal((g.Nz, g.Nx)) if first else None
+        O.noise(st, g, par, sc, ns, sc["dt0"], first, re, rs)
+    for k in ("xie", "xix", "xis"):
+        v = getattr(st, k)
+        assert np.all(np.isfinite(v)) and np.all(v >= 0), k
+    for k in ("xiew", "xieu", "xixw", "xixu"):
+        assert np.all(np.isfinite(getattr(st, k))), k
+
+
+def test_noise_from_zero_potential_finite():
+    """test/test_noise.jl:94-110 (N = 24): psie = psieo = 0 and a fresh draw."""
+    par, g, sc, ns, st, rng = _noise_setup(N=24)
+    O.store_noise(st)
+    st.psie[:] = 0.0
+    st.psieo[:] = 0.0
+    O.noise(st, g, par, sc, ns, sc["dt0"], True, rng.standard_normal((g.Nz, g.Nx)),
+            rng.standard_normal((g.Nz, g.Nx)))
+    assert np.all(np.isfinite(st.xie)) and np.all(np.isfinite(st.xiew))
+
+
+def test_update_end_to_end_smoke():
+    """test/test_update.jl:96-131: update! on a smooth x perturbation with a
+    weak W seed keeps rho, etamix, eta positive and finite, eII, tII >= 0."""
+    par = O.Params(D=10.0, N=32, L=10.0, etam0=10.0, x0=0.1)
+    g = O.make_grid(par)
+    sc = O.compute_scales(par, g)
+    st = O.State(g.Nz, g.Nx)
+    j = np.arange(1, g.Nz + 1)[:, None]
+    i = np.arange(1, g.Nx + 1)[None, :]
+    zg = (j - 0.5) * g.h / g.D
+    xg = (i - 0.5) * g.h / g.L
+    st.x = 0.1 + 0.05 * np.sin(2 * math.pi * zg) * np.cos(2 * math.pi * xg)
+    st.m = 1.0 - st.x
+    st.eta[:] = par.etam0
+    st.etaco[:] = par.etam0
+    nW = st.W.shape[0]
+    st.W = np.repeat(1e-3 * np.sin(np.arange(nW) * 2 * math.pi / nW)[:, None], st.W.shape[1], axis=1)
+    O.update(st, g, par, sc)
+    for k, positive in (("rho", True), ("etamix", True), ("eta", True), ("eII", False), ("tII", False)):
+        v = getattr(st, k)
+        assert np.all(np.isfinite(v)), k
+        assert np.all(v > 0) if positive else np.all(v >= 0), k
+    assert st.chi.shape == (g.Nz, g.Nx) and st.etamix.shape == (g.Nz, g.Nx)
+    assert st.exz.shape == (g.Nz + 1, g.Nx + 1)
+
+
+def test_history_stats_ordering_and_finite():
+    """test/test_history.jl:50-73 on the initialized N = 8 state of
+    test/test_history.jl:6-16: min <= mean <= max for x, min <= rms <= max
+    (+ sqrt(eps)) for V and vx, every recorded value finite."""
+    par = O.Params(D=10.0, N=8, L=10.0, etam0=10.0, x0=0.1, Da=0.0)
+    g = O.make_grid(par)
+    sc = O.compute_scales(par, g)
+    ns = O.NoiseStatic(g, sc)
+    rng = np.random.default_rng(5)
+    rp = rng.standard_normal((g.Nz, g.Nx))
+    rp = (rp - rp.mean()) / rp.std(ddof=1)
+    st = O.initialize(g, par, sc, ns, par.x0 * (1 + par.dxr * rp), rng.standard_normal((g.Nz, g.Nx)),
+                      rng.standard_normal((g.Nz, g.Nx)))
+    h = O.history_stats(st)
+    tol = math.sqrt(np.finfo(np.float64).eps)
+    assert h["x_min"] <= h["x_mean"] <= h["x_max"]
+    assert h["V_min"] <= h["V_rms"] <= h["V_max"] + tol
+    assert h["vx_min"] <= h["vx_rms"] <= h["vx_max"] + tol
+    assert all(math.isfinite(v) for v in h.values())
+    assert all(math.isfinite(v) for v in O.conservation_sums(st, g).values())
