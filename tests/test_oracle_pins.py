@@ -459,3 +459,16 @@ def test_history_stats_ordering_and_finite():
     assert h["vx_min"] <= h["vx_rms"] <= h["vx_max"] + tol
     assert all(math.isfinite(v) for v in h.values())
     assert all(math.isfinite(v) for v in O.conservation_sums(st, g).values())
+
+
+def test_snapshot_copies_primary_fields():
+    """test/test_diagnose.jl:34-50: snapshot! copies W, U, X into its own
+    buffers; changing a field afterwards leaves the snapshot unchanged."""
+    par, g, sc, ns, st, rng = _small_run(N=8)
+    st.W[1, 1] = 42.0
+    st.U[2, 1] = -7.0
+    st.X[0, 0] = 0.3
+    snap = O.snapshot(st)
+    assert snap["W"][1, 1] == 42.0 and snap["U"][2, 1] == -7.0 and snap["X"][0, 0] == 0.3
+    st.W[1, 1] = 0.0
+    assert snap["W"][1, 1] == 42.0
