@@ -144,8 +144,18 @@ def cpu_port_step_seconds(N, sweeps=3, steps=1, seed=0):
     return times
 
 
+CPU_GRID = 128   # largest grid whose sparse-LU steps fit a few-minute run on the host
+
+
+def cpu_note(N):
+    return (f"measured at {N}^2, not at the GPU workload's grid: the port's sparse LU (SciPy SuperLU) grows "
+            f"much faster than the cell count (about 10 s per factorisation at 256^2 and 100 s at 400^2 on an "
+            f"x86 core), so a 1024^2 CPU step is not measured and no cell-count extrapolation is reported")
+
+
 def run_reference(a):
-    """--impl reference: the CPU port of the reference path on the host cores."""
+    """--impl reference: the CPU port of the reference path on the host cores,
+    real time steps of the same workload at CPU_GRID^2."""
     rank, world, _ = dist_info()
     if world > 1:
         import torch.distributed as dist
@@ -153,28 +163,54 @@ def run_reference(a):
         if rank != 0:
             dist.barrier()
             return
-    sample_N = 128
-    scale = (a.N / sample_N) ** 2
-    times = cpu_port_step_seconds(sample_N, a.sweeps, steps=a.warmup + a.steps)[a.warmup:]
-    per_step = float(np.mean(times)) * scale
+    N = CPU_GRID
+    times = cpu_port_step_seconds(N, a.sweeps, steps=a.warmup + a.steps)[a.warmup:]
+    per_step = float(np.mean(times))
     value = 1.0 / per_step
-    sample = (f"{a.steps} timed 3-sweep time steps at {sample_N}^2 (after {a.warmup} warm-up steps), "
-              f"scaled by the cell-count ratio {scale:g} to {a.N}^2 (optimistic for the CPU: its sparse LU "
-              f"grows faster than the cell count)")
+    sample = (f"{a.steps} timed {a.sweeps}-sweep time steps at {N}^2 after {a.warmup} warm-up steps, "
+              f"{per_step:.2f} s each; " + cpu_note(N))
     out = {"metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": a.gpus, "steps": a.steps,
            "warmup": a.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-           "config": {"workload": f"xcore time step {a.N}x{a.N}, {a.sweeps} Picard sweeps, WENO5, BD2, "
+           "config": {"workload": f"xcore time step {N}x{N}, {a.sweeps} Picard sweeps, WENO5, BD2, "
                                   "lognormal crystal fraction, etacntr 1e4",
-                      "grid": f"{a.N}x{a.N}", "sweeps": a.sweeps,
+                      "grid": f"{N}x{N}", "sweeps": a.sweeps,
+                      "gpu_workload_grid": f"{a.N}x{a.N} (CPU steps at that grid unmeasured)",
                       "implementation": "CPU port of the reference path: numpy stencils + SciPy SuperLU "
-                                        "(the Julia reference and UMFPACK are not installed)"},
+                                        "(the Julia reference and UMFPACK are not installed); both are "
+                                        "single-threaded, so one core does the work"},
            "cpu_baseline": {"value": value, "unit": "timesteps/s", "cores": 1, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+def gpu_steps_per_second(xc, N, sweeps, steps, sopt, seed=5):
+    """Timesteps/s of the GPU path on the same workload at N^2 (the CPU
+    baseline's grid), CUDA events on the library stream, after 3 warm-up steps."""
+    import torch
+    par = workload_params(N)
+    st = xc.State(par)
+    x0, rng = initial_fields(N, seed)
+    st.initialize(x0, rng.standard_normal((N, N)), rng.standard_normal((N, N)))
+    stream = torch.cuda.ExternalStream(st.stream_handle())
+    dt = st.scales["dt0"]
+    total = 0.0
+    for k in range(3 + steps):
+        re, rs = rng.standard_normal((N, N)), rng.standard_normal((N, N))
+        st["re"], st["rs"] = re, rs
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        info = st.step(k + 1, dt, None, None, sweeps=sweeps, **sopt)
+        e1.record(stream)
+        e1.synchronize()
+        if k >= 3:
+            total += e0.elapsed_time(e1)
+        dt = info["dt_next"]
+    st.close()
+    return 1e3 * steps / total
 
 
 def main():
@@ -282,6 +318,7 @@ def main():
     # ---- plain FP64 GPU drop-in on the same state -------------------------------------
     # from the same saved state with the same draws as the two loops above
     ms_plain = None
+    field_err = None
     if a.plain_steps > 0:
         st.restore(snap)
         step, dt, k = step0, dt0, k0
@@ -299,6 +336,18 @@ def main():
             k += 1
         barrier()
         ms_plain = sum(e0.elapsed_time(e1) for e0, e1 in intervals) / a.plain_steps
+        # the same steps with the mixed solver, untimed: per-field deviation
+        # of the mixed trajectory from the plain FP64 one
+        plain_fields = {f: st[f] for f in ("W", "U", "P", "x")}
+        st.restore(snap)
+        step, dt, k = step0, dt0, k0
+        for _ in range(a.plain_steps):
+            step += 1
+            info = st.step(step, dt, draws[k][0], draws[k][1], sweeps=a.sweeps, **sopt)
+            dt = info["dt_next"]
+            k += 1
+        field_err = {f: float(np.abs(st[f] - v).max() / max(np.abs(v).max(), 1e-300))
+                     for f, v in plain_fields.items()}
     # ---- roofline of the dominant kernel (CUDA events on the library stream) ----------
     rk = st.bench_kernel(a.roofline_kernel, iters=20)
     peaks = {}
@@ -321,13 +370,15 @@ def main():
         barrier()
         return
     cpu = None
+    gpu_at_cpu_grid = None
     if not a.no_cpu and world == 1:
-        times = cpu_port_step_seconds(256, a.sweeps, steps=1)
-        scale = (N / 256) ** 2
-        v = 1.0 / (times[0] * scale)
-        cpu = {"value": v, "unit": "timesteps/s", "cores": 1, "kind": "port",
-               "sample": f"one {a.sweeps}-sweep time step at 256^2 ({times[0]:.1f} s on this host) scaled by the "
-                         f"cell-count ratio {scale:g} to {N}^2; numpy + SciPy SuperLU, single-threaded"}
+        times = cpu_port_step_seconds(CPU_GRID, a.sweeps, steps=3)[1:]
+        v = 1.0 / float(np.mean(times))
+        cpu = {"value": v, "unit": "timesteps/s", "cores": 1, "kind": "port", "grid": f"{CPU_GRID}x{CPU_GRID}",
+               "sample": f"2 timed {a.sweeps}-sweep time steps at {CPU_GRID}^2 after one warm-up step "
+                         f"({np.mean(times):.2f} s each on this host; numpy + SciPy SuperLU, single-threaded); "
+                         + cpu_note(CPU_GRID)}
+        gpu_at_cpu_grid = gpu_steps_per_second(xc, CPU_GRID, a.sweeps, 10, sopt)
     names = {0: "advect_tile_kernel (WENO5, one field)", 1: "stokes_apply_kernel<double>",
              2: "vel_sweep2d_kernel<float,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
              3: "vel_sweep2d_kernel<double,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
@@ -357,6 +408,10 @@ def main():
                       "and the crystal fraction copied out inside it",
             "plain_fp64_ms_per_step": ms_plain_max if ms_plain else None,
             "speedup_vs_plain_fp64": (ms_plain_max / ms) if ms_plain else None,
+            "mixed_vs_plain_fp64_field_error": field_err,
+            "field_error_note": f"max-norm relative deviation of W, U, P, x after {a.plain_steps} steps from the "
+                                "same saved state: mixed solver vs the plain FP64 solver",
+            "cpu_grid_gpu_timesteps_per_s": gpu_at_cpu_grid,
             "learned_preconditioner": "not built",
             "cache": "working set (~2 GB of fields and solver vectors) exceeds L2 (129 MB); no flush needed",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",

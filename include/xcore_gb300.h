@@ -8,8 +8,9 @@
  * keeps that state resident in GPU memory inside an opaque context with the
  * reference's field names and sizes (column-major, z the leading dimension,
  * src/state.jl:101-122, 218-258; src/noise.jl:82-92), and exports one entry
- * point per reference function.  Julia binds them with ccall (see
- * INTEGRATION.md); no torch or CUDA types appear in any signature.
+ * point per reference function.  Julia binds them with ccall (the binding is
+ * xcore.jl_gb300/julia/XcoreGPU.jl); no torch or CUDA types appear in any
+ * signature.
  *
  * Conventions
  *  - Every function returns an xc_status; on failure xc_last_error() holds a
@@ -137,12 +138,17 @@ typedef struct xc_solver_stats {
   double seconds;          /* device time of the solve */
 } xc_solver_stats;
 
+#define XC_MAX_SWEEPS 64
 typedef struct xc_step_stats {
-  double resnorm[16];      /* compute_resnorm per Picard sweep (diagnose.jl:57-71) */
-  int sweeps;
+  double resnorm[XC_MAX_SWEEPS];  /* compute_resnorm per Picard sweep (diagnose.jl:57-71) */
+  double resnorm0;         /* the loop's reference residual at the end (run.jl:246-249) */
+  int sweeps;              /* Picard sweeps run */
   int solver_iterations;   /* summed over sweeps */
   double solver_rel_residual;  /* worst final residual over the sweeps */
   double dt_next;          /* update_dt (update.jl:494-502) */
+  int unconverged_solves;  /* Stokes solves that stopped at their iteration cap above their rtol */
+  int picard_converged;    /* xc_step_converge: 1 when the loop ended on rtol / atol, 0 on maxit
+                              (or after the 3 sweeps of a loop that never met them); xc_step: 0 */
 } xc_step_stats;
 
 typedef struct xc_ctx xc_ctx;
@@ -224,17 +230,43 @@ int xc_conservation_sums(xc_ctx* ctx, double out[12]);
    out[22..57] Ra, Rc, ReD, Red, ks, ke, kx, eta, etamix, etae, etas, etat:
                min, geomean (exp(mean(log(max(a, eps))))), max each */
 int xc_history_stats(xc_ctx* ctx, double out[58]);
+/* The field statistics print_step! prints beyond record_history!'s
+                                                         src/diagnose.jl:92-182
+   (on the raw fields; the reference divides each by a scale first, which
+   min, max and geomean commute with):
+   out[0..2]   m: min, mean, max
+   out[3..23]  rho, V, vx, vm, xie, xix, xis: min, geomean, max each, with
+               geomean = exp(sum(log(max(a, 1e-300))) / length(a)) (diagnose.jl:10) */
+int xc_print_step_stats(xc_ctx* ctx, double out[24]);
 /* Fresh-start initialize! (src/run.jl:71-140) with the initial crystal
    fraction x (host (Nz,Nx)) in place of the MersenneTwister perturbation
    (run.jl:98-108) and the first white-noise draw re/rs. */
 int xc_initialize(xc_ctx* ctx, const double* x_init, const double* re, const double* rs);
-/* One outer time step of run! (src/run.jl:204-274): time_coefs, store_previous!,
-   store_noise!, `sweeps` Picard sweeps of phsevo! -> fluidmech! -> noise! ->
-   update_phase_velocities! -> update! -> compute_resnorm, then update_dt.
+/* One outer time step of run! (src/run.jl:204-274) with a fixed number of
+   Picard sweeps: time_coefs, store_previous!, store_noise!, `sweeps`
+   (1..XC_MAX_SWEEPS) sweeps of phsevo! -> fluidmech! -> noise! ->
+   update_phase_velocities! -> update! -> compute_resnorm, then update_dt.  This
+   is the reference's loop with maxit = sweeps >= 3 and rtol = atol = 0.
    re/rs are the step's white-noise draw (host arrays, or NULL to keep the
-   device ones).  stats may be NULL. */
+   device ones).  stats may be NULL.
+   Status: XC_NAN (and the step abandoned after that sweep, as report_iter
+   raises, diagnose.jl:80) when a sweep's residual norm is NaN; otherwise the
+   whole step is done and XC_NOT_CONVERGED is returned when any Stokes solve
+   of it stopped at its iteration cap above its rtol (the reference's direct
+   solve has no such case), XC_OK when every solve converged. */
 int xc_step(xc_ctx* ctx, int step, double dt, int sweeps, const double* re, const double* rs,
             const xc_solver_opts* opts, xc_step_stats* stats);
+/* The same step with run!'s own Picard loop (src/run.jl:220-250): at least 3
+   sweeps, then further sweeps while resnorm / resnorm0 >= rtol, resnorm >=
+   atol and fewer than maxit sweeps were run; resnorm0 is the first sweep's
+   norm and is raised whenever a sweep's norm exceeds it (both + 1e-32).  The
+   reference's defaults are rtol 1e-4, atol 1e-9, maxit 15
+   (src/parameters.jl:76-78); maxit is capped at XC_MAX_SWEEPS.  Statuses as
+   for xc_step; stats->picard_converged tells whether the loop met its
+   tolerances. */
+int xc_step_converge(xc_ctx* ctx, int step, double dt, double rtol, double atol, int maxit,
+                     const double* re, const double* rs, const xc_solver_opts* opts,
+                     xc_step_stats* stats);
 
 /* ------------------------------------------------------------------ */
 /* stencil-level entry points on caller device pointers                */
@@ -278,10 +310,14 @@ int xc_diffus_with_flux(double* dff, double* qx, double* qz, const double* f_hal
    holds until exit.  Limit: at most 2048 * 4096 = 8,388,608 elements per
    array (about 2894 x 2894 cells); larger grids return XC_BAD_ARG.  The first
    call on each device looks up the array's device address
-   (cudaGetSymbolAddress), so make that first call before any stream capture.
-   All calls share the array: calls that overlap on the GPU race and must not
-   be issued.  Nothing carries over between calls.  Stream-ordered on
-   `stream`; no host synchronisation. */
+   (cudaGetSymbolAddress) and keeps it, so make that first call before any
+   stream capture; the kept address dies with the device's primary context,
+   so do not call this again after a cudaDeviceReset (or a release of the
+   primary context) in the same process.  All calls share the array: calls
+   that overlap on the GPU race and must not be issued.  Nothing carries over
+   between calls.  Maxima and the final min / max follow Julia (a NaN input
+   gives a NaN step), as xc_update_dt does.  Stream-ordered on `stream`; no
+   host synchronisation. */
 int xc_update_dt_noalloc(const double* kx, const double* Wx, const double* Wm, const double* Ux,
                          const double* Um, int Nz, int Nx, double h, double CFL, double dtmax,
                          double dt_prev, double* dt_out, void* stream);

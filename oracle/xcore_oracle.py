@@ -806,13 +806,25 @@ def update(st: State, grid: Grid, par: Params, sc: dict, xBC="periodic", zBC="cl
     update_stresses(st, sc)
 
 
+def jmax(*v):
+    """Julia's max of Float64 scalars: NaN if any argument is NaN (Python's
+    builtin max keeps or drops a NaN depending on argument order)."""
+    return float(np.max(np.array(v, dtype=np.float64)))
+
+
+def jmin(*v):
+    """Julia's min of Float64 scalars (NaN propagates)."""
+    return float(np.min(np.array(v, dtype=np.float64)))
+
+
 def update_dt(st: State, grid: Grid, par: Params, dt_prev: float) -> float:
-    """src/update.jl:494-502."""
+    """src/update.jl:494-502 (numpy's max / min propagate NaN as Julia's
+    maximum / minimum do)."""
     h = grid.h
     dtk = (h / 2.0) * (h / 2.0) / st.kx.max()
-    vmax = max(np.abs(st.Wx).max(), np.abs(st.Wm).max(), np.abs(st.Ux).max(), np.abs(st.Um).max()) + EPS
+    vmax = jmax(np.abs(st.Wx).max(), np.abs(st.Wm).max(), np.abs(st.Ux).max(), np.abs(st.Um).max()) + EPS
     dta = (h / 2.0) / vmax
-    return min(1.5 * dt_prev, min(dtk, par.CFL * dta), par.dtmax)
+    return jmin(1.5 * dt_prev, jmin(dtk, par.CFL * dta), par.dtmax)
 
 
 # ---------------------------------------------------------------------------
@@ -1241,6 +1253,19 @@ def conservation_sums(st: State, grid: Grid) -> dict:
     return out
 
 
+def print_step_stats(st: State) -> dict:
+    """The statistics print_step! prints beyond record_history!'s
+    (src/diagnose.jl:92-182) on the raw fields, with
+    _gm(A) = exp(sum(log(max(A, 1e-300))) / length(A)) (diagnose.jl:10)."""
+    out = {"m_min": float(st.m.min()), "m_mean": float(st.m.mean()), "m_max": float(st.m.max())}
+    for f in ("rho", "V", "vx", "vm", "xie", "xix", "xis"):
+        a = getattr(st, f)
+        out[f + "_min"] = float(a.min())
+        out[f + "_gm"] = math.exp(float(np.log(np.maximum(a, 1e-300)).sum()) / a.size)
+        out[f + "_max"] = float(a.max())
+    return out
+
+
 def history_stats(st: State) -> dict:
     """Field statistics pushed by record_history! (src/history.jl:183-222), with
     _rms = sqrt(mean(x^2)) and _geomean = exp(mean(log(max(x, eps)))) (history.jl:8-9)."""
@@ -1316,6 +1341,27 @@ def picard_sweep(st, grid, par, sc, ns, coefs, dt, it, re, rs, ADVN=None, xBC="p
     update_phase_velocities(st, grid, par, xBC, zBC)
     update(st, grid, par, sc, xBC, zBC)
     return resnorm(st, snap, dt)
+
+
+def timestep_converge(st, grid, par, sc, ns, step, dt, re, rs, rtol=1e-4, atol=1e-9, maxit=15,
+                      xBC="periodic", zBC="closed", stokes=None):
+    """One outer step of run! with its own Picard loop (src/run.jl:204-274,
+    the while-condition of 220-222 and the resnorm0 rule of 246-249); returns
+    (dt_next, [resnorms], resnorm0)."""
+    coefs = time_coefs(par.TINT, step)
+    store_previous(st)
+    store_noise(st)
+    resnorm, resnorm0, it = 1.0, 1.0, 0
+    norms = []
+    while (resnorm / resnorm0 >= rtol and resnorm >= atol and it < maxit) or it < 3:
+        it += 1
+        resnorm = picard_sweep(st, grid, par, sc, ns, coefs, dt, it, re, rs, xBC=xBC, zBC=zBC, stokes=stokes)[0]
+        norms.append(resnorm)
+        if it == 1 or resnorm > resnorm0:
+            resnorm0 = resnorm + 1e-32
+        if math.isnan(resnorm):
+            raise FloatingPointError(f"Solver diverged with NaN at iter {it}")
+    return update_dt(st, grid, par, dt), norms, resnorm0
 
 
 def timestep(st, grid, par, sc, ns, step, dt, re, rs, sweeps=3, xBC="periodic", zBC="closed",

@@ -1,0 +1,216 @@
+"""Parity at the sizes of the benchmark configurations (tests/configs.py), on
+the GPU through the C ABI against the CPU oracle.
+
+1. Identical Stokes inputs, per sweep (c1 100^2 for 10 steps; c2 400^2 for
+   one step, WENO5 and QUICK): the GPU and the oracle run each Picard sweep
+   in lockstep, the oracle taking the GPU's Stokes solution (W, U, P) in
+   place of its sparse LU; every other field of FluidState, PhaseState and
+   NoiseState -- the stencils, phsevo!, the MFS update, noise!, the phase
+   velocities, update! -- must then agree within 1e-12 (normwise relative)
+   after every sweep, and dt and the residual norms with them.
+2. Whole trajectories against the committed oracle digests
+   (tests/golden/make_configs.py): 100 steps of c1 and 3 steps of c2 (WENO5,
+   QUICK), the GPU solving Stokes with FP64 FGMRES to 1e-11 where the oracle
+   factorises; the per-step field digests stay within the bounds stated at
+   each test.  The oracle itself must reproduce the c1 digests on this host.
+3. c3 (lognormal crystal fraction, etacntr 1e4): the FP64 and the mixed
+   solver against the sparse LU at 256^2, and the mixed solver against the
+   FP64 solver at 1024^2, field by field (W, U, P)."""
+import os
+
+import numpy as np
+import pytest
+
+import configs as C
+import xcore_oracle as O
+import xcore_gb300 as xc
+from gpu_helpers import device_state, rel_err
+
+pytestmark = pytest.mark.gpu
+pytest.importorskip("torch")
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+SOLVED = {"W", "U", "P"}
+COMPARED = [n for g in xc.CHECKPOINT_GROUPS.values() for n in g if n not in SOLVED]
+
+
+def _maxrel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _compare_all(ds, st, where, tol=1e-12):
+    bad = {}
+    for n in COMPARED:
+        ref = getattr(st, n)
+        got = ds[n]
+        if ref.dtype == bool:
+            if not np.array_equal(got, ref):
+                bad[n] = "mask differs"
+            continue
+        e = rel_err(got, ref)
+        if not e <= tol:
+            bad[n] = e
+    assert not bad, (where, bad)
+
+
+def _lockstep(cfg, scheme, steps):
+    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup(cfg, scheme=scheme)
+    st = O.initialize(g, par, sc, ns, x0, re0, rs0)
+    ds = device_state(par, g, sc)
+    ds.initialize(x0, re0, rs0)
+    _compare_all(ds, st, "initialize!")
+    dt = sc["dt0"]
+    for step in range(1, steps + 1):
+        re, rs = draws.next()
+        coefs = O.time_coefs(par.TINT, step)
+        O.store_previous(st)
+        O.store_noise(st)
+        ds.store_previous()
+        ds.store_noise()
+        for it in range(1, 4):
+            snap = O.snapshot(st)
+            ds.snapshot()
+            O.phsevo(st, g, par, sc, scheme, coefs, dt)
+            ds.phsevo(coefs, dt)
+            info = ds.fluidmech(coefs, dt, solver="fgmres64", rtol=1e-10, maxit=2000)
+            assert info["converged"], (step, it, info)
+            O.mfs_update(st, par, coefs, dt)         # the oracle's own MFS / drhodt
+            st.W, st.U, st.P = ds["W"], ds["U"], ds["P"]
+            O.noise(st, g, par, sc, ns, dt, it == 1, re, rs)
+            ds.noise(dt, it == 1, re, rs)
+            O.update_phase_velocities(st, g, par)
+            ds.update_phase_velocities()
+            O.update(st, g, par, sc)
+            ds.update()
+            _compare_all(ds, st, (cfg, scheme, step, it))
+            np.testing.assert_allclose(ds.compute_resnorm(dt), O.resnorm(st, snap, dt), rtol=1e-10)
+        dt_g = ds.update_dt(dt)
+        dt = O.update_dt(st, g, par, dt)
+        assert dt_g == pytest.approx(dt, rel=1e-14), step
+    ds.close()
+
+
+def test_c1_identical_stokes_inputs_ten_steps():
+    _lockstep("c1", "weno5", 10)
+
+
+@pytest.mark.parametrize("scheme", ["weno5", "quick"])
+def test_c2_identical_stokes_inputs_one_step(scheme):
+    _lockstep("c2", scheme, 1)
+
+
+def _trajectory(cfg, scheme, name, steps, bound_fields, bound_dt):
+    z = np.load(os.path.join(GOLD, name))
+    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup(cfg, scheme=scheme)
+    assert C.digest_error(C.digest(x0), z["x0_digest"]) == 0.0
+    chk = float((re0 * re0).sum() + rs0.sum())
+    ds = device_state(par, g, sc)
+    ds.initialize(x0, re0, rs0)
+    dt = sc["dt0"]
+    worst = {}
+    for step in range(1, steps + 1):
+        re, rs = draws.next()
+        chk += float((re * re).sum() + rs.sum())
+        assert dt == pytest.approx(z["dt"][step - 1], rel=bound_dt), step
+        info = ds.step(step, dt, re, rs, sweeps=3, solver="fgmres64", rtol=1e-11, maxit=3000)
+        dt = info["dt_next"]
+        for k, f in enumerate(C.DIGEST_FIELDS):
+            e = C.digest_error(C.digest(ds[f]), z["digest"][step - 1, k])
+            worst[f] = max(worst.get(f, 0.0), e)
+            assert e <= bound_fields, (name, step, f, e)
+        for f in ("x", "W", "U", "P"):
+            key = f"s{step}_{f}"
+            if key in z.files:
+                assert rel_err(ds[f], z[key]) <= bound_fields, (key, rel_err(ds[f], z[key]))
+    assert chk == pytest.approx(float(z["draw_checksum"][0]), rel=1e-12)
+    assert dt == pytest.approx(float(z["dt_next"][0]), rel=bound_dt)
+    print(name, "worst digest deviation per field over", steps, "steps:",
+          {k: f"{v:.1e}" for k, v in worst.items()})
+    ds.close()
+
+
+def test_c1_trajectory_100_steps_matches_oracle_digests():
+    """100 steps at 100^2: iterative Stokes (FP64 FGMRES, 1e-11) against the
+    oracle's sparse LU; the fields stay within 1e-6 of the oracle's digests
+    (norms, sums, extremes, 64 fixed samples per field) at every step."""
+    _trajectory("c1", "weno5", "c1_100.npz", 100, 1e-6, 1e-6)
+
+
+@pytest.mark.parametrize("scheme", ["weno5", "quick"])
+def test_c2_trajectory_three_steps_matches_oracle_digests(scheme):
+    name = f"c2_400_{scheme}.npz"
+    if not os.path.exists(os.path.join(GOLD, name)):
+        pytest.skip(f"{name} not generated")
+    _trajectory("c2", scheme, name, 3, 1e-7, 1e-8)
+
+
+def test_oracle_reproduces_c1_digests_on_this_host():
+    """The oracle run here (numpy, SciPy SuperLU) reproduces the committed c1
+    digests for the first ten steps: the checker is the same on every host."""
+    z = np.load(os.path.join(GOLD, "c1_100.npz"))
+    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup("c1")
+    st = O.initialize(g, par, sc, ns, x0, re0, rs0)
+    dt = sc["dt0"]
+    for step in range(1, 11):
+        re, rs = draws.next()
+        dt, _ = O.timestep(st, g, par, sc, ns, step, dt, re, rs, sweeps=3)
+        for k, f in enumerate(C.DIGEST_FIELDS):
+            e = C.digest_error(C.digest(getattr(st, f)), z["digest"][step - 1, k])
+            assert e <= 1e-9, (step, f, e)
+
+
+def _c3_state(N):
+    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup("c3", N=N)
+    ds = device_state(par, g, sc)
+    ds.initialize(x0, re0, rs0)
+    coefs = O.time_coefs(par.TINT, 1)
+    ds.store_previous()
+    ds.store_noise()
+    ds.snapshot()
+    ds.phsevo(coefs, sc["dt0"])
+    return par, g, sc, ds, coefs, sc["dt0"]
+
+
+def test_c3_fp64_and_mixed_against_lu_256():
+    """Per-field error of both GPU solvers against the sparse LU at 256^2
+    (lognormal crystal fraction, viscosity contrast cap 1e4): FP64 FGMRES to
+    1e-10 within 1e-8, the mixed solver to 1e-9 within 1e-7 (max-norm,
+    relative to each field's max)."""
+    par, g, sc, ds, coefs, dt = _c3_state(256)
+    state = ds.checkpoint()
+    st = O.State(g.Nz, g.Nx)
+    for name, arr in state.items():
+        setattr(st, name.split("/", 1)[1], arr.copy())
+    O.fluidmech(st, g, par, coefs, dt)
+    errs = {}
+    for solver, rtol, tol in (("fgmres64", 1e-10, 1e-8), ("mixed", 1e-9, 1e-7)):
+        ds.restore(state)
+        info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol, maxit=3000, inner_rtol=5e-2, inner_maxit=30,
+                            pressure_sweeps=1)
+        assert info["converged"], (solver, info)
+        for k in ("W", "U", "P"):
+            errs[(solver, k)] = _maxrel(ds[k], getattr(st, k))
+            assert errs[(solver, k)] <= tol, (solver, k, errs[(solver, k)], info)
+    print("c3 256^2 max-norm relative error against the sparse LU:",
+          {f"{s}/{k}": f"{v:.2e}" for (s, k), v in errs.items()})
+    ds.close()
+
+
+def test_c3_mixed_against_fp64_1024():
+    """The mixed solver (FP32 Krylov and multigrid in FP64 refinement, 1e-9)
+    against the plain FP64 solver (1e-11) at 1024^2, field by field."""
+    par, g, sc, ds, coefs, dt = _c3_state(1024)
+    state = {k: ds[k] for k in ("W", "U", "P", "MFS", "drhodt")}
+    info = ds.fluidmech(coefs, dt, solver="fgmres64", rtol=1e-11, maxit=3000)
+    assert info["converged"], info
+    ref = {k: ds[k] for k in ("W", "U", "P")}
+    for k, v in state.items():
+        ds[k] = v
+    info = ds.fluidmech(coefs, dt, solver="mixed", rtol=1e-9, maxit=400, inner_rtol=5e-2, inner_maxit=30,
+                        pressure_sweeps=1)
+    assert info["converged"], info
+    errs = {k: _maxrel(ds[k], ref[k]) for k in ("W", "U", "P")}
+    print("c3 1024^2 mixed vs FP64 max-norm relative error:", {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, e in errs.items():
+        assert e <= 1e-7, (k, e)
+    ds.close()

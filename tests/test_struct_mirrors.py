@@ -22,13 +22,15 @@ MIRRORS = {
     "xc_params": (xc._Params, "XcParams"),
     "xc_solver_opts": (xc.SolverOpts, "SolverOpts"),
     "xc_solver_stats": (xc.SolverStats, "SolverStats"),
-    "xc_step_stats": (xc.StepStats, None),
+    "xc_step_stats": (xc.StepStats, "StepStats"),
 }
 
 
 def c_fields(name):
     """[(field, ctype, count)] of `typedef struct name {...} name;` in the header."""
     src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    for k, v in re.findall(r"^#define (\w+) (\d+)$", src, flags=re.M):
+        src = re.sub(r"\b%s\b" % k, v, src)
     m = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), src, flags=re.S)
     assert m, name
     out = []

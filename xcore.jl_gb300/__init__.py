@@ -49,7 +49,11 @@ class XcoreError(RuntimeError):
 
 
 class NotConverged(XcoreError):
-    pass
+    """A Stokes solve stopped at its iteration cap above its tolerance.  For a
+    whole time step the step was still completed; ``info`` then holds its
+    statistics (as ``State.step`` returns them)."""
+
+    info = None
 
 
 class _Params(ctypes.Structure):
@@ -102,9 +106,20 @@ class SolverStats(ctypes.Structure):
                 ("converged", ctypes.c_int), ("seconds", ctypes.c_double)]
 
 
+MAX_SWEEPS = 64
+
+
 class StepStats(ctypes.Structure):
-    _fields_ = [("resnorm", ctypes.c_double * 16), ("sweeps", ctypes.c_int), ("solver_iterations", ctypes.c_int),
-                ("solver_rel_residual", ctypes.c_double), ("dt_next", ctypes.c_double)]
+    _fields_ = [("resnorm", ctypes.c_double * MAX_SWEEPS), ("resnorm0", ctypes.c_double),
+                ("sweeps", ctypes.c_int), ("solver_iterations", ctypes.c_int),
+                ("solver_rel_residual", ctypes.c_double), ("dt_next", ctypes.c_double),
+                ("unconverged_solves", ctypes.c_int), ("picard_converged", ctypes.c_int)]
+
+    def as_dict(self):
+        return dict(resnorm=list(self.resnorm[:self.sweeps]), resnorm0=self.resnorm0, sweeps=self.sweeps,
+                    solver_iterations=self.solver_iterations, solver_rel_residual=self.solver_rel_residual,
+                    dt_next=self.dt_next, unconverged_solves=self.unconverged_solves,
+                    picard_converged=bool(self.picard_converged))
 
 
 _lib = None
@@ -146,6 +161,9 @@ def lib():
             "xc_history_stats": (ip, [vp, D6]),
             "xc_initialize": (ip, [vp, vp, vp, vp]),
             "xc_step": (ip, [vp, ip, dp, ip, vp, vp, ctypes.POINTER(SolverOpts), ctypes.POINTER(StepStats)]),
+            "xc_step_converge": (ip, [vp, ip, dp, dp, dp, ip, vp, vp, ctypes.POINTER(SolverOpts),
+                                      ctypes.POINTER(StepStats)]),
+            "xc_print_step_stats": (ip, [vp, D6]),
             "xc_fill_ghosts": (ip, [vp, ip, ip, ip, ip, ip, vp]),
             "xc_advect": (ip, [vp, vp, vp, vp, ip, ip, dp, ip, vp]),
             "xc_advect_with_flux": (ip, [vp, vp, vp, vp, vp, vp, ip, ip, dp, ip, ip, ip, vp]),
@@ -483,6 +501,16 @@ class State:
         _check(lib().xc_history_stats(self._h, out))
         return dict(zip(self.HISTORY_KEYS, out))
 
+    PRINT_KEYS = (["m_min", "m_mean", "m_max"]
+                  + [f"{f}_{s}" for f in ("rho", "V", "vx", "vm", "xie", "xix", "xis") for s in ("min", "gm", "max")])
+
+    def print_step_stats(self):
+        """The statistics print_step! adds to record_history!'s, on the raw
+        fields -- src/diagnose.jl:92-182."""
+        out = (ctypes.c_double * 24)()
+        _check(lib().xc_print_step_stats(self._h, out))
+        return dict(zip(self.PRINT_KEYS, out))
+
     # ---- checkpoints -------------------------------------------------------
     def checkpoint(self):
         """The device state as save_checkpoint groups it (src/restart.jl:53-83):
@@ -525,19 +553,49 @@ class State:
         a, b = _host(re, (g.Nz, g.Nx)), _host(rs, (g.Nz, g.Nx))
         _check(lib().xc_initialize(self._h, x.ctypes.data, a.ctypes.data, b.ctypes.data))
 
-    def step(self, step, dt, re=None, rs=None, sweeps=3, solver="fgmres64", rtol=1e-10, maxit=500,
-             restart=30, inner_rtol=1e-4, inner_maxit=60, **knobs):
-        """One outer step of run! (src/run.jl:204-274) with `sweeps` Picard sweeps."""
+    def _draws(self, re, rs):
         g = self.grid
         a = _host(re, (g.Nz, g.Nx)) if re is not None else None
         b = _host(rs, (g.Nz, g.Nx)) if rs is not None else None
+        return a, b, (a.ctypes.data if a is not None else None), (b.ctypes.data if b is not None else None)
+
+    @staticmethod
+    def _step_result(status, st):
+        """The step's statistics; a non-converged Stokes solve raises
+        NotConverged carrying them (the step itself was completed)."""
+        info = st.as_dict()
+        if status == XC_NOT_CONVERGED:
+            err = NotConverged(status, lib().xc_last_error().decode())
+            err.info = info
+            raise err
+        _check(status)
+        return info
+
+    def step(self, step, dt, re=None, rs=None, sweeps=3, solver="fgmres64", rtol=1e-10, maxit=500,
+             restart=30, inner_rtol=1e-4, inner_maxit=60, **knobs):
+        """One outer step of run! (src/run.jl:204-274) with `sweeps` Picard
+        sweeps (the reference's loop with maxit = sweeps, rtol = atol = 0)."""
+        a, b, pa, pb = self._draws(re, rs)
         o = SolverOpts.make(solver, rtol, maxit, restart, inner_rtol, inner_maxit, **knobs)
         st = StepStats()
-        _check(lib().xc_step(self._h, int(step), float(dt), int(sweeps),
-                             a.ctypes.data if a is not None else None, b.ctypes.data if b is not None else None,
-                             ctypes.byref(o), ctypes.byref(st)))
-        return dict(resnorm=list(st.resnorm[:st.sweeps]), sweeps=st.sweeps, solver_iterations=st.solver_iterations,
-                    solver_rel_residual=st.solver_rel_residual, dt_next=st.dt_next)
+        status = lib().xc_step(self._h, int(step), float(dt), int(sweeps), pa, pb, ctypes.byref(o),
+                               ctypes.byref(st))
+        return self._step_result(status, st)
+
+    def step_converge(self, step, dt, re=None, rs=None, picard_rtol=1e-4, picard_atol=1e-9, picard_maxit=15,
+                      solver="fgmres64", rtol=1e-10, maxit=500, restart=30, inner_rtol=1e-4, inner_maxit=60,
+                      **knobs):
+        """One outer step of run! with the reference's own Picard loop
+        (src/run.jl:220-250): at least 3 sweeps, then on while
+        resnorm/resnorm0 >= picard_rtol and resnorm >= picard_atol and fewer
+        than picard_maxit sweeps ran (par.rtol, par.atol, par.maxit,
+        src/parameters.jl:76-78)."""
+        a, b, pa, pb = self._draws(re, rs)
+        o = SolverOpts.make(solver, rtol, maxit, restart, inner_rtol, inner_maxit, **knobs)
+        st = StepStats()
+        status = lib().xc_step_converge(self._h, int(step), float(dt), float(picard_rtol), float(picard_atol),
+                                        int(picard_maxit), pa, pb, ctypes.byref(o), ctypes.byref(st))
+        return self._step_result(status, st)
 
 
 class Ensemble:

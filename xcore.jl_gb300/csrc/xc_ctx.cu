@@ -135,6 +135,9 @@ extern "C" int xc_ctx_create(const xc_params* par, xc_ctx** out) {
     return fail(XC_CUDA);
   }
   cudaMemsetAsync(c->dscal, 0, sizeof(double) * 64, c->stream);
+  // the arrival counters at the end of each reduction scratch start at zero
+  cudaMemsetAsync(c->red_partials, 0, sizeof(double) * c->red_partials_len, c->stream);
+  cudaMemsetAsync(c->red_partials_side, 0, sizeof(double) * c->red_partials_len, c->stream);
   int st = noise_plan_create(c);
   if (st != XC_OK) return fail(st);
   st = stokes_create(c);
@@ -332,11 +335,11 @@ extern "C" int xc_initialize(xc_ctx* c, const double* x_init, const double* re, 
   return XC_OK;
 }
 
-// one outer step of run! (src/run.jl:204-274) with a fixed sweep count
-extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double* re,
-                       const double* rs, const xc_solver_opts* opts, xc_step_stats* stats) {
-  XC_TRY(check_ctx(c));
-  if (sweeps < 1 || sweeps > 16) { xc_set_error("xc_step: sweeps must be 1..16"); return XC_BAD_ARG; }
+// One outer step of run! (src/run.jl:204-274).  fixed_sweeps > 0 runs exactly
+// that many Picard sweeps; fixed_sweeps == 0 runs the reference's while-loop
+// (run.jl:220-250) with rtol / atol / maxit.
+static int step_impl(xc_ctx* c, int step, double dt, int fixed_sweeps, double rtol, double atol, int maxit,
+                     const double* re, const double* rs, const xc_solver_opts* opts, xc_step_stats* stats) {
   double coefs[6];
   XC_TRY(xc_time_coefs(c->p.TINT, step, coefs));
   XC_TRY(store_previous_impl(c));
@@ -349,10 +352,22 @@ extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double*
     XC_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     return XC_OK;
   };
-  for (int it = 1; it <= sweeps; ++it) {
-    XC_TRY(snapshot_impl(c));
+  auto finish = [&](int st) {
+    if (stats) *stats = local;
+    return st;
+  };
+  double resnorm = 1.0, resnorm0 = 1.0;
+  int it = 0;
+  auto more = [&]() {
+    if (fixed_sweeps > 0) return it < fixed_sweeps;
+    return (resnorm / resnorm0 >= rtol && resnorm >= atol && it < maxit) || it < 3;
+  };
+  while (more()) {
+    ++it;
+    local.sweeps = it;
+    XC_TRY(finish(snapshot_impl(c)));
     int st = phsevo_impl(c, c->p.ADVN, coefs, dt, c->p.alpha);
-    if (st != XC_OK) return st;
+    if (st != XC_OK) return finish(st);
     // noise! (run.jl:240) reads only what the previous update! (or the
     // initial state) left -- V, vx, fReL, ke, ks, chi, the face fractions and
     // the stored noise -- none of which phsevo! or fluidmech! write, and
@@ -362,29 +377,68 @@ extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double*
     XC_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
     int nst = noise_impl(c, dt, it == 1, it == 1 ? re : nullptr, it == 1 ? rs : nullptr, c->side,
                          c->red_partials_side);
-    if (nst != XC_OK) { join(); return nst; }
+    if (nst != XC_OK) { join(); return finish(nst); }
     xc_solver_stats ss;
     std::memset(&ss, 0, sizeof(ss));
     st = fluidmech_impl(c, coefs, dt, opts, &ss, nullptr);
-    XC_TRY(join());
-    if (st != XC_OK && st != XC_NOT_CONVERGED) return st;
+    XC_TRY(finish(join()));
+    // a solve that stopped at its iteration cap leaves a usable iterate; the
+    // step goes on as the reference's would and reports it at the end
+    if (st == XC_NOT_CONVERGED) ++local.unconverged_solves;
+    else if (st != XC_OK) return finish(st);
     local.solver_iterations += ss.iterations;
     if (ss.rel_residual > local.solver_rel_residual) local.solver_rel_residual = ss.rel_residual;
-    XC_TRY(phase_velocities_impl(c));
-    XC_TRY(update_impl(c));
+    XC_TRY(finish(phase_velocities_impl(c)));
+    XC_TRY(finish(update_impl(c)));
     double rn[3];
-    XC_TRY(resnorm_impl(c, dt, rn));
-    local.resnorm[it - 1] = rn[0];
-    if (std::isnan(rn[0])) {
+    XC_TRY(finish(resnorm_impl(c, dt, rn)));
+    resnorm = rn[0];
+    local.resnorm[it - 1] = resnorm;
+    // set the reference on the first sweep, raise it when the residual grew
+    // (run.jl:246-249)
+    if (it == 1 || resnorm > resnorm0) resnorm0 = resnorm + 1e-32;
+    local.resnorm0 = resnorm0;
+    if (std::isnan(resnorm)) {
       xc_set_error("Solver diverged with NaN at iter %d", it);
-      if (stats) *stats = local;
-      return XC_NAN;
+      return finish(XC_NAN);
     }
   }
-  local.sweeps = sweeps;
-  XC_TRY(update_dt_impl(c, dt, &local.dt_next));
-  if (stats) *stats = local;
-  return XC_OK;
+  if (fixed_sweeps == 0) local.picard_converged = (resnorm / resnorm0 < rtol || resnorm < atol) ? 1 : 0;
+  XC_TRY(finish(update_dt_impl(c, dt, &local.dt_next)));
+  if (local.unconverged_solves > 0) {
+    xc_set_error("step %d: %d of %d Stokes solves stopped at their iteration cap (worst relative residual "
+                 "%.3e); the step was completed with those iterates", step, local.unconverged_solves, it,
+                 local.solver_rel_residual);
+    return finish(XC_NOT_CONVERGED);
+  }
+  return finish(XC_OK);
+}
+
+extern "C" int xc_step(xc_ctx* c, int step, double dt, int sweeps, const double* re,
+                       const double* rs, const xc_solver_opts* opts, xc_step_stats* stats) {
+  XC_TRY(check_ctx(c));
+  if (sweeps < 1 || sweeps > XC_MAX_SWEEPS) {
+    xc_set_error("xc_step: sweeps must be 1..%d", XC_MAX_SWEEPS);
+    return XC_BAD_ARG;
+  }
+  return step_impl(c, step, dt, sweeps, 0.0, 0.0, sweeps, re, rs, opts, stats);
+}
+
+extern "C" int xc_step_converge(xc_ctx* c, int step, double dt, double rtol, double atol, int maxit,
+                                const double* re, const double* rs, const xc_solver_opts* opts,
+                                xc_step_stats* stats) {
+  XC_TRY(check_ctx(c));
+  if (maxit < 0 || maxit > XC_MAX_SWEEPS || !(rtol >= 0) || !(atol >= 0)) {
+    xc_set_error("xc_step_converge: need 0 <= maxit <= %d and rtol, atol >= 0", XC_MAX_SWEEPS);
+    return XC_BAD_ARG;
+  }
+  return step_impl(c, step, dt, 0, rtol, atol, maxit, re, rs, opts, stats);
+}
+
+extern "C" int xc_print_step_stats(xc_ctx* c, double out[24]) {
+  XC_TRY(check_ctx(c));
+  if (!out) { xc_set_error("xc_print_step_stats: null output"); return XC_BAD_ARG; }
+  return print_stats_impl(c, out);
 }
 
 // ---------------------------------------------------------------------------

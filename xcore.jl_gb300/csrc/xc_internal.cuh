@@ -183,9 +183,36 @@ inline dim3 grid2d(int rows, int cols, dim3 blk) {
   return dim3((unsigned)((rows + blk.x - 1) / blk.x), (unsigned)((cols + blk.y - 1) / blk.y));
 }
 
-// deterministic reductions (xc_reduce.cu): block partials + single-block final
+// Julia's max / min of two Float64 (a NaN argument gives NaN; CUDA's fmax /
+// fmin return the other argument instead)
+__host__ __device__ __forceinline__ double jmax(double a, double b) {
+  return (a != a || b != b) ? a + b : (a > b ? a : b);
+}
+__host__ __device__ __forceinline__ double jmin(double a, double b) {
+  return (a != a || b != b) ? a + b : (a < b ? a : b);
+}
+
+// deterministic reductions (xc_reduce.cu): CTA partials, combined in a fixed
+// order by the last CTA to finish; up to kMaxRedJobs reductions per launch
 enum RedOp : int { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2, RED_SUMSQ = 3, RED_MAXABS = 4,
-                   RED_SUMSQDIFF = 5, RED_SUMLOG = 6 /* sum of log(max(a, eps)) */ };
+                   RED_SUMSQDIFF = 5, RED_SUMLOG = 6 /* sum of log(max(a, floor)) */ };
+constexpr int kMaxRedJobs = 32;
+struct RedJob {
+  const double* a;
+  const double* b;           // second operand of RED_SUMSQDIFF
+  const double* center;      // device scalar: sum of (a - *center)^2 instead of op
+  double* out;               // device result: reduction / divisor
+  double divisor;
+  double floor;              // RED_SUMLOG floor (eps by default)
+  int lda, ldb, rows, cols;
+  int op;
+  int nblk;                  // set by reduce_batch
+};
+RedJob red_job(int op, CView a, CView b, const double* center, int rows, int cols, double* out,
+               double divisor = 1.0);
+// njobs independent reductions, kMaxRedJobs per launch, on stream s with
+// scratch `partials` (c->red_partials when null)
+int reduce_batch(xc_ctx* c, const RedJob* jobs, int njobs, cudaStream_t s, double* partials = nullptr);
 // reduce a column-major view of rows x cols into dscal[slot] (device); b may be
 // null unless op == RED_SUMSQDIFF (sum of (a-b)^2)
 int reduce_view(xc_ctx* c, int op, CView a, CView b, int rows, int cols, int slot);
@@ -218,6 +245,7 @@ int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out);
 int resnorm_impl(xc_ctx* c, double dt, double out[3]);
 int sums_impl(xc_ctx* c, double out[12]);
 int history_impl(xc_ctx* c, double out[58]);
+int print_stats_impl(xc_ctx* c, double out[24]);
 
 int noise_plan_create(xc_ctx* c);
 void noise_plan_destroy(xc_ctx* c);

@@ -34,7 +34,11 @@ std::mutex g_setup_mutex;
 double* g_scratch_addr[XC_NOALLOC_MAX_DEVICES] = {nullptr};
 
 // device address of g_dt_scratch for the current device (looked up once per
-// device; in host code the symbol itself is only a host-side stand-in)
+// device; in host code the symbol itself is only a host-side stand-in).  The
+// address lives as long as the device's primary context: a cudaDeviceReset,
+// or a release and re-creation of the primary context, unloads the module
+// and makes the kept address stale, so this entry point must not be called
+// after such a reset in the same process.
 int scratch_for_current_device(double** out) {
   int dev = 0;
   XC_CUDA_TRY(cudaGetDevice(&dev));
@@ -62,51 +66,53 @@ struct DtInputs {
   long long n[5];
 };
 
+// warp shuffles, then the eight warp maxima in order (Julia's max: NaN wins)
+__device__ __forceinline__ double block_max(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v = jmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = sh[0];
+  for (int k = 1; k < XC_NOALLOC_THREADS / 32; ++k) r = jmax(r, sh[k]);
+  return r;
+}
+
 // CTA (x, y) reduces elements [x*CHUNK, (x+1)*CHUNK) of array y into scratch
 __global__ void __launch_bounds__(XC_NOALLOC_THREADS) dt_partial_kernel(DtInputs in, double* scratch) {
-  __shared__ double sh[XC_NOALLOC_THREADS];
+  __shared__ double sh[XC_NOALLOC_THREADS / 32];
   const int y = blockIdx.y;
   const long long n = in.n[y];
   const long long base = (long long)blockIdx.x * XC_NOALLOC_CHUNK;
   double m = -INFINITY;
   for (long long t = base + threadIdx.x; t < n && t < base + XC_NOALLOC_CHUNK; t += XC_NOALLOC_THREADS) {
     double v = in.a[y][t];
-    m = fmax(m, y == 0 ? v : fabs(v));
+    m = jmax(m, y == 0 ? v : fabs(v));
   }
-  sh[threadIdx.x] = m;
-  __syncthreads();
-  for (int s = XC_NOALLOC_THREADS / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) scratch[(size_t)y * XC_NOALLOC_MAX_BLOCKS + blockIdx.x] = sh[0];
+  const double r = block_max(m, sh);
+  if (threadIdx.x == 0) scratch[(size_t)y * XC_NOALLOC_MAX_BLOCKS + blockIdx.x] = r;
 }
 
-// combine the partials and evaluate update_dt (src/update.jl:494-502)
+// combine the partials and evaluate update_dt (src/update.jl:494-502) with
+// Julia's min / max, as xc_update_dt does
 __global__ void __launch_bounds__(XC_NOALLOC_THREADS) dt_final_kernel(const double* scratch, DtInputs in,
                                                                       double h, double CFL, double dtmax,
                                                                       double dt_prev, double* dt_out) {
-  __shared__ double sh[XC_NOALLOC_THREADS];
+  __shared__ double sh[XC_NOALLOC_THREADS / 32];
   __shared__ double mx[5];
   for (int y = 0; y < 5; ++y) {
     const int nb = (int)((in.n[y] + XC_NOALLOC_CHUNK - 1) / XC_NOALLOC_CHUNK);
     double m = -INFINITY;
     for (int b = threadIdx.x; b < nb; b += XC_NOALLOC_THREADS)
-      m = fmax(m, scratch[(size_t)y * XC_NOALLOC_MAX_BLOCKS + b]);
-    sh[threadIdx.x] = m;
-    __syncthreads();
-    for (int s = XC_NOALLOC_THREADS / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) mx[y] = sh[0];
-    __syncthreads();
+      m = jmax(m, scratch[(size_t)y * XC_NOALLOC_MAX_BLOCKS + b]);
+    const double r = block_max(m, sh);
+    if (threadIdx.x == 0) mx[y] = r;
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
     double dtk = (h / 2.0) * (h / 2.0) / mx[0];
-    double vmax = fmax(fmax(fmax(mx[1], mx[2]), mx[3]), mx[4]) + XC_EPS;
+    double vmax = jmax(jmax(jmax(mx[1], mx[2]), mx[3]), mx[4]) + XC_EPS;
     double dta = (h / 2.0) / vmax;
-    *dt_out = fmin(fmin(1.5 * dt_prev, fmin(dtk, CFL * dta)), dtmax);
+    *dt_out = jmin(jmin(1.5 * dt_prev, jmin(dtk, CFL * dta)), dtmax);
   }
 }
 

@@ -243,13 +243,13 @@ __global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double l0h, dou
   double taus = l0h / (2.0 * (AT(vx, j, i) + XC_EPS));
   double St = txi0 / (taue + XC_EPS);
   double fr = AT(fReL, j, i), k = AT(ke, j, i), ch = AT(chi, j, i);
-  double sge = Xi * sqrt(fmax(0.0, (fr * k) / taue));
-  double sgx = Xi * sqrt(fmax(0.0, ((((ch * fr) * k) / taue) * St) / (1.0 + St * St)));
-  double sgs = Xi * sqrt(fmax(0.0, (ch * AT(ks, j, i)) / taus));
+  double sge = Xi * sqrt(jmax(0.0, (fr * k) / taue));
+  double sgx = Xi * sqrt(jmax(0.0, ((((ch * fr) * k) / taue) * St) / (1.0 + St * St)));
+  double sgs = Xi * sqrt(jmax(0.0, (ch * AT(ks, j, i)) / taus));
   taue = 1.0 / (1.0 / taue + 1.0 / (1e2 * dt)) + dt;
   taus = 1.0 / (1.0 / taus + 1.0 / (1e2 * dt)) + dt;
   double Fte = exp((-dt) / taue), Fts = exp((-dt) / taus);
-  double ae = sqrt(fmax(0.0, 1.0 - Fte * Fte)), as = sqrt(fmax(0.0, 1.0 - Fts * Fts));
+  double ae = sqrt(jmax(0.0, 1.0 - Fte * Fte)), as = sqrt(jmax(0.0, 1.0 - Fts * Fts));
   double r1 = AT(re, j, i), r2 = AT(rs, j, i);
   AT(psie, j, i) = Fte * AT(psieo, j, i) + ((ae * sge) * fL) * r1;
   AT(psix, j, i) = Fte * AT(psixo, j, i) + ((ae * sgx) * fL) * r1;
@@ -297,7 +297,7 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
     int jj = icz_c(j, Nz);
     AT(xieu, j, i) = corner_avg(pe, jj + 1, i, Nz, Nx) - corner_avg(pe, jj, i, Nz, Nx);
     double a = AT(chiu, j, i), b = AT(muu, j, i);
-    double tap = (1.0 - exp((-a) / 1e-4)) * (1.0 - exp((-fmax(0.0, b - 0.4)) / 0.05));
+    double tap = (1.0 - exp((-a) / 1e-4)) * (1.0 - exp((-jmax(0.0, b - 0.4)) / 0.05));
     AT(xixu, j, i) = (-(ext(px, j, i + 1, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
     AT(xisu, j, i) = (-(ext(ps, j, i + 1, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
   }
@@ -305,7 +305,7 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
     int ii = icx_p(i, Nx);
     AT(xiew, j, i) = -(corner_avg(pe, j, ii + 1, Nz, Nx) - corner_avg(pe, j, ii, Nz, Nx));
     double a = AT(chiw, j, i), b = AT(muw, j, i);
-    double tap = (1.0 - exp((-a) / 1e-4)) * (1.0 - exp((-fmax(0.0, b - 0.4)) / 0.05));
+    double tap = (1.0 - exp((-a) / 1e-4)) * (1.0 - exp((-jmax(0.0, b - 0.4)) / 0.05));
     AT(xixw, j, i) = (-(ext(px, j + 1, i, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
     AT(xisw, j, i) = (-(ext(ps, j + 1, i, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
   }
@@ -385,12 +385,19 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
   for (int q = 0; q < 3; ++q) {
     XC_TRY(run_line_filter(*zf[q], CF(c, src[q]), mid, Nz, Nx, 0, s));
     XC_TRY(run_line_filter(*xf[q], CView{mid.p, Nz}, flt[q], Nz, Nx, 1, s));
-    CView raw = CF(c, src[q]), fv{flt[q].p, Nz};
-    XC_TRY(reduce_to(c, RED_SUM, raw, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 0, s, n, partials));
-    XC_TRY(reduce_to(c, RED_SUM, raw, CView{nullptr, 0}, st + 4 * q + 0, Nz, Nx, st + 4 * q + 1, s, 1.0, partials));
-    XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 2, s, n, partials));
-    XC_TRY(reduce_to(c, RED_SUM, fv, CView{nullptr, 0}, st + 4 * q + 2, Nz, Nx, st + 4 * q + 3, s, 1.0, partials));
   }
+  // the six means in one launch, then the six centred sums of squares
+  // (mean and corrected std of noise.jl:261-264)
+  RedJob means[6], devs[6];
+  for (int q = 0; q < 3; ++q) {
+    CView raw = CF(c, src[q]), fv{flt[q].p, Nz};
+    means[2 * q] = red_job(RED_SUM, raw, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 0, n);
+    means[2 * q + 1] = red_job(RED_SUM, fv, CView{nullptr, 0}, nullptr, Nz, Nx, st + 4 * q + 2, n);
+    devs[2 * q] = red_job(RED_SUM, raw, CView{nullptr, 0}, st + 4 * q + 0, Nz, Nx, st + 4 * q + 1);
+    devs[2 * q + 1] = red_job(RED_SUM, fv, CView{nullptr, 0}, st + 4 * q + 2, Nz, Nx, st + 4 * q + 3);
+  }
+  XC_TRY(reduce_batch(c, means, 6, s, partials));
+  XC_TRY(reduce_batch(c, devs, 6, s, partials));
   rescale_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(Nz, Nx, flt[0], flt[1], flt[2], st); xc_count_launch();
   XC_LAUNCH_CHECK();
   stagger_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, s>>>(

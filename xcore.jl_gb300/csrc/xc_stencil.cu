@@ -57,7 +57,7 @@ __device__ __forceinline__ double tvd_flux(double fm, double fc, double fp, doub
   double num = vm * (fc - fm);
   double den = vp * (fp - fc);
   double R = num / (den + copysign(XC_EPS, den));
-  double l = fmax(0.0, fmax(fmin(1.0, 2.0 * R), fmin(2.0, R)));
+  double l = jmax(0.0, jmax(jmin(1.0, 2.0 * R), jmin(2.0, R)));
   return fc + (0.5 * l) * (fp - fc);
 }
 

@@ -154,7 +154,7 @@ __global__ void drho_pressure_kernel(int Nz, int Nx, double Ptop, const double* 
   if (j < Nz) {
     double pl = plcol[j];
     AT(Pl, j, i) = pl;
-    AT(Pt, j, i) = fmax(Ptop / 100.0, pl + AT(P, j + 1, i + 1));
+    AT(Pt, j, i) = jmax(Ptop / 100.0, pl + AT(P, j + 1, i + 1));
   }
 }
 
@@ -240,7 +240,7 @@ __global__ void blend_segvisc_kernel(int Nz, int Nx, const double* min_etai, dou
   AT(ks, j, i) = k;
   AT(etat, j, i) = et;
   AT(kx, j, i) = k + AT(fReL, j, i) * AT(ke, j, i);
-  AT(Rc, j, i) = v / fmax(vxc, XC_EPS);
+  AT(Rc, j, i) = v / jmax(vxc, XC_EPS);
 }
 
 // cap + blend of etas and Red (update.jl:396-402)
@@ -314,7 +314,7 @@ __global__ void phase_velocities_kernel(int Nz, int Nx, int xBC, int zBC, double
     w = w * AT(bndtaperw, j, is);
     AT(wx, j, i) = w;
     int ci = icx_at(i, Nx, xBC);
-    double xe = AT(x_w, j, ci), me = fmax(AT(m_w, j, ci), XC_EPS);
+    double xe = AT(x_w, j, ci), me = jmax(AT(m_w, j, ci), XC_EPS);
     double wmv = ((-xe) / me) * w;
     AT(wm, j, i) = wmv;
     double sx = AT(xisw, j, i) + AT(xixw, j, i);
@@ -324,7 +324,7 @@ __global__ void phase_velocities_kernel(int Nz, int Nx, int xBC, int zBC, double
   }
   if (i <= Nx) {   // U-shaped (Nz+2, Nx+1)
     int cj = icz_at(j, Nz, zBC);
-    double xe = AT(x_u, cj, i), me = fmax(AT(m_u, cj, i), XC_EPS);
+    double xe = AT(x_u, cj, i), me = jmax(AT(m_u, cj, i), XC_EPS);
     double sx = AT(xisu, j, i) + AT(xixu, j, i);
     double Uv = AT(U, j, i), xe_u = AT(xieu, j, i);
     AT(Ux, j, i) = (Uv + sx) + xe_u;
@@ -475,35 +475,41 @@ static const CView kNone{nullptr, 0};
 
 int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out) {
   const int Nz = c->Nz, Nx = c->Nx;
-  XC_TRY(reduce_view(c, RED_MAX, whole(c, FLD_kx), kNone, Nz, Nx, SC_DT + 0));
-  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Wx), kNone, Nz + 1, Nx + 2, SC_DT + 1));
-  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Wm), kNone, Nz + 1, Nx + 2, SC_DT + 2));
-  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Ux), kNone, Nz + 2, Nx + 1, SC_DT + 3));
-  XC_TRY(reduce_view(c, RED_MAXABS, whole(c, FLD_Um), kNone, Nz + 2, Nx + 1, SC_DT + 4));
+  double* d = c->dscal + SC_DT;
+  const RedJob jobs[5] = {
+      red_job(RED_MAX, whole(c, FLD_kx), kNone, nullptr, Nz, Nx, d + 0),
+      red_job(RED_MAXABS, whole(c, FLD_Wx), kNone, nullptr, Nz + 1, Nx + 2, d + 1),
+      red_job(RED_MAXABS, whole(c, FLD_Wm), kNone, nullptr, Nz + 1, Nx + 2, d + 2),
+      red_job(RED_MAXABS, whole(c, FLD_Ux), kNone, nullptr, Nz + 2, Nx + 1, d + 3),
+      red_job(RED_MAXABS, whole(c, FLD_Um), kNone, nullptr, Nz + 2, Nx + 1, d + 4)};
+  XC_TRY(reduce_batch(c, jobs, 5, c->stream));
   XC_TRY(fetch_scalars(c, SC_DT, 5));
   const double* m = c->hscal + SC_DT;
   const double h = c->p.h;
+  // Julia's min / max (a NaN speed or diffusivity gives a NaN step)
   double dtk = (h / 2.0) * (h / 2.0) / m[0];
-  double vmax = std::fmax(std::fmax(std::fmax(m[1], m[2]), m[3]), m[4]) + XC_EPS;
+  double vmax = jmax(jmax(jmax(m[1], m[2]), m[3]), m[4]) + XC_EPS;
   double dta = (h / 2.0) / vmax;
-  *dt_out = std::fmin(std::fmin(1.5 * dt_prev, std::fmin(dtk, c->p.CFL * dta)), c->p.dtmax);
+  *dt_out = jmin(jmin(1.5 * dt_prev, jmin(dtk, c->p.CFL * dta)), c->p.dtmax);
   return XC_OK;
 }
 
 int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
   const int Nz = c->Nz, Nx = c->Nx;
-  const int b = SC_RESNORM;
-  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_rho), kNone, Nz, Nx, b + 0));
-  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_X), whole(c, FLD_res_Xo), Nz, Nx, b + 1));
-  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_MFS), whole(c, FLD_res_MFSo), Nz, Nx, b + 2));
-  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_W), whole(c, FLD_res_Wo), Nz + 1, Nx + 2, b + 3));
-  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_W), kNone, Nz + 1, Nx + 2, b + 4));
-  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_U), whole(c, FLD_res_Uo), Nz + 2, Nx + 1, b + 5));
-  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_U), kNone, Nz + 2, Nx + 1, b + 6));
-  XC_TRY(reduce_view(c, RED_SUMSQDIFF, whole(c, FLD_P), whole(c, FLD_res_Po), Nz + 2, Nx + 2, b + 7));
-  XC_TRY(reduce_view(c, RED_SUMSQ, whole(c, FLD_P), kNone, Nz + 2, Nx + 2, b + 8));
-  XC_TRY(fetch_scalars(c, b, 9));
-  const double* q = c->hscal + b;
+  double* d = c->dscal + SC_RESNORM;
+  const RedJob jobs[9] = {
+      red_job(RED_SUMSQ, whole(c, FLD_rho), kNone, nullptr, Nz, Nx, d + 0),
+      red_job(RED_SUMSQDIFF, whole(c, FLD_X), whole(c, FLD_res_Xo), nullptr, Nz, Nx, d + 1),
+      red_job(RED_SUMSQDIFF, whole(c, FLD_MFS), whole(c, FLD_res_MFSo), nullptr, Nz, Nx, d + 2),
+      red_job(RED_SUMSQDIFF, whole(c, FLD_W), whole(c, FLD_res_Wo), nullptr, Nz + 1, Nx + 2, d + 3),
+      red_job(RED_SUMSQ, whole(c, FLD_W), kNone, nullptr, Nz + 1, Nx + 2, d + 4),
+      red_job(RED_SUMSQDIFF, whole(c, FLD_U), whole(c, FLD_res_Uo), nullptr, Nz + 2, Nx + 1, d + 5),
+      red_job(RED_SUMSQ, whole(c, FLD_U), kNone, nullptr, Nz + 2, Nx + 1, d + 6),
+      red_job(RED_SUMSQDIFF, whole(c, FLD_P), whole(c, FLD_res_Po), nullptr, Nz + 2, Nx + 2, d + 7),
+      red_job(RED_SUMSQ, whole(c, FLD_P), kNone, nullptr, Nz + 2, Nx + 2, d + 8)};
+  XC_TRY(reduce_batch(c, jobs, 9, c->stream));
+  XC_TRY(fetch_scalars(c, SC_RESNORM, 9));
+  const double* q = c->hscal + SC_RESNORM;
   const double ep = XC_EPS;
   double nrho = std::sqrt(q[0]);
   double res_mass = std::sqrt(q[1]) / (nrho + ep) + std::sqrt(q[2]) / (nrho / dt + ep);
@@ -518,18 +524,19 @@ int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
 int sums_impl(xc_ctx* c, double out[12]) {
   const int Nz = c->Nz, Nx = c->Nx;
   const int b = SC_SUMS;
-  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_rho), kNone, Nz, Nx, b + 0));
-  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_M), kNone, Nz, Nx, b + 1));
-  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_X), kNone, Nz, Nx, b + 2));
-  XC_TRY(reduce_view(c, RED_SUM, whole(c, FLD_Gx), kNone, Nz, Nx, b + 3));
+  double* d = c->dscal + b;
+  RedJob jobs[12];
+  const int whole_f[4] = {FLD_rho, FLD_M, FLD_X, FLD_Gx};
+  for (int k = 0; k < 4; ++k) jobs[k] = red_job(RED_SUM, whole(c, whole_f[k]), kNone, nullptr, Nz, Nx, d + k);
   const int fl[4] = {FLD_qz_advn_X, FLD_qz_advn_M, FLD_qz_dffn_X, FLD_qz_dffn_M};
   for (int k = 0; k < 4; ++k) {
     CView q = CF(c, fl[k]);
     CView top{q.p + q.ld, q.ld};                 // row 0, columns 1..Nx
     CView bot{q.p + q.ld + Nz, q.ld};            // row Nz, columns 1..Nx
-    XC_TRY(reduce_view(c, RED_SUM, top, kNone, 1, Nx, b + 4 + 2 * k));
-    XC_TRY(reduce_view(c, RED_SUM, bot, kNone, 1, Nx, b + 5 + 2 * k));
+    jobs[4 + 2 * k] = red_job(RED_SUM, top, kNone, nullptr, 1, Nx, d + 4 + 2 * k);
+    jobs[5 + 2 * k] = red_job(RED_SUM, bot, kNone, nullptr, 1, Nx, d + 5 + 2 * k);
   }
+  XC_TRY(reduce_batch(c, jobs, 12, c->stream));
   XC_TRY(fetch_scalars(c, b, 12));
   const double* q = c->hscal + b;
   const double h = c->p.h, h2 = h * h;
@@ -551,31 +558,74 @@ int history_impl(xc_ctx* c, double out[58]) {
   cudaStream_t s = c->stream;
   double* d = c->tmp[7];    // 64 device scalars
   const CView none{nullptr, 0};
+  RedJob jobs[58];
   int k = 0;
   CView x = CF(c, FLD_x);
-  XC_TRY(reduce_to(c, RED_MIN, x, none, nullptr, Nz, Nx, d + k++, s));
-  XC_TRY(reduce_to(c, RED_SUM, x, none, nullptr, Nz, Nx, d + k++, s, n));
-  XC_TRY(reduce_to(c, RED_MAX, x, none, nullptr, Nz, Nx, d + k++, s));
-  XC_TRY(reduce_to(c, RED_SUM, x, none, d + 1, Nz, Nx, d + k++, s));      // sum (x - mean)^2
+  jobs[k] = red_job(RED_MIN, x, none, nullptr, Nz, Nx, d + k); ++k;
+  jobs[k] = red_job(RED_SUM, x, none, nullptr, Nz, Nx, d + k, n); ++k;
+  jobs[k] = red_job(RED_MAX, x, none, nullptr, Nz, Nx, d + k); ++k;
+  ++k;   // d[3]: sum (x - mean)^2, after the mean (second batch)
   const int rms_f[6] = {FLD_V, FLD_vx, FLD_vm, FLD_xie, FLD_xix, FLD_xis};
   for (int q = 0; q < 6; ++q) {
     CView f = CF(c, rms_f[q]);
-    XC_TRY(reduce_to(c, RED_MIN, f, none, nullptr, Nz, Nx, d + k++, s));
-    XC_TRY(reduce_to(c, RED_SUMSQ, f, none, nullptr, Nz, Nx, d + k++, s, n));
-    XC_TRY(reduce_to(c, RED_MAX, f, none, nullptr, Nz, Nx, d + k++, s));
+    jobs[k] = red_job(RED_MIN, f, none, nullptr, Nz, Nx, d + k); ++k;
+    jobs[k] = red_job(RED_SUMSQ, f, none, nullptr, Nz, Nx, d + k, n); ++k;
+    jobs[k] = red_job(RED_MAX, f, none, nullptr, Nz, Nx, d + k); ++k;
   }
   const int gm_f[12] = {FLD_Ra, FLD_Rc, FLD_ReD, FLD_Red, FLD_ks, FLD_ke, FLD_kx, FLD_eta, FLD_etamix,
                         FLD_etae, FLD_etas, FLD_etat};
   for (int q = 0; q < 12; ++q) {
     CView f = CF(c, gm_f[q]);
-    XC_TRY(reduce_to(c, RED_MIN, f, none, nullptr, Nz, Nx, d + k++, s));
-    XC_TRY(reduce_to(c, RED_SUMLOG, f, none, nullptr, Nz, Nx, d + k++, s, n));
-    XC_TRY(reduce_to(c, RED_MAX, f, none, nullptr, Nz, Nx, d + k++, s));
+    jobs[k] = red_job(RED_MIN, f, none, nullptr, Nz, Nx, d + k); ++k;
+    jobs[k] = red_job(RED_SUMLOG, f, none, nullptr, Nz, Nx, d + k, n); ++k;
+    jobs[k] = red_job(RED_MAX, f, none, nullptr, Nz, Nx, d + k); ++k;
   }
+  // first batch: everything but the std; the mean of x lands in d[1]
+  RedJob first[57];
+  int nf = 0;
+  for (int q = 0; q < 58; ++q)
+    if (q != 3) first[nf++] = jobs[q];
+  XC_TRY(reduce_batch(c, first, nf, s));
+  const RedJob dev = red_job(RED_SUM, x, none, d + 1, Nz, Nx, d + 3);
+  XC_TRY(reduce_batch(c, &dev, 1, s));
   XC_CUDA_TRY(cudaMemcpyAsync(out, d, sizeof(double) * 58, cudaMemcpyDeviceToHost, s));
   XC_CUDA_TRY(cudaStreamSynchronize(s));
   out[3] = std::sqrt(out[3] / (n - 1.0));
   for (int q = 0; q < 6; ++q) out[4 + 3 * q + 1] = std::sqrt(out[4 + 3 * q + 1]);
   for (int q = 0; q < 12; ++q) out[22 + 3 * q + 1] = std::exp(out[22 + 3 * q + 1]);
+  return XC_OK;
+}
+
+// The statistics print_step! prints beyond record_history!'s
+// (src/diagnose.jl:92-182), each on the raw field (the reference divides by a
+// scale before printing; min, max and geomean commute with that division):
+// m: min, mean, max; rho: min, geomean, max; V, vx, vm, xie, xix, xis: min,
+// geomean, max -- with _gm(A) = exp(sum(log(max(A, 1e-300))) / length(A))
+// (diagnose.jl:10).
+int print_stats_impl(xc_ctx* c, double out[24]) {
+  const int Nz = c->Nz, Nx = c->Nx;
+  const double n = (double)Nz * (double)Nx;
+  cudaStream_t s = c->stream;
+  double* d = c->tmp[7];
+  const CView none{nullptr, 0};
+  RedJob jobs[24];
+  int k = 0;
+  CView m = CF(c, FLD_m);
+  jobs[k] = red_job(RED_MIN, m, none, nullptr, Nz, Nx, d + k); ++k;
+  jobs[k] = red_job(RED_SUM, m, none, nullptr, Nz, Nx, d + k, n); ++k;
+  jobs[k] = red_job(RED_MAX, m, none, nullptr, Nz, Nx, d + k); ++k;
+  const int gm_f[7] = {FLD_rho, FLD_V, FLD_vx, FLD_vm, FLD_xie, FLD_xix, FLD_xis};
+  for (int q = 0; q < 7; ++q) {
+    CView f = CF(c, gm_f[q]);
+    jobs[k] = red_job(RED_MIN, f, none, nullptr, Nz, Nx, d + k); ++k;
+    jobs[k] = red_job(RED_SUMLOG, f, none, nullptr, Nz, Nx, d + k, n);
+    jobs[k].floor = 1e-300;
+    ++k;
+    jobs[k] = red_job(RED_MAX, f, none, nullptr, Nz, Nx, d + k); ++k;
+  }
+  XC_TRY(reduce_batch(c, jobs, k, s));
+  XC_CUDA_TRY(cudaMemcpyAsync(out, d, sizeof(double) * 24, cudaMemcpyDeviceToHost, s));
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int q = 0; q < 7; ++q) out[3 + 3 * q + 1] = std::exp(out[3 + 3 * q + 1]);
   return XC_OK;
 }

@@ -50,6 +50,14 @@ struct SolverStats
     iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
 end
 
+const MAX_SWEEPS = 64
+# mirrors xc_step_stats
+struct StepStats
+    resnorm::NTuple{64,Cdouble}; resnorm0::Cdouble; sweeps::Cint; solver_iterations::Cint
+    solver_rel_residual::Cdouble; dt_next::Cdouble; unconverged_solves::Cint; picard_converged::Cint
+end
+StepStats() = StepStats(ntuple(_ -> 0.0, MAX_SWEEPS), 0.0, 0, 0, 0.0, 0.0, 0, 0)
+
 mutable struct Context
     h::Ptr{Cvoid}
     Nz::Int
@@ -191,16 +199,52 @@ function history_stats(ctx::Context)
     return Dict(zip(HISTORY_KEYS, out))
 end
 
+# The statistics print_step! prints beyond record_history!'s (src/diagnose.jl:92-182),
+# on the raw fields (divide by the scales as print_step! does before printing)
+const PRINT_KEYS = vcat(["m_min", "m_mean", "m_max"],
+                        ["$(f)_$(s)" for f in ("rho", "V", "vx", "vm", "xie", "xix", "xis") for s in ("min", "gm", "max")])
+
+function print_step_stats(ctx::Context)
+    out = Vector{Cdouble}(undef, 24)
+    check(ccall((:xc_print_step_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), ctx.h, out))
+    return Dict(zip(PRINT_KEYS, out))
+end
+
+# the measured optimum of the 1024^2 time step: FP32 inner solves to a 5e-2
+# reduction in at most 30 iterations, one pressure-multigrid sweep
+step_solver_opts(solver::Symbol, rtol) =
+    SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 5e-2, 30,
+               0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+
+# status 2 (XC_NOT_CONVERGED) from a step means the step was completed but a
+# Stokes solve stopped at its cap: raise with the step statistics
+function check_step(status, st::StepStats)
+    status == 2 && error("xcore_gb300: " * unsafe_string(ccall((:xc_last_error, LIB), Cstring, ())) *
+                         " (unconverged solves: $(st.unconverged_solves))")
+    check(status)
+    return st
+end
+
+# one outer step of run! with `sweeps` Picard sweeps; returns the next dt
 function step!(ctx::Context, step::Integer, dt, re, rs; sweeps = 3, solver::Symbol = :mixed, rtol = 1e-9)
-    # the measured optimum of the 1024^2 time step: FP32 inner solves to a 5e-2
-    # reduction in at most 30 iterations, one pressure-multigrid sweep
-    o = SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 5e-2, 30,
-                   0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0)
-    st = Ref{NTuple{19,UInt64}}()   # xc_step_stats storage (152 bytes; dt_next is the last word)
-    check(ccall((:xc_step, LIB), Cint,
-                (Ptr{Cvoid}, Cint, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts}, Ptr{Cvoid}),
-                ctx.h, step, dt, sweeps, Matrix{Float64}(re), Matrix{Float64}(rs), o, st))
-    return reinterpret(Float64, collect(st[]))[end]
+    st = Ref(StepStats())
+    status = ccall((:xc_step, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts}, Ref{StepStats}),
+                   ctx.h, step, dt, sweeps, Matrix{Float64}(re), Matrix{Float64}(rs), step_solver_opts(solver, rtol), st)
+    return check_step(status, st[]).dt_next
+end
+
+# one outer step of run! with the reference's Picard loop (src/run.jl:220-250) and
+# its par.rtol, par.atol, par.maxit; returns (dt_next, sweeps)
+function step_converge!(ctx::Context, step::Integer, dt, re, rs, par; solver::Symbol = :mixed, rtol = 1e-9)
+    st = Ref(StepStats())
+    status = ccall((:xc_step_converge, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts},
+                    Ref{StepStats}),
+                   ctx.h, step, dt, par.rtol, par.atol, par.maxit, Matrix{Float64}(re), Matrix{Float64}(rs),
+                   step_solver_opts(solver, rtol), st)
+    s = check_step(status, st[])
+    return (s.dt_next, Int(s.sweeps))
 end
 
 end # module
