@@ -326,6 +326,53 @@ int xc_update_dt_noalloc(const double* kx, const double* Wx, const double* Wm, c
 int xc_time_coefs(int tint, int step, double out[6]);
 
 /* ------------------------------------------------------------------ */
+/* learned preconditioner network (no counterpart in the reference)    */
+/* ------------------------------------------------------------------ */
+/* One 3x3 convolution of the preconditioner's U-Net on the tensor cores,
+   on caller device pointers: y = relu?(conv3x3(x, w) + bias), BF16 operands,
+   FP32 accumulation, zero padding.  x: NHWC BF16 [B][H][W][Cin]; w: BF16
+   [Cout][9][Cin] (tap 3 (dy + 1) + (dx + 1)); bias: FP32 [Cout] or NULL;
+   y: NHWC BF16 [B][H][W][Cout] and/or y_f32 FP32 (either may be NULL).
+   Cin, Cout in {16, 32, 64, 128}; W a multiple of 128, or a power of two
+   below 128 with H a multiple of 128 / W; pointers 16-byte aligned.
+   Synchronises the stream; XC_TIMEOUT if a bounded wait in the kernel ran
+   out. */
+int xc_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, float* y_f32, int B, int H, int W,
+                  int Cin, int Cout, int relu, void* stream);
+/* Its weight gradient: dw (FP32 [Cout][9][Cin]) = sum over pixels p of
+   dy[p][co] * x[p + off(tap)][ci] (zero outside the image).  Same shapes and
+   rules; synchronises the stream. */
+int xc_nn_conv3x3_wgrad(const void* x, const void* dy, float* dw, int B, int H, int W, int Cin, int Cout,
+                        void* stream);
+
+/* The U-Net: 4 levels (16, 32, 64, 128 channels), two 3x3 convolutions with
+   ReLU per level on the way down, 2x2 average pooling, nearest upsampling of
+   a 3x3 convolution plus an additive skip and one 3x3 convolution with ReLU
+   per level on the way up, a final 3x3 convolution to FP32.  Inputs and
+   outputs are FP32 NHWC arrays [batch][H][W][in_ch] / [..][out_ch] on the
+   device; H, W multiples of 8 whose four levels tile into 128-pixel tiles
+   (e.g. 256, 512, 1024, 2048).  Weights start He-normal from `seed`. */
+typedef struct xc_nn xc_nn;
+int xc_nn_create(int H, int W, int batch, int in_ch, int out_ch, unsigned long long seed, xc_nn** out);
+int xc_nn_destroy(xc_nn* net);
+/* FP32 parameter count of the flat block [w_0 b_0 w_1 b_1 ...] (weights
+   [Cout][9][Cin] per layer, each block 16-byte aligned) */
+long long xc_nn_param_count(const xc_nn* net);
+/* per layer: weight and bias offsets into the block, and (Cin, Cout, level,
+   relu); 15 layers */
+int xc_nn_layout(const xc_nn* net, long long woff[15], long long boff[15], int spec[60]);
+int xc_nn_get_params(xc_nn* net, float* host);
+int xc_nn_set_params(xc_nn* net, const float* host);
+int xc_nn_get_grads(xc_nn* net, float* host);
+/* out = net(in); synchronises the stream (NULL = the network's own) */
+int xc_nn_forward(xc_nn* net, const float* in, float* out, void* stream);
+/* loss = mean over pixels of sum over out_ch of (net(in) - target)^2 and its
+   parameter gradient (xc_nn_get_grads); synchronises */
+int xc_nn_loss_grad(xc_nn* net, const float* in, const float* target, float* loss, void* stream);
+/* xc_nn_loss_grad followed by one Adam step (beta 0.9, 0.999) at rate lr */
+int xc_nn_train_step(xc_nn* net, const float* in, const float* target, float lr, float* loss, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* instrumentation (no counterpart in the reference)                   */
 /* ------------------------------------------------------------------ */
 /* The context's CUDA stream (cudaStream_t), for events recorded by a caller. */

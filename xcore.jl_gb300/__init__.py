@@ -175,6 +175,19 @@ def lib():
             "xc_launch_count": (ctypes.c_longlong, []),
             "xc_bench_kernel": (ip, [vp, ip, ip, D6]),
             "xc_update_dt_noalloc": (ip, [vp, vp, vp, vp, vp, ip, ip, dp, dp, dp, dp, vp, vp]),
+            "xc_nn_conv3x3": (ip, [vp, vp, vp, vp, vp, ip, ip, ip, ip, ip, ip, vp]),
+            "xc_nn_conv3x3_wgrad": (ip, [vp, vp, vp, ip, ip, ip, ip, ip, vp]),
+            "xc_nn_create": (ip, [ip, ip, ip, ip, ip, ctypes.c_ulonglong, ctypes.POINTER(vp)]),
+            "xc_nn_destroy": (ip, [vp]),
+            "xc_nn_param_count": (ctypes.c_longlong, [vp]),
+            "xc_nn_layout": (ip, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                  ctypes.POINTER(ip)]),
+            "xc_nn_get_params": (ip, [vp, vp]),
+            "xc_nn_set_params": (ip, [vp, vp]),
+            "xc_nn_get_grads": (ip, [vp, vp]),
+            "xc_nn_forward": (ip, [vp, vp, vp, vp]),
+            "xc_nn_loss_grad": (ip, [vp, vp, vp, ctypes.POINTER(ctypes.c_float), vp]),
+            "xc_nn_train_step": (ip, [vp, vp, vp, ctypes.c_float, ctypes.POINTER(ctypes.c_float), vp]),
             "xc_last_error": (ctypes.c_char_p, []),
             "xc_version": (ctypes.c_char_p, []),
         }
