@@ -38,6 +38,11 @@ def parse():
     ap.add_argument("--N", type=int, default=1024)
     ap.add_argument("--sweeps", type=int, default=3)
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fgmres64"])
+    ap.add_argument("--learned", type=int, default=-1,
+                    help="preconditioner of the mixed solver's FP32 inner solves: 0 multigrid, 1 the learned "
+                         "network in its place (multigrid fallback), 2 the network after the V-cycle; -1 "
+                         "(default): the learned mode the committed weights record as best, 0 without weights")
+    ap.add_argument("--weights", default=None, help="learned preconditioner parameters (.npz)")
     ap.add_argument("--rtol", type=float, default=1e-9)
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
@@ -242,6 +247,20 @@ def main():
         draws.append(pair)
     st.initialize(x0, draws[0][0], draws[0][1])
     sopt = dict(solver=a.solver, rtol=a.rtol, maxit=400, inner_rtol=5e-2, inner_maxit=30, pressure_sweeps=1)
+    # the learned preconditioner (committed weights, trained by xcore.jl_gb300/learned.py)
+    import xcore_gb300.learned as learned_mod
+    wpath = a.weights or learned_mod.WEIGHTS
+    learned_info = {"weights": None, "mode": 0}
+    if a.solver == "mixed" and os.path.exists(wpath) and a.learned != 0:
+        with np.load(wpath) as z:
+            best = int(z["best_mode"]) if "best_mode" in z.files else 2
+            learned_info.update({k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files if k != "params"})
+        mode = best if a.learned < 0 else a.learned
+        if mode > 0:
+            learned_mod.use(st, learned_mod.load_params(wpath))
+            sopt["learned"] = mode
+        learned_info["weights"] = os.path.relpath(wpath, ROOT)
+        learned_info["mode"] = mode
     for kv in a.knob:
         key, val = kv.split("=", 1)
         sopt[key] = float(val) if any(ch in val for ch in ".e") else int(val)
@@ -412,7 +431,7 @@ def main():
             "field_error_note": f"max-norm relative deviation of W, U, P, x after {a.plain_steps} steps from the "
                                 "same saved state: mixed solver vs the plain FP64 solver",
             "cpu_grid_gpu_timesteps_per_s": gpu_at_cpu_grid,
-            "learned_preconditioner": "not built",
+            "learned_preconditioner": learned_info,
             "cache": "working set (~2 GB of fields and solver vectors) exceeds L2 (129 MB); no flush needed",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         },

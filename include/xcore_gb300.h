@@ -128,6 +128,12 @@ typedef struct xc_solver_opts {
   int jacobi_coarse;       /* 1: Jacobi sweeps (coarse_sweeps) on the coarsest levels even where they
                               have at most 64 unknowns, which by default are solved with their
                               dense inverse (formed and inverted on the device once per solve) */
+  int learned;             /* mixed solver, plain refinement: preconditioner of the FP32 inner
+                              solves.  0 the multigrid V-cycles; 1 the learned network
+                              (xc_set_learned_preconditioner) in their place, an inner solve that
+                              misses inner_rtol redone with the multigrid; 2 the V-cycles followed
+                              by the network on the residual they leave.  The FP64 residual of
+                              the refinement judges every pass either way. */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {
@@ -136,6 +142,7 @@ typedef struct xc_solver_stats {
   double rel_residual;     /* final ||RR - LL x|| / ||RR|| of the scaled system, FP64 */
   int converged;           /* 1 when rel_residual <= rtol */
   double seconds;          /* device time of the solve */
+  int learned_fallbacks;   /* inner solves of the learned preconditioner redone with the multigrid */
 } xc_solver_stats;
 
 #define XC_MAX_SWEEPS 64
@@ -371,6 +378,27 @@ int xc_nn_forward(xc_nn* net, const float* in, float* out, void* stream);
 int xc_nn_loss_grad(xc_nn* net, const float* in, const float* target, float* loss, void* stream);
 /* xc_nn_loss_grad followed by one Adam step (beta 0.9, 0.999) at rate lr */
 int xc_nn_train_step(xc_nn* net, const float* in, const float* target, float lr, float* loss, void* stream);
+
+/* The learned preconditioner of a context's mixed Stokes solver (no
+   counterpart in the reference; it replaces, with the multigrid, the LU of
+   fluidmech.jl:512-523): a network of this context's grid size (Nz, Nx
+   tiling as xc_nn_create requires; in 4 channels, out 3) with the given
+   FP32 parameter block of xc_nn_param_count values (trained at any grid size:
+   the weights do not depend on it).  params = NULL removes it.  Selected per
+   solve by xc_solver_opts.learned. */
+int xc_set_learned_preconditioner(xc_ctx* ctx, const float* params, long long nparams);
+/* One training pair from the context's last FP64 fluidmech operator: v is a
+   device FP32 vector of the scaled saddle system (length NW + NU + NP, the
+   layout of W, U, P one after the other, column-major); the plain FP64 solver
+   (FGMRES with the multigrid preconditioner, from zero, to rtol, at most maxit
+   iterations) solves S LL S z = v; in = the network input [Nz][Nx][4] of v and
+   the viscosity, target = z on the interior unknowns [Nz][Nx][3] (device
+   FP32).  Synchronises; XC_NOT_CONVERGED when the solve missed rtol. */
+int xc_learned_sample(xc_ctx* ctx, const float* v, float* in, float* target, double rtol, int maxit,
+                      int* iterations);
+/* y = S LL S v with the context's last fluidmech operator (device FP32
+   vectors, applied in FP64); synchronises. */
+int xc_stokes_apply_scaled(xc_ctx* ctx, const float* v, float* y);
 
 /* ------------------------------------------------------------------ */
 /* instrumentation (no counterpart in the reference)                   */

@@ -108,7 +108,9 @@ def test_c2_identical_stokes_inputs_one_step(scheme):
 def _trajectory(cfg, scheme, name, steps, bound_fields, bound_dt):
     z = np.load(os.path.join(GOLD, name))
     par, g, sc, ns, x0, draws, (re0, rs0) = C.setup(cfg, scheme=scheme)
-    assert C.digest_error(C.digest(x0), z["x0_digest"]) == 0.0
+    # the same draws (the samples exactly; the norm and sums to the summation
+    # order of this host's numpy)
+    assert C.digest_error(C.digest(x0), z["x0_digest"]) <= 1e-13
     chk = float((re0 * re0).sum() + rs0.sum())
     ds = device_state(par, g, sc)
     ds.initialize(x0, re0, rs0)

@@ -83,7 +83,7 @@ class SolverOpts(ctypes.Structure):
                 ("tiled_sweep", ctypes.c_int), ("post_sweeps", ctypes.c_int), ("outer_solver", ctypes.c_int),
                 ("fused_pressure_cells", ctypes.c_int),
                 ("stage_small_levels", ctypes.c_int),
-                ("jacobi_coarse", ctypes.c_int)]
+                ("jacobi_coarse", ctypes.c_int), ("learned", ctypes.c_int)]
 
     @classmethod
     def make(cls, solver="fgmres64", rtol=1e-10, maxit=500, restart=30, inner_rtol=1e-4, inner_maxit=60,
@@ -91,19 +91,19 @@ class SolverOpts(ctypes.Structure):
              coarse_cells=0, coarse_sweeps=0, small_cells=0, pressure_sweeps=0, inner_gs_passes=0,
              serial_launch=False, coarse_viscosity_mean=0, tiled_sweep=False, post_sweeps=0, outer_solver=0,
              fused_pressure_cells=0, stage_small_levels=False,
-             jacobi_coarse=False):
+             jacobi_coarse=False, learned=0):
         return cls(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit),
                    int(smooth_sweeps), float(omega_velocity), float(schur_mass), int(bool(schur_full_diagonal)),
                    int(coarse_cells), int(coarse_sweeps), int(small_cells), int(pressure_sweeps),
                    int(inner_gs_passes), int(bool(serial_launch)), int(coarse_viscosity_mean),
                    int(bool(tiled_sweep)), int(post_sweeps), int(outer_solver),
                    int(fused_pressure_cells), int(bool(stage_small_levels)),
-                   int(bool(jacobi_coarse)))
+                   int(bool(jacobi_coarse)), int(learned))
 
 
 class SolverStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("refinements", ctypes.c_int), ("rel_residual", ctypes.c_double),
-                ("converged", ctypes.c_int), ("seconds", ctypes.c_double)]
+                ("converged", ctypes.c_int), ("seconds", ctypes.c_double), ("learned_fallbacks", ctypes.c_int)]
 
 
 MAX_SWEEPS = 64
@@ -188,6 +188,9 @@ def lib():
             "xc_nn_forward": (ip, [vp, vp, vp, vp]),
             "xc_nn_loss_grad": (ip, [vp, vp, vp, ctypes.POINTER(ctypes.c_float), vp]),
             "xc_nn_train_step": (ip, [vp, vp, vp, ctypes.c_float, ctypes.POINTER(ctypes.c_float), vp]),
+            "xc_set_learned_preconditioner": (ip, [vp, vp, ctypes.c_longlong]),
+            "xc_learned_sample": (ip, [vp, vp, vp, vp, dp, ip, ctypes.POINTER(ip)]),
+            "xc_stokes_apply_scaled": (ip, [vp, vp, vp]),
             "xc_last_error": (ctypes.c_char_p, []),
             "xc_version": (ctypes.c_char_p, []),
         }

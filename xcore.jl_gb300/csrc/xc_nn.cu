@@ -503,6 +503,13 @@ void init_params(xc_nn* n, unsigned long long seed, std::vector<float>& h) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// internal entry points (the Stokes solver's learned preconditioner)
+// ---------------------------------------------------------------------------
+int nn_forward_async(xc_nn* n, const float* in, cudaStream_t s) { return forward(n, in, s); }
+const float* nn_out16(const xc_nn* n) { return n->out16; }
+int nn_check(xc_nn* n, cudaStream_t s) { return check_err(n, s, "learned preconditioner"); }
+
+// ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" int xc_nn_create(int H, int W, int batch, int in_ch, int out_ch, unsigned long long seed, xc_nn** out) {

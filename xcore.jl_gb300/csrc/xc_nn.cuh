@@ -15,3 +15,12 @@ int nn_conv3x3_fwd(const void* x, const void* w, const float* bias, void* y, flo
 // accumulate); partial: FP32 scratch of partial_blocks * 9 * Cout * Cin
 int nn_conv3x3_wgrad(const void* x, const void* dy, float* dw, float* partial, int partial_blocks, int B, int H,
                      int W, int Cin, int Cout, float scale, int accumulate, int* err, cudaStream_t s);
+
+// the network on the stream without synchronising (graph capture allowed):
+// the FP32 result [npix][16] (first out_ch channels used) is nn_out16(n)
+struct xc_nn;
+int nn_forward_async(xc_nn* n, const float* in, cudaStream_t s);
+const float* nn_out16(const xc_nn* n);
+// wait for the stream and report a bounded wait that ran out inside a
+// convolution as XC_TIMEOUT
+int nn_check(xc_nn* n, cudaStream_t s);

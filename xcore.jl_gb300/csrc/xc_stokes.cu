@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "xc_internal.cuh"
+#include "xc_nn.cuh"
 
 namespace {
 
@@ -2001,6 +2002,43 @@ inline dim3 grid2(const Geo& g) { return dim3((unsigned)((g.Nz + 2 + 31) / 32), 
 
 }  // namespace
 
+namespace {
+
+struct SolveCfg {
+  double omega_v = 0.7, omega_p = 0.8;
+  int nu = 1;              // velocity pre-smoothing sweeps (and both on the one-CTA levels)
+  int nu_post = 2;         // velocity post-smoothing sweeps on the large levels
+  int coarse_sweeps = 0;   // 0: 4 * (Nz + Nx) of the coarsest level, at least 32
+  int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
+                           // solved by Jacobi sweeps
+  int small_cells = 256;   // levels of at most this many cells run in one CTA
+  int nu_p = 2;            // pressure smoothing sweeps before and after each coarse correction
+  int gs_passes = 2;       // classical Gram-Schmidt passes per Arnoldi step
+  bool pdl = true;         // programmatic dependent launch inside the captured graphs
+  bool tiled = false;      // FP32 sweeps from shared-memory tiles (opt-in, measured slower)
+  // Schur approximation (Cahouet-Chabard): S^-1 ~ L_in^-1 + cmass * eta/rho with
+  // L_in = DM diag(a1 rho/dt)^-1 GG (kplane 9); kplane 0 builds L from the full
+  // velocity diagonal instead (cmass then defaults to 0)
+  double cmass = 0.5;
+  int kplane = 9;
+  // pressure levels of at most this many cells use the fused descent /
+  // ascent kernels, larger ones one launch per operation (none by default:
+  // measured no faster at any level size, programmatic launch already hides
+  // the launches they save, and 1% slower on the fine levels)
+  long long pfuse_cells = 0;
+  // one-CTA levels staged in shared memory (off by default: measured 1.5%
+  // slower at 1024^2 -- the small levels' sweeps are bound by instruction
+  // latency on one SM, and their L1-resident loads gain nothing from it)
+  bool stage_small = false;
+  // coarsest levels of at most kDenseMax unknowns solved by their inverse
+  bool direct_coarse = true;
+  // FP32 inner solves: 0 multigrid preconditioner, 1 the learned network in
+  // its place, 2 the network applied to what the multigrid V-cycle leaves
+  int learned = 0;
+};
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // host-side solver state
 // ---------------------------------------------------------------------------
@@ -2047,10 +2085,13 @@ struct Hier {
   T* rv;          // preconditioner scratch (velocity part, physical)
   T* rp;          // preconditioner scratch (pressure, physical full layout)
   T* rin;         // interior pressure rhs
-  // one captured graph per Arnoldi index; rebuilt when the key changes
-  cudaGraphExec_t gexec[kMaxRestart];
-  long long gnodes[kMaxRestart];
-  unsigned long long gkey;
+  // captured graphs per Arnoldi index for two configuration keys (the
+  // learned preconditioner and its multigrid fallback alternate within one
+  // solve); the least recently used set is rebuilt when a third key appears
+  cudaGraphExec_t gexec[2][kMaxRestart];
+  long long gnodes[2][kMaxRestart];
+  unsigned long long gkey[2];
+  int glast;
 };
 
 struct StokesWork {
@@ -2073,6 +2114,16 @@ struct StokesWork {
   double *fz, *uz, *wz, *fx, *ux, *wx, *advz, *advx;
   double *srcw, *srcu, *srcp;
   cudaEvent_t ev0, ev1;
+  // learned preconditioner: the network sized for this grid, its input
+  // [Nz][Nx][4] (W, U, P components of the vector, log10(eta / etam0)), the
+  // log-viscosity channel of the current solve and the hybrid's residual
+  xc_nn* net;
+  float* nn_in;
+  float* nn_logeta;
+  float* nn_r;          // 2 n: the V-cycle's residual and A times the network's direction
+  float* nn_z;          // n: the network's direction
+  bool last_fp64_mg;    // the last solve set up the FP64 multigrid
+  SolveCfg last_cfg;
 };
 
 namespace {
@@ -2146,8 +2197,9 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
 
 template <typename T>
 void free_hier(Hier<T>& H) {
-  for (int q = 0; q < kMaxRestart; ++q)
-    if (H.gexec[q]) { cudaGraphExecDestroy(H.gexec[q]); H.gexec[q] = nullptr; }
+  for (int e = 0; e < 2; ++e)
+    for (int q = 0; q < kMaxRestart; ++q)
+      if (H.gexec[e][q]) { cudaGraphExecDestroy(H.gexec[e][q]); H.gexec[e][q] = nullptr; }
   for (int l = 0; l < H.nv; ++l) {
     cudaFree(H.cw[l]); cudaFree(H.cu[l]); cudaFree(H.vx[l]); cudaFree(H.vx2[l]); cudaFree(H.vb[l]); cudaFree(H.vr[l]);
     cudaFree(H.feta[l]); cudaFree(H.fetaco[l]); cudaFree(H.fdw[l]); cudaFree(H.fdu[l]); cudaFree(H.fdbot[l]);
@@ -2169,35 +2221,7 @@ VOp<T> vop(const Hier<T>& H, int l) {
   return o;
 }
 
-struct SolveCfg {
-  double omega_v = 0.7, omega_p = 0.8;
-  int nu = 1;              // velocity pre-smoothing sweeps (and both on the one-CTA levels)
-  int nu_post = 2;         // velocity post-smoothing sweeps on the large levels
-  int coarse_sweeps = 0;   // 0: 4 * (Nz + Nx) of the coarsest level, at least 32
-  int coarse_cells = 16;   // a velocity level of at most this many cells (pressure: a quarter) is
-                           // solved by Jacobi sweeps
-  int small_cells = 256;   // levels of at most this many cells run in one CTA
-  int nu_p = 2;            // pressure smoothing sweeps before and after each coarse correction
-  int gs_passes = 2;       // classical Gram-Schmidt passes per Arnoldi step
-  bool pdl = true;         // programmatic dependent launch inside the captured graphs
-  bool tiled = false;      // FP32 sweeps from shared-memory tiles (opt-in, measured slower)
-  // Schur approximation (Cahouet-Chabard): S^-1 ~ L_in^-1 + cmass * eta/rho with
-  // L_in = DM diag(a1 rho/dt)^-1 GG (kplane 9); kplane 0 builds L from the full
-  // velocity diagonal instead (cmass then defaults to 0)
-  double cmass = 0.5;
-  int kplane = 9;
-  // pressure levels of at most this many cells use the fused descent /
-  // ascent kernels, larger ones one launch per operation (none by default:
-  // measured no faster at any level size, programmatic launch already hides
-  // the launches they save, and 1% slower on the fine levels)
-  long long pfuse_cells = 0;
-  // one-CTA levels staged in shared memory (off by default: measured 1.5%
-  // slower at 1024^2 -- the small levels' sweeps are bound by instruction
-  // latency on one SM, and their L1-resident loads gain nothing from it)
-  bool stage_small = false;
-  // coarsest levels of at most kDenseMax unknowns solved by their inverse
-  bool direct_coarse = true;
-};
+
 
 // Jacobi sweeps on a coarsest level of Nz x Nx cells: a few times the grid's
 // diameter, enough for the smoothing to reach across the level
@@ -2471,6 +2495,136 @@ int dot_self(StokesWork* w, Hier<T>& H, const T* v, long long n, int slot, cudaS
   return XC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// learned preconditioner glue.  The network sees the grid's Nz x Nx cells as
+// an image (row j = z, column i = x) with four channels: the vector's W
+// component on the top face of the cell W(j, i+1), its U component on the
+// left face U(j+1, i), its P component P(j+1, i+1), and log10(eta / etam0).
+// Its three output channels give the correction on the interior unknowns
+// (W rows 1..Nz-1, U columns 0..Nx-1, interior P); every boundary, ghost and
+// duplicated-periodic unknown keeps the vector's own value (their scaled rows
+// are near identity).
+// ---------------------------------------------------------------------------
+__global__ void nn_logeta_kernel(int Nz, int Nx, const double* __restrict__ eta, double etam0, float* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)Nz * Nx) return;
+  const int j = (int)(t / Nx), i = (int)(t % Nx);
+  out[t] = (float)log10(eta[(size_t)i * Nz + j] / etam0);
+}
+
+// network input of a vector v: its components times scale (times 1/||v||
+// from the device when inv_norm is given).  Vectors of unit norm enter with
+// scale sqrt(Nz Nx), i.e. at O(1) per pixel.
+template <typename V>
+__global__ void nn_pack_kernel(Geo g, const V* __restrict__ v, const float* __restrict__ logeta,
+                               const double* __restrict__ inv_norm, float scale, float* in, int channels) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)g.Nz * g.Nx) return;
+  const int j = (int)(t / g.Nx), i = (int)(t % g.Nx);
+  const float sc = (inv_norm ? (float)*inv_norm : 1.0f) * scale;
+  float* o = in + t * channels;
+  o[0] = sc * (float)v[(size_t)(i + 1) * (g.Nz + 1) + j];
+  o[1] = sc * (float)v[(size_t)g.NW + (size_t)i * (g.Nz + 2) + j + 1];
+  o[2] = sc * (float)v[(size_t)g.NW + g.NU + (size_t)(i + 1) * (g.Nz + 2) + j + 1];
+  if (channels > 3) o[3] = logeta[t];
+}
+
+// image pixel and channel of unknown t, or -1 for the unknowns the network
+// does not correct
+__device__ __forceinline__ long long nn_pixel(const Geo& g, long long t, int* ch) {
+  if (t < g.NW) {
+    const int i = (int)(t / (g.Nz + 1)), j = (int)(t % (g.Nz + 1));
+    *ch = 0;
+    return (j >= 1 && j <= g.Nz - 1 && i >= 1 && i <= g.Nx) ? (long long)j * g.Nx + (i - 1) : -1;
+  }
+  t -= g.NW;
+  if (t < g.NU) {
+    const int i = (int)(t / (g.Nz + 2)), j = (int)(t % (g.Nz + 2));
+    *ch = 1;
+    return (j >= 1 && j <= g.Nz && i <= g.Nx - 1) ? (long long)(j - 1) * g.Nx + i : -1;
+  }
+  t -= g.NU;
+  const int i = (int)(t / (g.Nz + 2)), j = (int)(t % (g.Nz + 2));
+  *ch = 2;
+  return (j >= 1 && j <= g.Nz && i >= 1 && i <= g.Nx) ? (long long)(j - 1) * g.Nx + (i - 1) : -1;
+}
+
+// z = network output on the interior unknowns and `outside` elsewhere (zero
+// when outside is null)
+__global__ void nn_unpack_kernel(Geo g, const float* __restrict__ o16, const float* __restrict__ outside,
+                                 float* z) {
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  int ch = 0;
+  const long long p = nn_pixel(g, t, &ch);
+  z[t] = p >= 0 ? o16[p * 16 + ch] : (outside ? outside[t] : 0.0f);
+}
+
+// z += alpha n with alpha = dots[0] / dots[1] (the least-squares step of n
+// against the residual it targets; no step when dots[1] vanishes)
+__global__ void nn_axpy_kernel(long long n, const double* __restrict__ dots, const float* __restrict__ nz, float* z) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double den = dots[1];
+  const float alpha = den > 0.0 ? (float)(dots[0] / den) : 0.0f;
+  z[t] += alpha * nz[t];
+}
+
+// the training target: a scaled FP64 solution y on the interior unknowns,
+// [Nz][Nx][3] in the input's pixel layout
+__global__ void nn_target_kernel(Geo g, const double* __restrict__ y, float* out) {
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  int ch = 0;
+  const long long p = nn_pixel(g, t, &ch);
+  if (p >= 0) out[p * 3 + ch] = (float)y[t];
+}
+
+// z = M v for the configured preconditioner
+template <typename T>
+int apply_precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* v, T* out,
+                  cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (cfg.learned != 0) {
+      const Geo& g = w->g;
+      const long long n = (long long)g.NW + g.NU + g.NP;
+      const long long npx = (long long)g.Nz * g.Nx;
+      const float unit = sqrtf((float)npx);
+      if (cfg.learned == 1) {
+        // the network in place of the V-cycle (the Krylov vector has unit
+        // norm; FGMRES is indifferent to the scale of each z)
+        nn_pack_kernel<float><<<nblk(npx), 256, 0, s>>>(g, v, w->nn_logeta, nullptr, unit, w->nn_in, 4);
+        xc_count_launch();
+        XC_TRY(nn_forward_async(w->net, w->nn_in, s));
+        nn_unpack_kernel<<<nblk(n), 256, 0, s>>>(g, nn_out16(w->net), v, out); xc_count_launch();
+      } else {
+        // V-cycle; r = v - A z its residual (nn_r[0..n)); the network's
+        // direction for r, nz; A nz (nn_r[n..2n)); z += alpha nz with the
+        // least-squares alpha = (r . A nz) / (A nz . A nz)
+        float* r = w->nn_r;
+        float* anz = w->nn_r + n;
+        XC_TRY(precond<T>(w, H, k, cfg, v, out, s));
+        XC_TRY(apply_scaled<T>(w, H, k, out, v, r, s));
+        XC_TRY(dot_self<T>(w, H, r, n, 5, s));
+        nn_pack_kernel<float><<<nblk(npx), 256, 0, s>>>(g, r, w->nn_logeta, w->hdev + 6, unit, w->nn_in, 4);
+        xc_count_launch();
+        XC_TRY(nn_forward_async(w->net, w->nn_in, s));
+        nn_unpack_kernel<<<nblk(n), 256, 0, s>>>(g, nn_out16(w->net), nullptr, w->nn_z); xc_count_launch();
+        XC_TRY(apply_scaled<T>(w, H, k, w->nn_z, nullptr, anz, s));
+        double* dots = w->hdev + 8;   // free until this step's Gram-Schmidt
+        const int nb = launch_multidot<float>(n, 2, r, n, anz, w->part, s);
+        pdl(PDL_ON, multidot_final_kernel, 2, KB, s, 2, nb, w->part, dots);
+        nn_axpy_kernel<<<nblk(n), 256, 0, s>>>(n, dots, w->nn_z, out); xc_count_launch();
+      }
+      XC_LAUNCH_CHECK();
+      return XC_OK;
+    }
+  }
+  return precond<T>(w, H, k, cfg, v, out, s);
+}
+
 // The launches of one Arnoldi step k: z_k = M v_k; w = A z_k; two classical
 // Gram-Schmidt passes against v_0..v_k (coefficients to hdev[8..]); ||w||^2 to
 // hdev[2]; v_{k+1} = w / ||w||; the H column to the pinned host mirror.
@@ -2483,7 +2637,7 @@ int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg
   T* zk = H.Z + (size_t)kk * n;
   T* wv = H.V + (size_t)(kk + 1) * n;
   if (kk + 1 > 32) { xc_set_error("fgmres: restart above 32 basis vectors"); return XC_BAD_ARG; }
-  if (with_precond) XC_TRY(precond<T>(w, H, k, cfg, vk, zk, s));
+  if (with_precond) XC_TRY(apply_precond<T>(w, H, k, cfg, vk, zk, s));
   XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
   double* hd = w->hdev + 8;
   for (int pass = 0; pass < cfg.gs_passes; ++pass) {
@@ -2505,16 +2659,16 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0); mix((double)cfg.learned);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
 
 template <typename T>
-void drop_graphs(Hier<T>& H) {
+void drop_graphs(Hier<T>& H, int e) {
   for (int q = 0; q < kMaxRestart; ++q)
-    if (H.gexec[q]) { cudaGraphExecDestroy(H.gexec[q]); H.gexec[q] = nullptr; }
-  H.gkey = 0;
+    if (H.gexec[e][q]) { cudaGraphExecDestroy(H.gexec[e][q]); H.gexec[e][q] = nullptr; }
+  H.gkey[e] = 0;
 }
 
 // Arnoldi step kk as a CUDA graph captured on first use (the buffers are fixed
@@ -2522,26 +2676,34 @@ void drop_graphs(Hier<T>& H) {
 template <typename T>
 int arnoldi_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s) {
   const unsigned long long key = graph_key(k, cfg);
-  if (H.gkey != key) { drop_graphs(H); H.gkey = key; }
-  if (!H.gexec[kk]) {
+  int e = H.gkey[0] == key ? 0 : (H.gkey[1] == key ? 1 : -1);
+  if (e < 0) {
+    e = 1 - H.glast;   // replace the set used less recently
+    drop_graphs(H, e);
+    H.gkey[e] = key;
+  }
+  H.glast = e;
+  cudaGraphExec_t* gexec = H.gexec[e];
+  long long* gnodes = H.gnodes[e];
+  if (!gexec[kk]) {
     cudaGraph_t graph = nullptr;
     XC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     // launches recorded into the graph run only when it is launched: count
     // them from this thread's counter and take them out of the totals
     const long long before = g_xc_thread_launches;
     int st = arnoldi_launches<T>(w, H, k, cfg, kk, s);
-    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (st != XC_OK) { if (graph) cudaGraphDestroy(graph); return st; }
-    if (e != cudaSuccess) { xc_set_error("graph capture failed: %s", cudaGetErrorString(e)); return XC_CUDA; }
-    H.gnodes[kk] = g_xc_thread_launches - before;
+    if (ce != cudaSuccess) { xc_set_error("graph capture failed: %s", cudaGetErrorString(ce)); return XC_CUDA; }
+    gnodes[kk] = g_xc_thread_launches - before;
     g_xc_thread_launches = before;
-    g_xc_launches.fetch_sub(H.gnodes[kk]);
-    e = cudaGraphInstantiate(&H.gexec[kk], graph, 0);
+    g_xc_launches.fetch_sub(gnodes[kk]);
+    ce = cudaGraphInstantiate(&gexec[kk], graph, 0);
     cudaGraphDestroy(graph);
-    if (e != cudaSuccess) { H.gexec[kk] = nullptr; xc_set_error("graph instantiate: %s", cudaGetErrorString(e)); return XC_CUDA; }
+    if (ce != cudaSuccess) { gexec[kk] = nullptr; xc_set_error("graph instantiate: %s", cudaGetErrorString(ce)); return XC_CUDA; }
   }
-  XC_CUDA_TRY(cudaGraphLaunch(H.gexec[kk], s));
-  g_xc_launches.fetch_add(H.gnodes[kk]);
+  XC_CUDA_TRY(cudaGraphLaunch(gexec[kk], s));
+  g_xc_launches.fetch_add(gnodes[kk]);
   return XC_OK;
 }
 
@@ -2874,8 +3036,95 @@ void stokes_destroy(xc_ctx* c) {
   cudaFree(w->advz); cudaFree(w->advx); cudaFree(w->srcw); cudaFree(w->srcu); cudaFree(w->srcp);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
+  if (w->net) xc_nn_destroy(w->net);
+  cudaFree(w->nn_in); cudaFree(w->nn_logeta); cudaFree(w->nn_r); cudaFree(w->nn_z);
   delete w;
   c->stokes = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI of the learned preconditioner
+// ---------------------------------------------------------------------------
+static int nn_buffers(StokesWork* w) {
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  if (!w->nn_in) XC_CUDA_TRY(cudaMalloc(&w->nn_in, sizeof(float) * (size_t)g.Nz * g.Nx * 4));
+  if (!w->nn_logeta) XC_CUDA_TRY(cudaMalloc(&w->nn_logeta, sizeof(float) * (size_t)g.Nz * g.Nx));
+  if (!w->nn_r) XC_CUDA_TRY(cudaMalloc(&w->nn_r, sizeof(float) * 2 * n));
+  if (!w->nn_z) XC_CUDA_TRY(cudaMalloc(&w->nn_z, sizeof(float) * n));
+  return XC_OK;
+}
+
+extern "C" int xc_set_learned_preconditioner(xc_ctx* c, const float* params, long long nparams) {
+  if (!c || !c->stokes) { xc_set_error("xc_set_learned_preconditioner: no Stokes solver in this context"); return XC_BAD_ARG; }
+  StokesWork* w = c->stokes;
+  if (!params) {
+    if (w->net) xc_nn_destroy(w->net);
+    w->net = nullptr;
+    return XC_OK;
+  }
+  if (!w->net) XC_TRY(xc_nn_create(c->Nz, c->Nx, 1, 4, 3, 0, &w->net));
+  if (nparams != xc_nn_param_count(w->net)) {
+    xc_set_error("xc_set_learned_preconditioner: %lld parameters given, the network has %lld", nparams,
+                 xc_nn_param_count(w->net));
+    return XC_BAD_ARG;
+  }
+  XC_TRY(xc_nn_set_params(w->net, params));
+  XC_TRY(nn_buffers(w));
+  // the FP32 inner graphs of the next solve are captured with the network
+  return XC_OK;
+}
+
+extern "C" int xc_learned_sample(xc_ctx* c, const float* v, float* in, float* target, double rtol, int maxit,
+                                 int* iterations) {
+  if (!c || !c->stokes || !v || !in || !target) { xc_set_error("xc_learned_sample: null argument"); return XC_BAD_ARG; }
+  StokesWork* w = c->stokes;
+  if (!w->have_k || !w->last_fp64_mg) {
+    xc_set_error("xc_learned_sample: needs a previous FP64 fluidmech solve on this context (its operator and multigrid)");
+    return XC_BAD_ARG;
+  }
+  XC_TRY(nn_buffers(w));
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  const long long npx = (long long)g.Nz * g.Nx;
+  cudaStream_t s = c->stream;
+  nn_logeta_kernel<<<nblk(npx), 256, 0, s>>>(g.Nz, g.Nx, (const double*)c->field[FLD_eta], c->p.etam0,
+                                             w->nn_logeta);
+  xc_count_launch();
+  convert_kernel<float, double><<<nblk(n), 256, 0, s>>>(n, v, w->d.w); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  int its = 0;
+  double rr = 1.0;
+  XC_TRY(fgmres<double>(w, w->d, w->last_k, w->last_cfg, w->d.w, rtol, maxit, &its, &rr, s, FG_ZERO_GUESS));
+  // v enters at unit norm, as every Krylov vector does
+  XC_TRY(dot_self<double>(w, w->d, w->d.w, n, 5, s));
+  nn_pack_kernel<float><<<nblk(npx), 256, 0, s>>>(g, v, w->nn_logeta, w->hdev + 6, sqrtf((float)npx), in, 4);
+  xc_count_launch();
+  XC_CUDA_TRY(cudaMemsetAsync(target, 0, sizeof(float) * npx * 3, s));
+  nn_target_kernel<<<nblk(n), 256, 0, s>>>(g, w->d.y, target); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  if (iterations) *iterations = its;
+  if (!(rr <= rtol)) {
+    xc_set_error("xc_learned_sample: the FP64 solve stopped at %.3e after %d iterations", rr, its);
+    return XC_NOT_CONVERGED;
+  }
+  return XC_OK;
+}
+
+extern "C" int xc_stokes_apply_scaled(xc_ctx* c, const float* v, float* y) {
+  if (!c || !c->stokes || !v || !y) { xc_set_error("xc_stokes_apply_scaled: null argument"); return XC_BAD_ARG; }
+  StokesWork* w = c->stokes;
+  if (!w->have_k) { xc_set_error("xc_stokes_apply_scaled: needs a previous fluidmech solve"); return XC_BAD_ARG; }
+  const Geo& g = w->g;
+  const long long n = (long long)g.NW + g.NU + g.NP;
+  cudaStream_t s = c->stream;
+  convert_kernel<float, double><<<nblk(n), 256, 0, s>>>(n, v, w->d.w); xc_count_launch();
+  XC_TRY(apply_scaled<double>(w, w->d, w->last_k, w->d.w, nullptr, w->d.V, s));
+  convert_kernel<double, float><<<nblk(n), 256, 0, s>>>(n, w->d.V, y); xc_count_launch();
+  XC_LAUNCH_CHECK();
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  return XC_OK;
 }
 
 int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_opts* opts,
@@ -3000,9 +3249,32 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   // the FP64 solve keeps two
   SolveCfg icfg = cfg;
   icfg.gs_passes = o.inner_gs_passes >= 2 ? 2 : 1;
+  // learned preconditioner of the FP32 inner solves (plain refinement only)
+  SolveCfg icfg_nn = icfg;
+  if (o.learned != 0) {
+    if (o.learned != 1 && o.learned != 2) { xc_set_error("fluidmech: learned must be 0, 1 or 2"); return XC_BAD_ARG; }
+    if (o.kind != XC_SOLVER_MIXED || o.outer_solver == 1 || mms) {
+      xc_set_error("fluidmech: the learned preconditioner serves the mixed solver's plain refinement only");
+      return XC_BAD_ARG;
+    }
+    if (!w->net) {
+      xc_set_error("fluidmech: no learned preconditioner set (xc_set_learned_preconditioner)");
+      return XC_BAD_ARG;
+    }
+    icfg_nn.learned = o.learned;
+  }
   w->last_k = k;
   w->have_k = true;
+  w->last_cfg = cfg;
+  w->last_fp64_mg = o.kind != XC_SOLVER_MIXED;
   XC_TRY(setup_hier<double>(w, w->d, k, cfg, c, s, o.kind != XC_SOLVER_MIXED));
+  if (o.learned != 0) {
+    nn_logeta_kernel<<<nblk((long long)Nz * Nx), 256, 0, s>>>(Nz, Nx, (const double*)c->field[FLD_eta], p.etam0,
+                                                             w->nn_logeta);
+    xc_count_launch();
+    XC_LAUNCH_CHECK();
+  }
+  int fallbacks = 0;
   scl_kernel<<<nblk(n), 256, 0, s>>>(g, k, w->d.cw[0], w->d.cu[0], CF(c, FLD_rho), CF(c, FLD_eta), w->d.scl,
                                      w->d.etarho); xc_count_launch();
   XC_LAUNCH_CHECK();
@@ -3050,9 +3322,18 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       const float* frhs = w->f.w;
       int iits = 0;
       double irr = 1.0;
-      XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
-                           FG_ZERO_GUESS | FG_TRUST_EST, w->hhost[3]));
+      const double rn2 = w->hhost[3];
+      XC_TRY(fgmres<float>(w, w->f, k, o.learned ? icfg_nn : icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
+                           FG_ZERO_GUESS | FG_TRUST_EST, rn2));
       its += iits;
+      if (o.learned && !(irr <= o.inner_rtol)) {
+        // the learned inner solve missed its reduction: the multigrid
+        // preconditioner redoes this pass from zero
+        ++fallbacks;
+        XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
+                             FG_ZERO_GUESS | FG_TRUST_EST, rn2));
+        its += iits;
+      }
       refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
       XC_LAUNCH_CHECK();
     }
@@ -3083,7 +3364,9 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     stats->rel_residual = relres;
     stats->converged = relres <= o.rtol;
     stats->seconds = ms * 1e-3;
+    stats->learned_fallbacks = fallbacks;
   }
+  if (o.learned != 0) XC_TRY(nn_check(w->net, s));
   if (status != XC_OK) return status;
   if (!(relres <= o.rtol)) {
     xc_set_error("fluidmech: not converged, relative residual %.3e after %d iterations", relres, its);
