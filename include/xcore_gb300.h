@@ -178,6 +178,16 @@ int xc_field_id(const char* name);            /* -1 when unknown */
 int xc_field_shape(const xc_ctx* ctx, int id, int* rows, int* cols, int* elem_bytes);
 /* Device address of a field (column-major, leading dimension = rows). */
 int xc_field_device_ptr(const xc_ctx* ctx, int id, void** dev_ptr);
+/* Work in place on the caller's device array for field `id`: every later
+   call reads and writes dev_ptr (xc_field_shape's rows x cols, column-major,
+   16-byte aligned) instead of the context's own copy -- a CuArray of the
+   reference's FluidState / PhaseState (state.jl:74-258) bound field by field
+   makes the library a zero-copy drop-in on the caller's state.  The memory
+   stays the caller's: it must outlive the binding, and the library never
+   frees it.  dev_ptr = NULL unbinds (the context's own copy, with the values
+   it held before the binding, is used again).  Synchronises the context
+   first, so no queued work sees the switch. */
+int xc_field_bind(xc_ctx* ctx, int id, void* dev_ptr);
 /* Copy a whole field host -> device / device -> host (synchronous). */
 int xc_field_upload(xc_ctx* ctx, int id, const void* host);
 int xc_field_download(xc_ctx* ctx, int id, void* host);

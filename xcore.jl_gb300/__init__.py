@@ -142,6 +142,7 @@ def lib():
             "xc_field_id": (ip, [ctypes.c_char_p]),
             "xc_field_shape": (ip, [vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip), ctypes.POINTER(ip)]),
             "xc_field_device_ptr": (ip, [vp, ip, ctypes.POINTER(vp)]),
+            "xc_field_bind": (ip, [vp, ip, vp]),
             "xc_field_upload": (ip, [vp, ip, vp]),
             "xc_field_download": (ip, [vp, ip, vp]),
             "xc_synchronize": (ip, [vp]),
@@ -411,6 +412,19 @@ class State:
         p = ctypes.c_void_p()
         _check(lib().xc_field_device_ptr(self._h, self._ids[name], ctypes.byref(p)))
         return p.value
+
+    def bind(self, name, tensor):
+        """Work in place on a caller's CUDA tensor for field `name` (zero
+        copy): a contiguous tensor of shape (cols, rows) -- the field's
+        column-major bytes -- and its dtype (float64; uint8/bool for hasx,
+        hasm).  None unbinds.  The tensor must outlive the binding."""
+        if tensor is None:
+            _check(lib().xc_field_bind(self._h, self._ids[name], None))
+            return
+        (rows, cols), eb = self.shape(name)
+        if tuple(tensor.shape) != (cols, rows) or tensor.element_size() != eb or not tensor.is_contiguous():
+            raise ValueError(f"{name}: need a contiguous ({cols}, {rows}) tensor of {eb}-byte elements")
+        _check(lib().xc_field_bind(self._h, self._ids[name], ctypes.c_void_p(tensor.data_ptr())))
 
     def synchronize(self):
         _check(lib().xc_synchronize(self._h))

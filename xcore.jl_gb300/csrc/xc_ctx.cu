@@ -124,7 +124,7 @@ extern "C" int xc_ctx_create(const xc_params* par, xc_ctx** out) {
   }
   c->arena_bytes = total;
   if (cudaMemsetAsync(c->arena, 0, total, c->stream) != cudaSuccess) return fail(XC_CUDA);
-  for (int k = 0; k < FLD_COUNT; ++k) c->field[k] = c->arena + off[k];
+  for (int k = 0; k < FLD_COUNT; ++k) c->field[k] = c->own[k] = c->arena + off[k];
   for (int k = 0; k < 8; ++k) c->tmp[k] = (double*)(c->arena + tmp_off + k * tmpn);
   c->red_partials_len = reduce_partials_len();
   if (cudaMalloc(&c->red_partials, sizeof(double) * c->red_partials_len) != cudaSuccess ||
@@ -182,6 +182,28 @@ extern "C" int xc_field_device_ptr(const xc_ctx* c, int id, void** dev_ptr) {
   XC_TRY(check_ctx(c));
   if (id < 0 || id >= FLD_COUNT || !dev_ptr) { xc_set_error("bad field id %d", id); return XC_BAD_ARG; }
   *dev_ptr = c->field[id];
+  return XC_OK;
+}
+
+extern "C" int xc_field_bind(xc_ctx* c, int id, void* dev_ptr) {
+  XC_TRY(check_ctx(c));
+  if (id < 0 || id >= FLD_COUNT) { xc_set_error("xc_field_bind: bad field id %d", id); return XC_BAD_ARG; }
+  if (((uintptr_t)dev_ptr & 15u) != 0) {
+    xc_set_error("xc_field_bind: field %s: device pointer not 16-byte aligned", kFields[id].name);
+    return XC_BAD_ARG;
+  }
+  if (dev_ptr) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, dev_ptr) != cudaSuccess ||
+        (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+      cudaGetLastError();
+      xc_set_error("xc_field_bind: field %s: not a device pointer", kFields[id].name);
+      return XC_BAD_ARG;
+    }
+  }
+  XC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  XC_CUDA_TRY(cudaStreamSynchronize(c->side));
+  c->field[id] = dev_ptr ? dev_ptr : c->own[id];
   return XC_OK;
 }
 

@@ -148,6 +148,7 @@ struct xc_ctx {
   char* arena;
   size_t arena_bytes;
   void* field[FLD_COUNT];
+  void* own[FLD_COUNT];      // the context's own storage of each field (field[] may be bound elsewhere)
   Shape shape[FLD_COUNT];
   int elem[FLD_COUNT];
   // scratch

@@ -158,10 +158,11 @@ function fluidmech!(ctx::Context; dt, a1 = 1.0, a2 = 1.0, a3 = 0.0, b1 = 1.0, b2
 end
 
 function noise!(ctx::Context, dt; first_iter::Bool = true, re = nothing, rs = nothing)
-    pre = re === nothing ? C_NULL : pointer(Matrix{Float64}(re))
-    prs = rs === nothing ? C_NULL : pointer(Matrix{Float64}(rs))
+    # ccall keeps the converted arrays alive for the duration of the call
+    hre = re === nothing ? Ptr{Cdouble}(C_NULL) : Matrix{Float64}(re)
+    hrs = rs === nothing ? Ptr{Cdouble}(C_NULL) : Matrix{Float64}(rs)
     check(ccall((:xc_noise, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cint, Ptr{Cdouble}, Ptr{Cdouble}),
-                ctx.h, dt, first_iter, pre, prs))
+                ctx.h, dt, first_iter, hre, hrs))
 end
 
 update_phase_velocities!(ctx::Context) =
@@ -247,5 +248,96 @@ function step_converge!(ctx::Context, step::Integer, dt, re, rs, par; solver::Sy
     s = check_step(status, st[])
     return (s.dt_next, Int(s.sweeps))
 end
+
+# ---- call-site drop-in on CuArray-backed states -------------------------------------
+# With CUDA.jl loaded and the reference's FluidState / PhaseState built on
+# CuArrays (xcore_zeros with a CUDA backend, src/backend.jl:12-13), the methods
+# below give run! (src/run.jl:204-275) the GPU path with its calls unchanged:
+# each adds a method of the reference function for CuArray-backed states that
+# binds the structs' arrays to a context field by field (xc_field_bind, zero
+# copy; one context per PhaseState, cached) and calls the library.  The
+# NoiseState stays on the host -- its MersenneTwister draws the white noise
+# exactly as the reference does (noise.jl:154-157) -- while its time-evolving
+# fields live in the context (download! / upload! move them for checkpoints).
+using CUDA
+using Random
+
+const GPUFluid = xcore.FluidState{Float64,<:CuArray}
+const GPUPhase = xcore.PhaseState{Float64,<:CuArray}
+const BOUND = IdDict{Any,Context}()
+const BOUND_BC = IdDict{Any,NTuple{4,Int}}()   # (sds, top_cnv, bot_cnv, open_cnv) of each bound context
+
+function bind!(ctx::Context, name::Symbol, a::CuArray)
+    id = fieldid(name)
+    id < 0 && return
+    check(ccall((:xc_field_bind, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), ctx.h, id,
+                reinterpret(Ptr{Cvoid}, pointer(a))))
+end
+
+# the context whose fields are the arrays of (phase, fluid); created and bound
+# on first use with the run's boundary keywords
+function bound_context(phase::GPUPhase, fluid::GPUFluid, grid, par, scales; xBC = :periodic, zBC = :closed,
+                       sds = -1, top_cnv = 1, bot_cnv = 1, open_cnv = false)
+    get!(BOUND, phase) do
+        BOUND_BC[phase] = (sds, top_cnv, bot_cnv, Int(open_cnv))
+        ctx = Context(par, grid, scales; xBC, zBC, sds, top_cnv, bot_cnv, open_cnv)
+        foreach_field((n, v) -> v isa CuArray && bind!(ctx, n, v), fluid, phase)
+        ctx
+    end
+end
+function bound_context(phase::GPUPhase)
+    haskey(BOUND, phase) || error("XcoreGPU: no context bound to this PhaseState yet (call phsevo! or " *
+                                  "fluidmech! with its grid, par and scales first)")
+    return BOUND[phase]
+end
+
+function xcore.store_previous!(fluid::GPUFluid, phase::GPUPhase)
+    ctx = bound_context(phase)
+    store_previous!(ctx)
+    # run! calls store_noise!(ns) right after (run.jl:206-207); the noise
+    # history lives in the context, so it is stored here
+    store_noise!(ctx)
+end
+
+xcore.snapshot!(res, phase::GPUPhase, fluid::GPUFluid) = snapshot!(bound_context(phase))
+
+function xcore.phsevo!(phase::GPUPhase, fluid::GPUFluid, grid, par, scales; ADVN = par.ADVN, xBC = :periodic,
+                       zBC = :closed, a1, a2, a3, b1, b2, b3, dt, alpha = par.alpha)
+    ctx = bound_context(phase, fluid, grid, par, scales; xBC, zBC)
+    phsevo!(ctx; ADVN, a1, a2, a3, b1, b2, b3, dt, alpha)
+end
+
+function xcore.fluidmech!(fluid::GPUFluid, grid, par; phase::GPUPhase, sds = -1, top_cnv = 1, bot_cnv = 1,
+                          open_cnv = false, xBC = :periodic, zBC = :closed, dt = 1e32, a1 = 1.0, a2 = 1.0,
+                          a3 = 0.0, b1 = 1.0, b2 = 0.0, b3 = 0.0)
+    # run! calls phsevo! first in every sweep, which binds the context; the
+    # Stokes boundary keywords are the context's (call bound_context with
+    # them before run! when they are not the defaults)
+    ctx = bound_context(phase)
+    BOUND_BC[phase] == (sds, top_cnv, bot_cnv, Int(open_cnv)) ||
+        error("XcoreGPU.fluidmech!: boundary keywords differ from the bound context's $(BOUND_BC[phase])")
+    s = Ref{SolverStats}()
+    check(ccall((:xc_fluidmech, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cdouble, Ref{SolverOpts}, Ref{SolverStats}),
+                ctx.h, coefs(a1, a2, a3, b1, b2, b3), dt, step_solver_opts(:mixed, 1e-9), s))
+    return nothing
+end
+
+function xcore.noise!(ns, phase::GPUPhase, grid, par, scales, dt; first_iter::Bool = true)
+    ctx = bound_context(phase)
+    if first_iter
+        randn!(ns.rng, ns.re)
+        randn!(ns.rng, ns.rs)
+        noise!(ctx, dt; first_iter = true, re = ns.re, rs = ns.rs)
+    else
+        noise!(ctx, dt; first_iter = false)
+    end
+end
+
+xcore.update_phase_velocities!(phase::GPUPhase, fluid::GPUFluid, ns, grid, par; xBC = :periodic, zBC = :closed) =
+    update_phase_velocities!(bound_context(phase))
+xcore.update!(phase::GPUPhase, fluid::GPUFluid, grid, par, scales; xBC = :periodic, zBC = :closed) =
+    update!(bound_context(phase))
+xcore.compute_resnorm(res, phase::GPUPhase, fluid::GPUFluid, dt) = compute_resnorm(bound_context(phase), dt)
+xcore.update_dt(phase::GPUPhase, fluid::GPUFluid, grid, par, dt_prev) = update_dt(bound_context(phase), dt_prev)
 
 end # module
