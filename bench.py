@@ -44,7 +44,8 @@ def parse():
                          "(default): the learned mode the committed weights record as best, 0 without weights")
     ap.add_argument("--weights", default=None, help="learned preconditioner parameters (.npz)")
     ap.add_argument("--rtol", type=float, default=1e-9)
-    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--plain-steps", type=int, default=None,
+                    help="time steps of the plain FP64 comparison loop (default: --steps, the same steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--roofline-kernel", type=int, default=2)
     ap.add_argument("--knob", action="append", default=[],
@@ -220,6 +221,8 @@ def gpu_steps_per_second(xc, N, sweeps, steps, sopt, seed=5):
 
 def main():
     a = parse()
+    if a.plain_steps is None:
+        a.plain_steps = a.steps
     if a.impl == "reference":
         return run_reference(a)
     import torch
@@ -235,7 +238,8 @@ def main():
     par = workload_params(N)
     st = xc.State(par)
     x0, rng = initial_fields(N, seed=1234 + rank)
-    nstep_total = a.warmup + a.steps + a.steps + a.plain_steps
+    # every timed loop replays draws k0, k0 + 1, ... of the same saved state
+    nstep_total = a.warmup + max(a.steps, a.plain_steps)
     # white-noise draws for every step, in pinned host memory laid out column-major
     draws = []
     for _ in range(nstep_total + 1):
@@ -377,8 +381,8 @@ def main():
     achieved = rk[1] / (rk[0] * 1e-3) / 1e9
     # DRAM bytes (read + write) per cell of one launch, measured by one ncu
     # capture of each kernel on this workload at 1024^2, scaled to this grid
-    ncu_bytes_per_cell = {0: 25.23e6 / 1048576, 1: (235.73e6 + 18.77e6) / 1048576, 2: 33.64e6 / 1048576,
-                          3: (185.02e6 + 11.52e6) / 1048576, 4: 8.43e6 / 1048576}
+    ncu_bytes_per_cell = {0: 25.23e6 / 1048576, 1: (235.73e6 + 18.77e6) / 1048576,
+                          3: (185.02e6 + 11.52e6) / 1048576, 4: 8.43e6 / 1048576, 5: 33.64e6 / 1048576}
     traffic = ncu_bytes_per_cell[a.roofline_kernel] * rk[3] if a.roofline_kernel in ncu_bytes_per_cell else None
     ms_t = torch.tensor([ms, ms_e2e, ms_plain or 0.0], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -399,7 +403,10 @@ def main():
                          + cpu_note(CPU_GRID)}
         gpu_at_cpu_grid = gpu_steps_per_second(xc, CPU_GRID, a.sweeps, 10, sopt)
     names = {0: "advect_tile_kernel (WENO5, one field)", 1: "stokes_apply_kernel<double>",
-             2: "vel_sweep2d_kernel<float,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
+             2: "vel_sweep_rb_kernel<1> (finest-level FP32 velocity Jacobi sweep, four rows along z per thread; "
+                "operand copies exceed 2x L2)",
+             5: "vel_sweep2d_kernel<float,1> (finest-level FP32 velocity Jacobi sweep, one row per thread; operand "
+                "copies exceed 2x L2)",
              3: "vel_sweep2d_kernel<double,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
              4: "line_filter_kernel (FFT z pass)"}
     out = {

@@ -477,7 +477,7 @@ int noise_bench_zpass(xc_ctx* c, int iters, double out[4]);
 extern "C" int xc_bench_kernel(xc_ctx* c, int which, int iters, double out[4]) {
   XC_TRY(check_ctx(c));
   if (!out || iters < 1) { xc_set_error("xc_bench_kernel: bad arguments"); return XC_BAD_ARG; }
-  if (which == 1 || which == 2 || which == 3) return stokes_bench(c, which, iters, out);
+  if (which == 1 || which == 2 || which == 3 || which == 5) return stokes_bench(c, which, iters, out);
   if (which == 4) return noise_bench_zpass(c, iters, out);
   if (which != 0) { xc_set_error("xc_bench_kernel: unknown kernel %d", which); return XC_BAD_ARG; }
   const int Nz = c->Nz, Nx = c->Nx;

@@ -611,6 +611,119 @@ __global__ void __launch_bounds__(256) vel_sweep2d_kernel(Geo g, OpConst k, VOp<
 }
 
 
+// FP32 sweep (all MODEs of vel_sweep2d_kernel) with each thread taking kRB
+// consecutive rows along z of one column i, W and U rows alike.  Threads whose
+// rows are all interior (W rows 1..Nz-1, U rows 1..Nz, columns 1..Nx-1, no
+// MMS pin) take a path without any boundary classification or periodic wrap,
+// and vertically adjacent rows share their loads: the W rows' lower corner
+// and cell viscosities are the next row's upper ones, the U rows reuse the W
+// rows' corner and cell values of the same column, and the unknowns of the
+// column are loaded once for both row kinds.  Per row the weights and the
+// products are those of vel_update_w / vel_update_u in the same order.  Other
+// threads run those per-row bodies.
+constexpr int kRB = 4;
+
+template <int MODE>
+__device__ __forceinline__ void rb_store(float* out, long long t, float xc, float bt, float ax, float d,
+                                         float omega, const float* dscl) {
+  if (MODE == 2) out[t] = bt - ax;
+  else if (MODE == 3) out[t] = (xc + sdiv<float>(omega * (bt - ax), d)) / dscl[t];
+  else out[t] = xc + sdiv<float>(omega * (bt - ax), d);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) vel_sweep_rb_kernel(Geo g, OpConst k, VOp<float> op,
+                                                          const float* __restrict__ xi,
+                                                          const float* __restrict__ b, float* out, float omega,
+                                                          const float* __restrict__ dscl) {
+  XC_PDL_WAIT();
+  const int j0 = (blockIdx.x * 32 + threadIdx.x) * kRB;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  const int Nz = g.Nz, Nx = g.Nx, lw = Nz + 1, lu = Nz + 2;
+  const bool interior = !k.mms && j0 >= 1 && j0 + kRB - 1 <= Nz - 1 && i >= 1 && i <= Nx - 1;
+  if (!interior) {
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) {
+      const int j = j0 + r;
+      if (j <= Nz && i <= Nx + 1)
+        vel_update_w<float, MODE>(g, k, op, xi, b, out, omega, (long long)i * lw + j, j, i, dscl);
+      if (j <= Nz + 1 && i <= Nx)
+        vel_update_u<float, MODE>(g, k, op, xi, b, out, omega, (long long)i * lu + j, j, i, dscl);
+    }
+    return;
+  }
+  const float ih2 = g.ih2f;
+  const float* xw = xi;
+  const float* xu = xi + g.NW;
+  // viscosities: corners of columns i-1 (W rows' C1) and i (W rows' C2, U
+  // rows' C1 / C2) at z = j0-1 .. j0+kRB-1; cells of columns i-1 and i at
+  // z = j0-1 .. j0+kRB-1
+  float ca[kRB + 1], cb[kRB + 1], pa[kRB + 1], pb[kRB + 1];
+#pragma unroll
+  for (int r = 0; r <= kRB; ++r) {
+    ca[r] = op.etaco[(i - 1) * lw + j0 - 1 + r];
+    cb[r] = op.etaco[i * lw + j0 - 1 + r];
+    pa[r] = op.eta[(i - 1) * Nz + j0 - 1 + r];
+    pb[r] = op.eta[i * Nz + j0 - 1 + r];
+  }
+  // W rows (j, i), j = j0 + r: C1 = corner (j, i-1), C2 = corner (j, i),
+  // P1 = cell (j-1, i-1), P2 = cell (j, i-1)
+  {
+    const long long t0 = (long long)i * lw + j0;
+    const float* pw = xw + t0;
+    const float* pu = xu + ((i - 1) * lu + j0);
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) {
+      const long long t = t0 + r;
+      const RowW<float> c = fly_row<float>(ca[r + 1], cb[r + 1], pa[r], pa[r + 1], op.dw[t], ih2);
+      if (MODE == 0) {
+        out[t] = sdiv<float>(omega * b[t], c.d);
+        continue;
+      }
+      float sum = c.d * pw[r];
+      sum += c.c1 * pw[r - 1];
+      sum += c.c2 * pw[r + 1];
+      sum += c.c3 * pw[r - lw];
+      sum += c.c4 * pw[r + lw];
+      sum += c.c5 * pu[r];
+      sum += c.c6 * pu[r + 1];
+      sum += c.c7 * pu[r + lu];
+      sum += c.c8 * pu[r + lu + 1];
+      rb_store<MODE>(out, t, pw[r], b[t], sum, c.d, omega, dscl);
+    }
+  }
+  // U rows (j, i): C1 = corner (j-1, i), C2 = corner (j, i), P1 = cell (j-1,
+  // i-1), P2 = cell (j-1, i); no periodic wrap for 1 <= i <= Nx-1
+  {
+    const long long u0 = (long long)i * lu + j0;
+    const float* pu = xu + u0;
+    const float* pw = xw + (i * lw + j0 - 1);
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) {
+      const long long u = u0 + r;
+      const RowW<float> c = fly_row<float>(cb[r], cb[r + 1], pa[r], pb[r], op.du[u], ih2);
+      if (MODE == 0) {
+        out[g.NW + u] = sdiv<float>(omega * b[g.NW + u], c.d);
+        continue;
+      }
+      float sum = c.d * pu[r];
+      sum += c.c1 * pu[r - lu];
+      sum += c.c2 * pu[r + lu];
+      sum += c.c3 * pu[r - 1];
+      sum += c.c4 * pu[r + 1];
+      sum += c.c5 * pw[r];
+      sum += c.c6 * pw[r + lw];
+      sum += c.c7 * pw[r + 1];
+      sum += c.c8 * pw[r + lw + 1];
+      rb_store<MODE>(out, g.NW + u, pu[r], b[g.NW + u], sum, c.d, omega, dscl);
+    }
+  }
+}
+
+inline dim3 grid_rb(const Geo& g) {
+  return dim3((unsigned)((g.Nz + 2 + 32 * kRB - 1) / (32 * kRB)), (unsigned)((g.Nx + 2 + 7) / 8));
+}
+
 // FP32 sweep (MODE 1, 2, 3 of vel_sweep2d_kernel) of a block from shared
 // memory.  A 32 x 8 block stages the W and U unknowns and the cell and corner
 // viscosities of its rows with a one-row and one-column halo (34 x 10 each)
@@ -2035,6 +2148,8 @@ struct SolveCfg {
   // FP32 inner solves: 0 multigrid preconditioner, 1 the learned network in
   // its place, 2 the network applied to what the multigrid V-cycle leaves
   int learned = 0;
+  // FP32 velocity sweeps with four rows along z per thread (vel_sweep_rb_kernel)
+  bool row_block = true;
 };
 
 }  // namespace
@@ -2249,9 +2364,13 @@ static int coarse_threads(long long n) { return n > 512 ? 1024 : (n > 128 ? 256 
 template <typename T, int MODE>
 void launch_sweep(const SolveCfg& cfg, const Geo& g, const OpConst& k, const VOp<T>& op, const T* xi, const T* b,
                   T* out, T om, const T* dscl, cudaStream_t s) {
-  if constexpr (kFly<T> && MODE != 0) {
-    if (cfg.tiled) {
+  if constexpr (kFly<T>) {
+    if (MODE != 0 && cfg.tiled) {
       pdl(PDL_ON, vel_sweep_tiled_kernel<MODE>, grid2(g), blk2(), s, g, k, op, xi, b, out, om, dscl);
+      return;
+    }
+    if (cfg.row_block) {
+      pdl(PDL_ON, vel_sweep_rb_kernel<MODE>, grid_rb(g), blk2(), s, g, k, op, xi, b, out, om, dscl);
       return;
     }
   }
@@ -2659,7 +2778,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0); mix((double)cfg.learned);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0); mix((double)cfg.learned); mix(cfg.row_block ? 1.0 : 0.0);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -3240,6 +3359,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.pressure_sweeps > 0) cfg.nu_p = o.pressure_sweeps;
   cfg.pdl = !o.serial_launch;
   cfg.tiled = o.tiled_sweep != 0;
+  cfg.row_block = o.row_sweep == 0;
   cfg.stage_small = o.stage_small_levels != 0;
   cfg.direct_coarse = !o.jacobi_coarse;
   if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;
@@ -3381,7 +3501,8 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
 // together exceed twice the L2: launches cycle through the copies back to back,
 // so each reads operands the others have evicted and no launch gap is timed.
 template <typename T>
-int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H, int iters, float* ms_out) {
+int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H, int iters, float* ms_out,
+                bool row_block = false) {
   const size_t nvv = (size_t)g.NW + g.NU;
   std::vector<std::pair<const void*, size_t>> src;   // operand, bytes
   if (kFly<T>) {
@@ -3426,6 +3547,15 @@ int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H
     for (int it = -nc; it < iters; ++it) {   // one untimed pass over all copies first
       if (it == 0) cudaEventRecord(e0, s);
       const int q = ((it % nc) + nc) % nc;
+      if constexpr (kFly<T>) {
+        if (row_block) {
+          vel_sweep_rb_kernel<1><<<grid_rb(g), blk2(), 0, s>>>(g, k, op_of(q), (const T*)cp[q][xo],
+                                                               (const T*)cp[q][xo + 1], (T*)cp[q][xo + 2], (T)0.7,
+                                                               (const T*)nullptr);
+          xc_count_launch();
+          continue;
+        }
+      }
       vel_sweep2d_kernel<T, 1><<<grid2(g), blk2(), 0, s>>>(g, k, op_of(q), (const T*)cp[q][xo],
                                                            (const T*)cp[q][xo + 1], (T*)cp[q][xo + 2], (T)0.7,
                                                            (const T*)nullptr);
@@ -3450,7 +3580,7 @@ int sweep_bench(cudaStream_t s, const Geo& g, const OpConst& k, const Hier<T>& H
 
 int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   StokesWork* w = c->stokes;
-  if (!w || !w->have_k || (which == 2 && !w->f_alloc)) {
+  if (!w || !w->have_k || ((which == 2 || which == 5) && !w->f_alloc)) {
     xc_set_error("xc_bench_kernel: run xc_fluidmech (mixed for kernel 2) first");
     return XC_BAD_ARG;
   }
@@ -3462,12 +3592,13 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   // unknowns and the right-hand side (W, U, bW, bU for a sweep) and the
   // operator's material fields (eta, etaco, rho, rhow, rhou), write the
   // result: 11 arrays, FP64 88 B/cell, FP32 44 B/cell
-  out[1] = (which == 2 ? 44.0 : 88.0) * cells;
+  out[1] = (which == 2 || which == 5 ? 44.0 : 88.0) * cells;
   out[2] = 52.0 * cells;            // 2 flops per stencil entry, ~26 entries per cell
   out[3] = cells;
-  if (which == 2 || which == 3) {
+  if (which == 2 || which == 3 || which == 5) {
     float ms = 0;
-    XC_TRY(which == 2 ? sweep_bench<float>(s, g, k, w->f, iters, &ms) : sweep_bench<double>(s, g, k, w->d, iters, &ms));
+    XC_TRY(which == 3 ? sweep_bench<double>(s, g, k, w->d, iters, &ms)
+                      : sweep_bench<float>(s, g, k, w->f, iters, &ms, which == 2));
     out[0] = ms;
     return XC_OK;
   }
