@@ -401,13 +401,16 @@ int xc_nn_train_step(xc_nn* net, const float* in, const float* target, float lr,
 int xc_set_learned_preconditioner(xc_ctx* ctx, const float* params, long long nparams);
 /* One training pair from the context's last FP64 fluidmech operator: v is a
    device FP32 vector of the scaled saddle system (length NW + NU + NP, the
-   layout of W, U, P one after the other, column-major); the plain FP64 solver
-   (FGMRES with the multigrid preconditioner, from zero, to rtol, at most maxit
-   iterations) solves S LL S z = v; in = the network input [Nz][Nx][4] of v and
-   the viscosity, target = z on the interior unknowns [Nz][Nx][3] (device
-   FP32).  Synchronises; XC_NOT_CONVERGED when the solve missed rtol. */
-int xc_learned_sample(xc_ctx* ctx, const float* v, float* in, float* target, double rtol, int maxit,
-                      int* iterations);
+   layout of W, U, P one after the other, column-major).  The right-hand side
+   r is v itself, or with after_vcycle = 1 the residual v - S LL S M(v) that
+   one FP64 V-cycle M of the multigrid preconditioner leaves; the plain FP64
+   solver (FGMRES with the multigrid preconditioner, from zero, to rtol, at
+   most maxit iterations) solves S LL S z = r; in = the network input
+   [Nz][Nx][4] of r (at unit norm) and the viscosity, target = z on the
+   interior unknowns [Nz][Nx][3] (device FP32).  Synchronises;
+   XC_NOT_CONVERGED when the solve missed rtol. */
+int xc_learned_sample(xc_ctx* ctx, const float* v, int after_vcycle, float* in, float* target, double rtol,
+                      int maxit, int* iterations);
 /* y = S LL S v with the context's last fluidmech operator (device FP32
    vectors, applied in FP64); synchronises. */
 int xc_stokes_apply_scaled(xc_ctx* ctx, const float* v, float* y);

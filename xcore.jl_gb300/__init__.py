@@ -190,7 +190,7 @@ def lib():
             "xc_nn_loss_grad": (ip, [vp, vp, vp, ctypes.POINTER(ctypes.c_float), vp]),
             "xc_nn_train_step": (ip, [vp, vp, vp, ctypes.c_float, ctypes.POINTER(ctypes.c_float), vp]),
             "xc_set_learned_preconditioner": (ip, [vp, vp, ctypes.c_longlong]),
-            "xc_learned_sample": (ip, [vp, vp, vp, vp, dp, ip, ctypes.POINTER(ip)]),
+            "xc_learned_sample": (ip, [vp, vp, ip, vp, vp, dp, ip, ctypes.POINTER(ip)]),
             "xc_stokes_apply_scaled": (ip, [vp, vp, vp]),
             "xc_last_error": (ctypes.c_char_p, []),
             "xc_version": (ctypes.c_char_p, []),

@@ -2237,6 +2237,8 @@ struct StokesWork {
   float* nn_logeta;
   float* nn_r;          // 2 n: the V-cycle's residual and A times the network's direction
   float* nn_z;          // n: the network's direction
+  double* nn_xprev;     // n: the iterate before a learned refinement pass (restored if the pass fails)
+  double* nn_dv;        // 2 n: training samples' V-cycle result and its residual
   bool last_fp64_mg;    // the last solve set up the FP64 multigrid
   SolveCfg last_cfg;
 };
@@ -2680,13 +2682,18 @@ __global__ void nn_unpack_kernel(Geo g, const float* __restrict__ o16, const flo
   z[t] = p >= 0 ? o16[p * 16 + ch] : (outside ? outside[t] : 0.0f);
 }
 
-// z += alpha n with alpha = dots[0] / dots[1] (the least-squares step of n
-// against the residual it targets; no step when dots[1] vanishes)
-__global__ void nn_axpy_kernel(long long n, const double* __restrict__ dots, const float* __restrict__ nz, float* z) {
+// z += alpha n with alpha = dots[0] / dots[1], the least-squares step of n
+// against the residual r it targets (|r|^2 = *rnorm2).  The step is taken
+// only when it removes at least a tenth of |r|^2: a direction the network
+// gets wrong is then left out instead of adding a large, nearly A-null
+// component that the FP32 Krylov basis could not resolve.
+__global__ void nn_axpy_kernel(long long n, const double* __restrict__ dots, const double* __restrict__ rnorm2,
+                               const float* __restrict__ nz, float* z) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const double den = dots[1];
-  const float alpha = den > 0.0 ? (float)(dots[0] / den) : 0.0f;
+  const double num = dots[0], den = dots[1];
+  const bool take = den > 0.0 && num * num >= 0.1 * (*rnorm2) * den;
+  const float alpha = take ? (float)(num / den) : 0.0f;
   z[t] += alpha * nz[t];
 }
 
@@ -2735,7 +2742,7 @@ int apply_precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& c
         double* dots = w->hdev + 8;   // free until this step's Gram-Schmidt
         const int nb = launch_multidot<float>(n, 2, r, n, anz, w->part, s);
         pdl(PDL_ON, multidot_final_kernel, 2, KB, s, 2, nb, w->part, dots);
-        nn_axpy_kernel<<<nblk(n), 256, 0, s>>>(n, dots, w->nn_z, out); xc_count_launch();
+        nn_axpy_kernel<<<nblk(n), 256, 0, s>>>(n, dots, w->hdev + 5, w->nn_z, out); xc_count_launch();
       }
       XC_LAUNCH_CHECK();
       return XC_OK;
@@ -3156,7 +3163,8 @@ void stokes_destroy(xc_ctx* c) {
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   if (w->net) xc_nn_destroy(w->net);
-  cudaFree(w->nn_in); cudaFree(w->nn_logeta); cudaFree(w->nn_r); cudaFree(w->nn_z);
+  cudaFree(w->nn_in); cudaFree(w->nn_logeta); cudaFree(w->nn_r); cudaFree(w->nn_z); cudaFree(w->nn_xprev);
+  cudaFree(w->nn_dv);
   delete w;
   c->stokes = nullptr;
 }
@@ -3171,6 +3179,8 @@ static int nn_buffers(StokesWork* w) {
   if (!w->nn_logeta) XC_CUDA_TRY(cudaMalloc(&w->nn_logeta, sizeof(float) * (size_t)g.Nz * g.Nx));
   if (!w->nn_r) XC_CUDA_TRY(cudaMalloc(&w->nn_r, sizeof(float) * 2 * n));
   if (!w->nn_z) XC_CUDA_TRY(cudaMalloc(&w->nn_z, sizeof(float) * n));
+  if (!w->nn_xprev) XC_CUDA_TRY(cudaMalloc(&w->nn_xprev, sizeof(double) * n));
+  if (!w->nn_dv) XC_CUDA_TRY(cudaMalloc(&w->nn_dv, sizeof(double) * 2 * n));
   return XC_OK;
 }
 
@@ -3194,8 +3204,8 @@ extern "C" int xc_set_learned_preconditioner(xc_ctx* c, const float* params, lon
   return XC_OK;
 }
 
-extern "C" int xc_learned_sample(xc_ctx* c, const float* v, float* in, float* target, double rtol, int maxit,
-                                 int* iterations) {
+extern "C" int xc_learned_sample(xc_ctx* c, const float* v, int after_vcycle, float* in, float* target,
+                                 double rtol, int maxit, int* iterations) {
   if (!c || !c->stokes || !v || !in || !target) { xc_set_error("xc_learned_sample: null argument"); return XC_BAD_ARG; }
   StokesWork* w = c->stokes;
   if (!w->have_k || !w->last_fp64_mg) {
@@ -3212,12 +3222,23 @@ extern "C" int xc_learned_sample(xc_ctx* c, const float* v, float* in, float* ta
   xc_count_launch();
   convert_kernel<float, double><<<nblk(n), 256, 0, s>>>(n, v, w->d.w); xc_count_launch();
   XC_LAUNCH_CHECK();
+  // the system solved: S LL S z = v, or for the V-cycle's residual
+  // r = v - S LL S M(v) (M one FP64 V-cycle of the multigrid preconditioner)
+  double* rhs = w->d.w;
+  if (after_vcycle) {
+    double* zmg = w->nn_dv;
+    double* r = w->nn_dv + n;
+    XC_TRY(precond<double>(w, w->d, w->last_k, w->last_cfg, w->d.w, zmg, s));
+    XC_TRY(apply_scaled<double>(w, w->d, w->last_k, zmg, w->d.w, r, s));
+    rhs = r;
+  }
   int its = 0;
   double rr = 1.0;
-  XC_TRY(fgmres<double>(w, w->d, w->last_k, w->last_cfg, w->d.w, rtol, maxit, &its, &rr, s, FG_ZERO_GUESS));
-  // v enters at unit norm, as every Krylov vector does
-  XC_TRY(dot_self<double>(w, w->d, w->d.w, n, 5, s));
-  nn_pack_kernel<float><<<nblk(npx), 256, 0, s>>>(g, v, w->nn_logeta, w->hdev + 6, sqrtf((float)npx), in, 4);
+  XC_TRY(fgmres<double>(w, w->d, w->last_k, w->last_cfg, rhs, rtol, maxit, &its, &rr, s, FG_ZERO_GUESS));
+  // the input at unit norm, as every Krylov vector and every normalised
+  // V-cycle residual enters the network
+  XC_TRY(dot_self<double>(w, w->d, rhs, n, 5, s));
+  nn_pack_kernel<double><<<nblk(npx), 256, 0, s>>>(g, rhs, w->nn_logeta, w->hdev + 6, sqrtf((float)npx), in, 4);
   xc_count_launch();
   XC_CUDA_TRY(cudaMemsetAsync(target, 0, sizeof(float) * npx * 3, s));
   nn_target_kernel<<<nblk(n), 256, 0, s>>>(g, w->d.y, target); xc_count_launch();
@@ -3423,6 +3444,10 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     const double bn = std::sqrt(w->hhost[3]) > 0 ? std::sqrt(w->hhost[3]) : 1.0;
     // the FP64 operator reuses d.V[0] as residual storage
     double* res = w->d.V;
+    // the learned preconditioner serves a pass only while its passes at
+    // least halve the FP64 residual; the multigrid takes the rest of the solve
+    bool learned_on = o.learned != 0, judge = false;
+    double relres_before = 0.0;
     for (int outer = 0; outer < 50; ++outer) {
       // res = S RR - S LL x (FP64), the operator applied to the physical x
       pdl(PDL_ON, stokes_apply_kernel<double>, grid2(g), blk2(), s, g, k, vop(w->d, 0), w->d.cp, w->d.scl, w->x,
@@ -3432,6 +3457,16 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
       XC_CUDA_TRY(cudaStreamSynchronize(s));
       relres = std::sqrt(w->hhost[3]) / bn;
+      if (judge) {
+        judge = false;
+        if (!(relres <= 0.5 * relres_before)) {
+          // restore the iterate of before the pass and go on without the network
+          XC_CUDA_TRY(cudaMemcpyAsync(w->x, w->nn_xprev, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+          learned_on = false;
+          ++fallbacks;
+          continue;
+        }
+      }
       if (!std::isfinite(relres)) { xc_set_error("mixed solver: non-finite residual"); status = XC_NAN; break; }
       if (relres <= o.rtol || its >= o.maxit) break;
       ++refinements;
@@ -3443,13 +3478,19 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       int iits = 0;
       double irr = 1.0;
       const double rn2 = w->hhost[3];
-      XC_TRY(fgmres<float>(w, w->f, k, o.learned ? icfg_nn : icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
-                           FG_ZERO_GUESS | FG_TRUST_EST, rn2));
+      if (learned_on) {
+        XC_CUDA_TRY(cudaMemcpyAsync(w->nn_xprev, w->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        relres_before = relres;
+        judge = true;
+      }
+      XC_TRY(fgmres<float>(w, w->f, k, learned_on ? icfg_nn : icfg, frhs, o.inner_rtol, o.inner_maxit, &iits,
+                           &irr, s, FG_ZERO_GUESS | FG_TRUST_EST, rn2));
       its += iits;
-      if (o.learned && !(irr <= o.inner_rtol)) {
+      if (learned_on && !(irr <= o.inner_rtol)) {
         // the learned inner solve missed its reduction: the multigrid
         // preconditioner redoes this pass from zero
         ++fallbacks;
+        judge = false;
         XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
                              FG_ZERO_GUESS | FG_TRUST_EST, rn2));
         its += iits;

@@ -175,12 +175,15 @@ def workload_state(N, seed=0):
     return st, coefs, st.scales["dt0"]
 
 
-def generate(N=256, count=1024, per_field=16, contrasts=(1e2, 1e5), seed=0, rtol=1e-6, log=None):
+def generate(N=256, count=1024, per_field=16, contrasts=(1e2, 1e5), seed=0, rtol=1e-6, after_vcycle=True,
+             log=None):
     """Training pairs (inputs [count][N][N][4], targets [count][N][N][3],
     device FP32): `count / per_field` injected viscosity fields, `per_field`
-    random vectors each, targets the plain FP64 solver's solutions normalised
-    to unit RMS (the network predicts the direction; FGMRES and the hybrid's
-    least-squares step fix the scale)."""
+    random vectors each; with after_vcycle the right-hand side is the residual
+    one multigrid V-cycle leaves of the vector (what the network corrects in
+    learned mode 2), else the vector itself (mode 1); targets the plain FP64
+    solver's solutions normalised to unit RMS (the network predicts the
+    direction; FGMRES and the hybrid's least-squares step fix the scale)."""
     import torch
     dev = torch.device("cuda")
     st, coefs, dt = workload_state(N, seed)
@@ -198,7 +201,7 @@ def generate(N=256, count=1024, per_field=16, contrasts=(1e2, 1e5), seed=0, rtol
             # the operator of this viscosity (an FP64 solve sets up its multigrid)
             st.fluidmech(coefs, dt, solver="fgmres64", rtol=1e-6, maxit=600)
         v = staggered_vector(torch, gen, N, N, dev, float(np.exp(rng.uniform(0.0, math.log(N / 4)))))
-        xc._check(xc.lib().xc_learned_sample(st._h, ctypes.c_void_p(v.data_ptr()),
+        xc._check(xc.lib().xc_learned_sample(st._h, ctypes.c_void_p(v.data_ptr()), int(bool(after_vcycle)),
                                              ctypes.c_void_p(inputs[k].data_ptr()),
                                              ctypes.c_void_p(targets[k].data_ptr()), float(rtol), 600,
                                              ctypes.byref(iters)))
@@ -229,9 +232,74 @@ def train(net: Network, inputs, targets, steps=2000, lr=2e-3, seed=0, log=None):
     return losses
 
 
+SOLVE = dict(solver="mixed", rtol=1e-9, maxit=600, inner_rtol=5e-2, inner_maxit=30, pressure_sweeps=1)
+
+
+def evaluate(params, N, seed=7, modes=(0, 1, 2), repeats=3):
+    """The mixed solve of one Stokes system of the workload at N^2 with each
+    preconditioner mode: inner iterations, learned fallbacks, final FP64
+    residual and the device time of the solve (median of `repeats` after one
+    untimed solve that captures the graphs)."""
+    st, coefs, dt = workload_state(N, seed)
+    use(st, params)
+    snap = {k: st[k] for k in ("W", "U", "P", "MFS", "drhodt")}
+    out = {}
+    for mode in modes:
+        secs = []
+        info = None
+        for r in range(repeats + 1):
+            for k, v in snap.items():
+                st[k] = v
+            try:
+                info = st.fluidmech(coefs, dt, learned=mode, **SOLVE)
+            except xc.XcoreError as e:
+                info = {"error": str(e)}
+                break
+            if r > 0:
+                secs.append(info["seconds"])
+        if secs:
+            info["median_ms"] = 1e3 * float(np.median(secs))
+        out[mode] = info
+    st.close()
+    return out
+
+
+# (input channels, output channels, level) of the 15 convolutions
+LAYERS = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (64, 128, 3),
+          (128, 128, 3), (128, 64, 3), (64, 64, 2), (64, 32, 2), (32, 32, 1), (32, 16, 1), (16, 16, 0), (16, 16, 0)]
+
+
+def forward_flops(H, W):
+    """Multiply-add flops of one forward pass (2 per multiply-add)."""
+    return sum(2.0 * 9 * ci * co * (H >> lv) * (W >> lv) for ci, co, lv in LAYERS)
+
+
+def bench_forward(N, iters=20):
+    """Device time of one forward pass of the network at N^2 (CUDA events on
+    the network's stream, after a warm-up pass) and its convolution flop
+    rate."""
+    import torch
+    net = Network(N, N, 1, seed=0)
+    inp = torch.randn((1, N, N, IN_CH), device="cuda")
+    out = torch.empty((1, N, N, OUT_CH), device="cuda")
+    net.forward(inp, out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        net.forward(inp, out)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    net.close()
+    return {"N": N, "ms_per_forward": ms, "conv_tflops": forward_flops(N, N) / (ms * 1e-3) / 1e12}
+
+
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser()
+    ap.add_argument("--bench-forward", type=int, default=None, metavar="N",
+                    help="only time the network's forward pass at N^2 and exit")
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--N", type=int, default=256)
     ap.add_argument("--samples", type=int, default=2048)
@@ -242,13 +310,33 @@ def main(argv=None):
     a = ap.parse_args(argv)
     xc.build()
     log = lambda m: print(m, flush=True)  # noqa: E731
-    inputs, targets = generate(a.N, a.samples, seed=a.seed, log=log)
+    if a.bench_forward:
+        import json
+        log(json.dumps(bench_forward(a.bench_forward)))
+        return
+    inputs, targets = generate(a.N, a.samples, seed=a.seed, after_vcycle=True, log=log)
+    # the loss of predicting zero, for reference: the targets have unit RMS
+    zero_loss = float(targets.pow(2).sum(dim=3).mean())
     net = Network(a.N, a.N, a.batch, seed=a.seed)
     losses = train(net, inputs, targets, steps=a.steps, lr=a.lr, seed=a.seed, log=log)
-    save_params(a.out, net.params(), {"N": np.int64(a.N), "samples": np.int64(a.samples),
-                                      "steps": np.int64(a.steps), "loss_first": np.float64(np.mean(losses[:50])),
-                                      "loss_last": np.float64(np.mean(losses[-50:]))})
-    log(f"wrote {a.out}: loss {np.mean(losses[:50]):.4f} -> {np.mean(losses[-50:]):.4f}")
+    params = net.params()
+    net.close()
+    del inputs, targets
+    import json
+    report = {n: evaluate(params, n) for n in (a.N, 1024)}
+    log("evaluation: " + json.dumps(report))
+    # the mode the bench uses: the fastest at 1024^2 (0 = the multigrid alone)
+    times = {m: r.get("median_ms", float("inf")) for m, r in report[1024].items()}
+    best = min(times, key=times.get)
+    save_params(a.out, params, {"N": np.int64(a.N), "samples": np.int64(a.samples), "steps": np.int64(a.steps),
+                                "loss_first": np.float64(np.mean(losses[:50])),
+                                "loss_last": np.float64(np.mean(losses[-50:])), "loss_zero": np.float64(zero_loss),
+                                "best_mode": np.int64(best),
+                                **{f"ms_1024_mode{m}": np.float64(t) for m, t in times.items()},
+                                **{f"iterations_1024_mode{m}": np.int64(r.get("iterations", -1))
+                                   for m, r in report[1024].items()}})
+    log(f"wrote {a.out}: loss {np.mean(losses[:50]):.4f} -> {np.mean(losses[-50:]):.4f} (zero predictor "
+        f"{zero_loss:.4f}); best mode at 1024^2: {best}")
 
 
 if __name__ == "__main__":
