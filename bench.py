@@ -258,7 +258,10 @@ def main():
     if a.solver == "mixed" and os.path.exists(wpath) and a.learned != 0:
         with np.load(wpath) as z:
             best = int(z["best_mode"]) if "best_mode" in z.files else 2
-            learned_info.update({k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files if k != "params"})
+            for key in z.files:
+                if key != "params" and z[key].ndim == 0:
+                    v = z[key].item()
+                    learned_info[key] = v if not isinstance(v, float) or math.isfinite(v) else None
         mode = best if a.learned < 0 else a.learned
         if mode > 0:
             learned_mod.use(st, learned_mod.load_params(wpath))
@@ -371,6 +374,37 @@ def main():
             k += 1
         field_err = {f: float(np.abs(st[f] - v).max() / max(np.abs(v).max(), 1e-300))
                      for f, v in plain_fields.items()}
+    # ---- the learned preconditioner's modes beside the headline -------------------------
+    # each mode of the committed network the headline does not use, timed on the
+    # same steps from the same saved state (device-resident, as `value`)
+    learned_runs = {}
+    if learned_info["weights"] and a.solver == "mixed":
+        if "learned" not in sopt:
+            learned_mod.use(st, learned_mod.load_params(wpath))
+        for mode in (1, 2):
+            if sopt.get("learned", 0) == mode:
+                continue
+            st.restore(snap)
+            step, dt, k = step0, dt0, k0
+            intervals, its_l = [], 0
+            barrier()
+            try:
+                for _ in range(a.steps):
+                    step += 1
+                    st["re"], st["rs"] = draws[k][0], draws[k][1]
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    info = st.step(step, dt, None, None, sweeps=a.sweeps, **dict(sopt, learned=mode))
+                    e1.record(stream)
+                    intervals.append((e0, e1))
+                    dt = info["dt_next"]
+                    its_l += info["solver_iterations"]
+                    k += 1
+                barrier()
+                learned_runs[mode] = {"ms_per_step": sum(x.elapsed_time(y) for x, y in intervals) / a.steps,
+                                      "solver_iterations_per_step": its_l / a.steps}
+            except xc.XcoreError as e:
+                learned_runs[mode] = {"error": str(e)}
     # ---- roofline of the dominant kernel (CUDA events on the library stream) ----------
     rk = st.bench_kernel(a.roofline_kernel, iters=20)
     peaks = {}
@@ -381,8 +415,8 @@ def main():
     achieved = rk[1] / (rk[0] * 1e-3) / 1e9
     # DRAM bytes (read + write) per cell of one launch, measured by one ncu
     # capture of each kernel on this workload at 1024^2, scaled to this grid
-    ncu_bytes_per_cell = {0: 25.23e6 / 1048576, 1: (235.73e6 + 18.77e6) / 1048576,
-                          3: (185.02e6 + 11.52e6) / 1048576, 4: 8.43e6 / 1048576, 5: 33.64e6 / 1048576}
+    ncu_bytes_per_cell = {0: 25.23e6 / 1048576, 1: (235.73e6 + 18.77e6) / 1048576, 2: 33.64e6 / 1048576,
+                          3: (185.02e6 + 11.52e6) / 1048576, 4: 8.43e6 / 1048576}
     traffic = ncu_bytes_per_cell[a.roofline_kernel] * rk[3] if a.roofline_kernel in ncu_bytes_per_cell else None
     ms_t = torch.tensor([ms, ms_e2e, ms_plain or 0.0], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -403,10 +437,10 @@ def main():
                          + cpu_note(CPU_GRID)}
         gpu_at_cpu_grid = gpu_steps_per_second(xc, CPU_GRID, a.sweeps, 10, sopt)
     names = {0: "advect_tile_kernel (WENO5, one field)", 1: "stokes_apply_kernel<double>",
-             2: "vel_sweep_rb_kernel<1> (finest-level FP32 velocity Jacobi sweep, four rows along z per thread; "
-                "operand copies exceed 2x L2)",
-             5: "vel_sweep2d_kernel<float,1> (finest-level FP32 velocity Jacobi sweep, one row per thread; operand "
+             2: "vel_sweep2d_kernel<float,1> (finest-level FP32 velocity Jacobi sweep, one row per thread; operand "
                 "copies exceed 2x L2)",
+             5: "vel_sweep_rb_kernel<1> (finest-level FP32 velocity Jacobi sweep, four rows along z per thread; "
+                "operand copies exceed 2x L2)",
              3: "vel_sweep2d_kernel<double,1> (finest-level velocity Jacobi sweep; operand copies exceed 2x L2)",
              4: "line_filter_kernel (FFT z pass)"}
     out = {
@@ -438,7 +472,7 @@ def main():
             "field_error_note": f"max-norm relative deviation of W, U, P, x after {a.plain_steps} steps from the "
                                 "same saved state: mixed solver vs the plain FP64 solver",
             "cpu_grid_gpu_timesteps_per_s": gpu_at_cpu_grid,
-            "learned_preconditioner": learned_info,
+            "learned_preconditioner": dict(learned_info, other_modes=learned_runs),
             "cache": "working set (~2 GB of fields and solver vectors) exceeds L2 (129 MB); no flush needed",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         },

@@ -128,8 +128,11 @@ typedef struct xc_solver_opts {
   int jacobi_coarse;       /* 1: Jacobi sweeps (coarse_sweeps) on the coarsest levels even where they
                               have at most 64 unknowns, which by default are solved with their
                               dense inverse (formed and inverted on the device once per solve) */
-  int row_sweep;           /* 1: FP32 velocity sweeps one row per thread (vel_sweep2d_kernel) instead
-                              of four consecutive rows along z per thread (same operations) */
+  int row_block_sweep;     /* 1: FP32 velocity sweeps with four consecutive rows along z per thread
+                              and an interior path without boundary tests (same operations as the
+                              default one row per thread; measured 20% slower at 1024^2: the
+                              strided per-thread rows cost more L1 wavefronts than the shared
+                              loads save) */
   int learned;             /* mixed solver, plain refinement: preconditioner of the FP32 inner
                               solves.  0 the multigrid V-cycles; 1 the learned network
                               (xc_set_learned_preconditioner) in their place, an inner solve that
@@ -428,9 +431,9 @@ long long xc_launch_count(void);
    that evicts L2; kernels 2, 3: back to back over copies of the operands that
    together exceed twice the L2).  which: 0 WENO5/QUICK advect-with-flux of X (phsevo!),
    1 FP64 Stokes operator apply, 2 FP32 velocity Jacobi sweep (finest level,
-   four rows per thread as the mixed solver runs it), 3 FP64 velocity Jacobi
-   sweep, 4 FFT line filter (z pass of psie), 5 the FP32 sweep one row per
-   thread.
+   one row per thread as the mixed solver runs it), 3 FP64 velocity Jacobi
+   sweep, 4 FFT line filter (z pass of psie), 5 the FP32 sweep with four rows
+   per thread (row_block_sweep).
    out = {ms per launch, algorithmic bytes per
    launch, algorithmic flops per launch, units per launch}.  Kernels 1-3 need
    a previous xc_fluidmech call (2 needs the mixed solver). */

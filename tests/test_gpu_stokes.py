@@ -270,7 +270,7 @@ def test_row_blocked_fp32_sweep_matches_the_per_row_sweep(N):
     for row in (False, True):
         ds = device_state(par, g, sc, st)
         info = ds.fluidmech(coefs, dt, solver="mixed", rtol=1e-9, maxit=600, inner_rtol=5e-2, inner_maxit=30,
-                            pressure_sweeps=1, row_sweep=row)
+                            pressure_sweeps=1, row_block_sweep=row)
         assert info["converged"], info
         out[row] = (info, ds["W"], ds["U"], ds["P"])
         ds.close()

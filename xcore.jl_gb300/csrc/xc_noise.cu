@@ -258,15 +258,25 @@ __global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double l0h, dou
 
 // re-standardise to the raw mean/std (noise.jl:261-267); st = {raw mean,
 // raw sum sq dev, flt mean, flt sum sq dev} per field
+// (the two standard deviations, the same for every cell, are formed once per
+// block by the same operations)
 __global__ void rescale_kernel(int Nz, int Nx, DView f0, DView f1, DView f2, const double* st) {
+  __shared__ double sd[6];
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const double nm1 = (double)Nz * (double)Nx - 1.0;
+    for (int q = 0; q < 3; ++q) {
+      sd[2 * q] = sqrt(st[4 * q + 1] / nm1);
+      sd[2 * q + 1] = sqrt(st[4 * q + 3] / nm1);
+    }
+  }
+  __syncthreads();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
-  const double nm1 = (double)Nz * (double)Nx - 1.0;
   DView fs[3] = {f0, f1, f2};
   for (int q = 0; q < 3; ++q) {
     const double* s = st + 4 * q;
-    double raw_std = sqrt(s[1] / nm1), flt_std = sqrt(s[3] / nm1);
+    const double raw_std = sd[2 * q], flt_std = sd[2 * q + 1];
     if (flt_std > XC_EPS) {
       double v = AT(fs[q], j, i);
       AT(fs[q], j, i) = (((v - s[2]) * raw_std) / flt_std) + s[0];

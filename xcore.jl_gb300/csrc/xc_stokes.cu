@@ -2148,8 +2148,9 @@ struct SolveCfg {
   // FP32 inner solves: 0 multigrid preconditioner, 1 the learned network in
   // its place, 2 the network applied to what the multigrid V-cycle leaves
   int learned = 0;
-  // FP32 velocity sweeps with four rows along z per thread (vel_sweep_rb_kernel)
-  bool row_block = true;
+  // FP32 velocity sweeps with four rows along z per thread (vel_sweep_rb_kernel;
+  // opt-in: measured 20% slower at 1024^2 than one row per thread)
+  bool row_block = false;
 };
 
 }  // namespace
@@ -3380,7 +3381,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.pressure_sweeps > 0) cfg.nu_p = o.pressure_sweeps;
   cfg.pdl = !o.serial_launch;
   cfg.tiled = o.tiled_sweep != 0;
-  cfg.row_block = o.row_sweep == 0;
+  cfg.row_block = o.row_block_sweep != 0;
   cfg.stage_small = o.stage_small_levels != 0;
   cfg.direct_coarse = !o.jacobi_coarse;
   if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;
@@ -3488,11 +3489,14 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
       its += iits;
       if (learned_on && !(irr <= o.inner_rtol)) {
         // the learned inner solve missed its reduction: the multigrid
-        // preconditioner redoes this pass from zero
+        // preconditioner redoes this pass from zero and takes the rest of
+        // the solve.  (Its right-hand side's norm is recomputed: the device
+        // reciprocal the first attempt started from has been overwritten.)
         ++fallbacks;
         judge = false;
+        learned_on = false;
         XC_TRY(fgmres<float>(w, w->f, k, icfg, frhs, o.inner_rtol, o.inner_maxit, &iits, &irr, s,
-                             FG_ZERO_GUESS | FG_TRUST_EST, rn2));
+                             FG_ZERO_GUESS | FG_TRUST_EST, -1.0));
         its += iits;
       }
       refine_update_kernel<float><<<nblk(n), 256, 0, s>>>(n, w->f.y, w->d.scl, w->x); xc_count_launch();
@@ -3639,7 +3643,7 @@ int stokes_bench(xc_ctx* c, int which, int iters, double out[4]) {
   if (which == 2 || which == 3 || which == 5) {
     float ms = 0;
     XC_TRY(which == 3 ? sweep_bench<double>(s, g, k, w->d, iters, &ms)
-                      : sweep_bench<float>(s, g, k, w->f, iters, &ms, which == 2));
+                      : sweep_bench<float>(s, g, k, w->f, iters, &ms, which == 5));
     out[0] = ms;
     return XC_OK;
   }

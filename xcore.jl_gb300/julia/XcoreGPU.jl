@@ -41,7 +41,7 @@ struct SolverOpts
     smooth_sweeps::Cint; omega_velocity::Cdouble; schur_mass::Cdouble; schur_full_diagonal::Cint
     coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint; pressure_sweeps::Cint; inner_gs_passes::Cint
     serial_launch::Cint; coarse_viscosity_mean::Cint; tiled_sweep::Cint; post_sweeps::Cint; outer_solver::Cint
-    fused_pressure_cells::Cint; stage_small_levels::Cint; jacobi_coarse::Cint; row_sweep::Cint; learned::Cint
+    fused_pressure_cells::Cint; stage_small_levels::Cint; jacobi_coarse::Cint; row_block_sweep::Cint; learned::Cint
 end
 SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
     SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)

@@ -332,7 +332,8 @@ def main(argv=None):
                                 "loss_first": np.float64(np.mean(losses[:50])),
                                 "loss_last": np.float64(np.mean(losses[-50:])), "loss_zero": np.float64(zero_loss),
                                 "best_mode": np.int64(best),
-                                **{f"ms_1024_mode{m}": np.float64(t) for m, t in times.items()},
+                                **{f"ms_1024_mode{m}": np.float64(t if math.isfinite(t) else -1.0)
+                                   for m, t in times.items()},
                                 **{f"iterations_1024_mode{m}": np.int64(r.get("iterations", -1))
                                    for m, r in report[1024].items()}})
     log(f"wrote {a.out}: loss {np.mean(losses[:50]):.4f} -> {np.mean(losses[-50:]):.4f} (zero predictor "
