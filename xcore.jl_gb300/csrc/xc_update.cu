@@ -116,30 +116,57 @@ __global__ void interp_kernel(int Nz, int Nx, int xBC, int zBC, double rhom0, do
 // One thread per row j sums the row in column order; the columns are loaded
 // 16 at a time ahead of the additions, so the order (and the bits) of the sum
 // stay sequential while many loads are in flight.
-__global__ void rowmean_kernel(int Nz, int Nx, CView rhow, double* rhoref) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j > Nz) return;
+// mean(rhow, dims = 2) in Julia's order: for each row, the columns added one
+// after another from the left.  A block of 256 threads takes 32 rows: all its
+// threads load 32 x kRowTile tiles (coalesced, many loads in flight) into
+// shared memory, then one warp -- a thread per row -- adds them in column
+// order.  Same additions as a thread walking its row alone.
+constexpr int kRowTile = 128;
+__global__ void __launch_bounds__(256) rowmean_kernel(int Nz, int Nx, CView rhow, double* rhoref) {
+  __shared__ double tile[kRowTile][33];
+  const int j0 = blockIdx.x * 32;
+  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;   // row in the block, column phase
+  const int j = j0 + r;
   double acc = 0.0;
-  int i = 0;
-  for (; i + 16 <= Nx; i += 16) {
-    double v[16];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = AT(rhow, j, i + q);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc = acc + v[q];
-  }
-  for (; i < Nx; ++i) acc = acc + AT(rhow, j, i);
-  rhoref[j] = acc / (double)Nx;
-}
-__global__ void pressure_scan_kernel(int Nz, double g0, double h, double Ptop, const double* rhoref,
-                                     double* plcol) {
-  if (threadIdx.x == 0) {
-    double p = ((rhoref[0] * g0) * h) / 2.0 + Ptop;
-    plcol[0] = p;
-    for (int j = 1; j < Nz; ++j) {
-      p = p + (rhoref[j] * g0) * h;
-      plcol[j] = p;
+  for (int i0 = 0; i0 < Nx; i0 += kRowTile) {
+    for (int c = cw; c < kRowTile; c += 8) {
+      const int i = i0 + c;
+      tile[c][r] = (j <= Nz && i < Nx) ? AT(rhow, j, i) : 0.0;
     }
+    __syncthreads();
+    if (cw == 0) {
+      const int n = Nx - i0 < kRowTile ? Nx - i0 : kRowTile;
+      for (int c = 0; c < n; ++c) acc = acc + tile[c][r];
+    }
+    __syncthreads();
+  }
+  if (cw == 0 && j <= Nz) rhoref[j] = acc / (double)Nx;
+}
+
+// the column of Pl (update.jl:123-131): the terms (rhoref[j] g0) h of all
+// rows formed by the block into shared memory, then added in row order by one
+// thread (the reference's loop), in chunks of kScanChunk rows
+constexpr int kScanChunk = 4096;
+__global__ void __launch_bounds__(256) pressure_scan_kernel(int Nz, double g0, double h, double Ptop,
+                                                            const double* rhoref, double* plcol) {
+  __shared__ double q[kScanChunk];
+  double p = 0.0;
+  for (int j0 = 0; j0 < Nz; j0 += kScanChunk) {
+    const int n = Nz - j0 < kScanChunk ? Nz - j0 : kScanChunk;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const int j = j0 + k;
+      q[k] = j == 0 ? ((rhoref[0] * g0) * h) / 2.0 + Ptop : (rhoref[j] * g0) * h;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < n; ++k) {
+        p = (j0 + k == 0) ? q[0] : p + q[k];
+        q[k] = p;
+      }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) plcol[j0 + k] = q[k];
+    __syncthreads();
   }
 }
 
@@ -267,7 +294,9 @@ __global__ void corner_eta_etasw_kernel(int Nz, int Nx, int zBC, CView eta, DVie
   int a = icz_at(j, Nz, XC_CLOSED), b = icz_at(j + 1, Nz, XC_CLOSED);
   int c = icx_at(i, Nx, XC_PERIODIC), d = icx_at(i + 1, Nx, XC_PERIODIC);
   double e00 = AT(eta, a, c), e10 = AT(eta, b, c), e01 = AT(eta, a, d), e11 = AT(eta, b, d);
-  AT(etaco, j, i) = pow(((e00 * e10) * e01) * e11, 0.25);
+  // the fourth root as two correctly rounded square roots: within one ulp,
+  // as pow is, at a fraction of pow's FP64 work
+  AT(etaco, j, i) = sqrt(sqrt(((e00 * e10) * e01) * e11));
   if (i < Nx) {
     int p = icz_at(j, Nz, zBC), q = icz_at(j + 1, Nz, zBC);
     AT(etasw, j, i) = sqrt(AT(etas, p, i) * AT(etas, q, i));
@@ -383,8 +412,8 @@ int update_impl(xc_ctx* c) {
   XC_LAUNCH_CHECK();
   double* rhoref = c->tmp[6];
   double* plcol = c->tmp[6] + (Nz + 8);
-  rowmean_kernel<<<(Nz + 1 + 31) / 32, 32, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), rhoref); xc_count_launch();
-  pressure_scan_kernel<<<1, 32, 0, s>>>(Nz, p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
+  rowmean_kernel<<<(Nz + 1 + 31) / 32, 256, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), rhoref); xc_count_launch();
+  pressure_scan_kernel<<<1, 256, 0, s>>>(Nz, p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
   XC_LAUNCH_CHECK();
   drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, s>>>(
       Nz, Nx, p.Ptop, rhoref, plcol, CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
