@@ -44,6 +44,9 @@ def parse():
                          "(default): the learned mode the committed weights record as best, 0 without weights")
     ap.add_argument("--weights", default=None, help="learned preconditioner parameters (.npz)")
     ap.add_argument("--rtol", type=float, default=1e-9)
+    ap.add_argument("--weno-weights", type=int, default=0, choices=[0, 1],
+                    help="WENO5 weights: 0 the reference's four-division form, 1 over a common denominator "
+                         "(one division; within 1e-12)")
     ap.add_argument("--plain-steps", type=int, default=None,
                     help="time steps of the plain FP64 comparison loop (default: --steps, the same steps)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -193,12 +196,12 @@ def run_reference(a):
         dist.barrier()
 
 
-def gpu_steps_per_second(xc, N, sweeps, steps, sopt, seed=5):
+def gpu_steps_per_second(xc, N, sweeps, steps, sopt, seed=5, weno_weights=0):
     """Timesteps/s of the GPU path on the same workload at N^2 (the CPU
     baseline's grid), CUDA events on the library stream, after 3 warm-up steps."""
     import torch
     par = workload_params(N)
-    st = xc.State(par)
+    st = xc.State(par, weno_weights=weno_weights)
     x0, rng = initial_fields(N, seed)
     st.initialize(x0, rng.standard_normal((N, N)), rng.standard_normal((N, N)))
     stream = torch.cuda.ExternalStream(st.stream_handle())
@@ -236,7 +239,7 @@ def main():
     xc.build()
     N = a.N
     par = workload_params(N)
-    st = xc.State(par)
+    st = xc.State(par, weno_weights=a.weno_weights)
     x0, rng = initial_fields(N, seed=1234 + rank)
     # every timed loop replays draws k0, k0 + 1, ... of the same saved state
     nstep_total = a.warmup + max(a.steps, a.plain_steps)
@@ -435,7 +438,7 @@ def main():
                "sample": f"2 timed {a.sweeps}-sweep time steps at {CPU_GRID}^2 after one warm-up step "
                          f"({np.mean(times):.2f} s each on this host; numpy + SciPy SuperLU, single-threaded); "
                          + cpu_note(CPU_GRID)}
-        gpu_at_cpu_grid = gpu_steps_per_second(xc, CPU_GRID, a.sweeps, 10, sopt)
+        gpu_at_cpu_grid = gpu_steps_per_second(xc, CPU_GRID, a.sweeps, 10, sopt, weno_weights=a.weno_weights)
     names = {0: "advect_tile_kernel (WENO5, one field)", 1: "stokes_apply_kernel<double>",
              2: "vel_sweep2d_kernel<float,1> (finest-level FP32 velocity Jacobi sweep, one row per thread; operand "
                 "copies exceed 2x L2)",
@@ -460,6 +463,8 @@ def main():
             "workload": f"xcore time step {N}x{N}: {a.sweeps} Picard sweeps (phsevo!, fluidmech!, noise!, "
                         f"update_phase_velocities!, update!), WENO5, BD2, etacntr 1e4, lognormal x",
             "grid": f"{N}x{N}", "sweeps": a.sweeps, "solver": a.solver, "stokes_rtol": a.rtol,
+            "weno_weights": "common denominator, one division (within 1e-12)" if a.weno_weights
+                            else "the reference's four-division form (bit for bit)",
             "solver_options": {k: v for k, v in sopt.items() if k not in ("solver", "rtol")},
             "solver_iterations_per_step": iters / a.steps, "worst_solver_rel_residual": resid,
             "e2e_solver_iterations_per_step": iters_e2e / a.steps,

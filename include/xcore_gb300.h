@@ -81,6 +81,11 @@ typedef struct xc_params {
   int TINT;                /* xc_tint */
   int xBC, zBC;            /* xc_bc; the reference default is periodic x, closed z */
   int sds, top_cnv, bot_cnv, open_cnv;   /* fluidmech! keywords (fluidmech.jl:71-80) */
+  int weno_weights;        /* WENO5 nonlinear weights (advect.jl:35-53): 0 the reference's form,
+                              three divisions for the weights and one to normalise them, bit for
+                              bit; 1 the same weights over a common denominator, one division per
+                              reconstruction (within a few ulps of the reference: its 1e-12 stencil
+                              tolerance) */
 } xc_params;
 
 typedef struct xc_solver_opts {
@@ -139,6 +144,10 @@ typedef struct xc_solver_opts {
                               misses inner_rtol redone with the multigrid; 2 the V-cycles followed
                               by the network on the residual they leave.  The FP64 residual of
                               the refinement judges every pass either way. */
+  int host_givens;         /* 1: the FGMRES least-squares update (Givens rotations, back
+                              substitution) on the host with one synchronisation per Arnoldi
+                              step, instead of on the device inside conditional CUDA graphs where
+                              the host queues the next step before the current one ends */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {
@@ -148,6 +157,8 @@ typedef struct xc_solver_stats {
   int converged;           /* 1 when rel_residual <= rtol */
   double seconds;          /* device time of the solve */
   int learned_fallbacks;   /* inner solves of the learned preconditioner redone with the multigrid */
+  int device_givens_steps; /* Arnoldi steps whose least-squares update ran on the device (conditional
+                              graphs; 0 with host_givens or where those graphs cannot be built) */
 } xc_solver_stats;
 
 #define XC_MAX_SWEEPS 64

@@ -36,8 +36,8 @@ def realistic_state(N=24, Nx=20, steps=2, seed=7, **kw):
     return par, g, sc, ns, st, dt, rng
 
 
-def device_state(par, g, sc, st=None):
-    s = xc.State(product_params(par), grid=xc.Grid(Nx=g.Nx, Nz=g.Nz, h=g.h, D=g.D, L=g.L), scales=sc)
+def device_state(par, g, sc, st=None, **kw):
+    s = xc.State(product_params(par), grid=xc.Grid(Nx=g.Nx, Nz=g.Nz, h=g.h, D=g.D, L=g.L), scales=sc, **kw)
     if st is not None:
         upload_all(s, st)
     return s

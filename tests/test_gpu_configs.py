@@ -58,10 +58,10 @@ def _compare_all(ds, st, where, tol=1e-12):
     assert not bad, (where, bad)
 
 
-def _lockstep(cfg, scheme, steps):
+def _lockstep(cfg, scheme, steps, **kw):
     par, g, sc, ns, x0, draws, (re0, rs0) = C.setup(cfg, scheme=scheme)
     st = O.initialize(g, par, sc, ns, x0, re0, rs0)
-    ds = device_state(par, g, sc)
+    ds = device_state(par, g, sc, **kw)
     ds.initialize(x0, re0, rs0)
     _compare_all(ds, st, "initialize!")
     dt = sc["dt0"]
@@ -103,6 +103,12 @@ def test_c1_identical_stokes_inputs_ten_steps():
 @pytest.mark.parametrize("scheme", ["weno5", "quick"])
 def test_c2_identical_stokes_inputs_one_step(scheme):
     _lockstep("c2", scheme, 1)
+
+
+def test_c2_weno5_one_division_weights_identical_stokes_inputs():
+    """WENO5 with its weights over a common denominator (weno_weights = 1):
+    every field within the same 1e-12 of the oracle's four-division form."""
+    _lockstep("c2", "weno5", 1, weno_weights=1)
 
 
 def _trajectory(cfg, scheme, name, steps, bound_fields, bound_dt):

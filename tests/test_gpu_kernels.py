@@ -127,6 +127,22 @@ def test_phsevo_bitwise(scheme):
                            "x", "m"], exact=True)
 
 
+@pytest.mark.parametrize("ADVN", ["weno5", "weno3"])
+def test_phsevo_weno5_one_division_weights(ADVN):
+    """weno_weights = 1: WENO5's nonlinear weights over a common denominator,
+    one division per reconstruction; within 1e-12 of the reference's form
+    (and WENO3, which it does not touch, still bit for bit)."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=40, Nx=36, ADVN=ADVN)
+    ds = device_state(par, g, sc, st, weno_weights=1)
+    coefs = O.time_coefs("bd2im", 3)
+    O.phsevo(st, g, par, sc, ADVN, coefs, dt)
+    ds.phsevo(coefs, dt, ADVN=ADVN)
+    names = ["advn_X", "advn_M", "qx_advn_X", "qz_advn_X", "qx_advn_M", "qz_advn_M", "Gx", "dXdt", "X", "M",
+             "x", "m"]
+    assert_fields(ds, st, names, exact=ADVN == "weno3", tol=1e-12)
+    ds.close()
+
+
 def test_store_and_phase_velocities_bitwise():
     par, g, sc, ns, st, dt, rng = realistic_state()
     ds = device_state(par, g, sc, st)

@@ -260,7 +260,7 @@ def test_not_converged_is_reported():
 
 @pytest.mark.parametrize("N", [64, 130])
 def test_row_blocked_fp32_sweep_matches_the_per_row_sweep(N):
-    """The FP32 velocity sweeps with four rows along z per thread (the default)
+    """The FP32 velocity sweeps with four rows along z per thread (opt-in)
     compute every row with the operations of the one-row-per-thread kernel:
     the mixed solve takes the same iterations to the same solution (130 has a
     partial row block at the bottom and interior columns next to the seam)."""
@@ -278,3 +278,42 @@ def test_row_blocked_fp32_sweep_matches_the_per_row_sweep(N):
     assert ia["iterations"] == ib["iterations"], (ia, ib)
     for a, b in zip(fa, fb):
         assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("solver,rtol,restart", [("fgmres64", 1e-10, 30), ("fgmres64", 1e-10, 8), ("mixed", 1e-9, 30)])
+def test_device_givens_matches_host_givens(solver, rtol, restart):
+    """The FGMRES least-squares update on the device (the default: each
+    Arnoldi step a conditional graph whose gate skips it once the cycle has
+    stopped, the host queueing the next step before the current one ends)
+    against the same update on the host: the same FP64 rotations (hypot may
+    round differently in the last bit), so the same iteration count within one
+    and the same solution.  restart 8 runs several restart cycles."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=64, Nx=48, steps=1)
+    coefs = O.time_coefs("bd2im", 2)
+    out = {}
+    for host in (True, False):
+        ds = device_state(par, g, sc, st)
+        info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol, maxit=600, restart=restart, inner_rtol=5e-2,
+                            inner_maxit=30, pressure_sweeps=1, host_givens=host)
+        assert info["converged"] and info["rel_residual"] <= rtol, (host, info)
+        out[host] = (info, ds["W"], ds["U"], ds["P"])
+        ds.close()
+    (ih, *fh), (idv, *fd) = out[True], out[False]
+    assert ih["device_givens_steps"] == 0
+    assert idv["device_givens_steps"] == idv["iterations"] > 0, idv
+    assert abs(ih["iterations"] - idv["iterations"]) <= 1, (ih, idv)
+    for a, b in zip(fd, fh):
+        assert np.abs(a - b).max() <= (1e-8 if solver == "fgmres64" else 1e-7) * np.abs(b).max()
+
+
+def test_device_givens_respects_the_iteration_cap():
+    """maxit inside a restart cycle: the gate stops the queued steps at the cap
+    and the solve reports the capped iteration count."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=48, Nx=48, steps=1)
+    for maxit in (1, 5, 13):
+        ds = device_state(par, g, sc, st)
+        with pytest.raises(xc.NotConverged) as e:
+            ds.fluidmech(O.time_coefs("bd2im", 2), dt, solver="fgmres64", rtol=1e-14, maxit=maxit, restart=8)
+        ds.close()
+        its = int(str(e.value).split(" after ")[1].split()[0])
+        assert its == maxit, (maxit, str(e.value))

@@ -69,7 +69,7 @@ class _Params(ctypes.Structure):
                 ("G0", ctypes.c_double), ("bnd_w", ctypes.c_double), ("dt0", ctypes.c_double),
                 ("ADVN", ctypes.c_int), ("TINT", ctypes.c_int), ("xBC", ctypes.c_int), ("zBC", ctypes.c_int),
                 ("sds", ctypes.c_int), ("top_cnv", ctypes.c_int), ("bot_cnv", ctypes.c_int),
-                ("open_cnv", ctypes.c_int)]
+                ("open_cnv", ctypes.c_int), ("weno_weights", ctypes.c_int)]
 
 
 class SolverOpts(ctypes.Structure):
@@ -83,7 +83,8 @@ class SolverOpts(ctypes.Structure):
                 ("tiled_sweep", ctypes.c_int), ("post_sweeps", ctypes.c_int), ("outer_solver", ctypes.c_int),
                 ("fused_pressure_cells", ctypes.c_int),
                 ("stage_small_levels", ctypes.c_int),
-                ("jacobi_coarse", ctypes.c_int), ("row_block_sweep", ctypes.c_int), ("learned", ctypes.c_int)]
+                ("jacobi_coarse", ctypes.c_int), ("row_block_sweep", ctypes.c_int), ("learned", ctypes.c_int),
+                ("host_givens", ctypes.c_int)]
 
     @classmethod
     def make(cls, solver="fgmres64", rtol=1e-10, maxit=500, restart=30, inner_rtol=1e-4, inner_maxit=60,
@@ -91,19 +92,20 @@ class SolverOpts(ctypes.Structure):
              coarse_cells=0, coarse_sweeps=0, small_cells=0, pressure_sweeps=0, inner_gs_passes=0,
              serial_launch=False, coarse_viscosity_mean=0, tiled_sweep=False, post_sweeps=0, outer_solver=0,
              fused_pressure_cells=0, stage_small_levels=False,
-             jacobi_coarse=False, row_block_sweep=False, learned=0):
+             jacobi_coarse=False, row_block_sweep=False, learned=0, host_givens=False):
         return cls(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit),
                    int(smooth_sweeps), float(omega_velocity), float(schur_mass), int(bool(schur_full_diagonal)),
                    int(coarse_cells), int(coarse_sweeps), int(small_cells), int(pressure_sweeps),
                    int(inner_gs_passes), int(bool(serial_launch)), int(coarse_viscosity_mean),
                    int(bool(tiled_sweep)), int(post_sweeps), int(outer_solver),
                    int(fused_pressure_cells), int(bool(stage_small_levels)),
-                   int(bool(jacobi_coarse)), int(bool(row_block_sweep)), int(learned))
+                   int(bool(jacobi_coarse)), int(bool(row_block_sweep)), int(learned), int(bool(host_givens)))
 
 
 class SolverStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("refinements", ctypes.c_int), ("rel_residual", ctypes.c_double),
-                ("converged", ctypes.c_int), ("seconds", ctypes.c_double), ("learned_fallbacks", ctypes.c_int)]
+                ("converged", ctypes.c_int), ("seconds", ctypes.c_double), ("learned_fallbacks", ctypes.c_int),
+                ("device_givens_steps", ctypes.c_int)]
 
 
 MAX_SWEEPS = 64
@@ -354,7 +356,8 @@ class State:
     """FluidState + PhaseState + NoiseState + StepResidual resident on the GPU."""
 
     def __init__(self, par: Parameters, grid: Grid | None = None, scales: dict | None = None,
-                 xBC="periodic", zBC="closed", sds=-1, top_cnv=1, bot_cnv=1, open_cnv=False):
+                 xBC="periodic", zBC="closed", sds=-1, top_cnv=1, bot_cnv=1, open_cnv=False,
+                 weno_weights=0):
         self.par = par
         self.grid = grid or Grid.from_params(par)
         self.scales = scales or compute_scales(par, self.grid)
@@ -373,6 +376,7 @@ class State:
         P.ADVN, P.TINT = SCHEMES[par.ADVN], TINTS[par.TINT]
         P.xBC, P.zBC = BCS[xBC], BCS[zBC]
         P.sds, P.top_cnv, P.bot_cnv, P.open_cnv = int(sds), int(top_cnv), int(bot_cnv), int(bool(open_cnv))
+        P.weno_weights = int(weno_weights)
         self._p = P
         h = ctypes.c_void_p()
         _check(lib().xc_ctx_create(ctypes.byref(P), ctypes.byref(h)))

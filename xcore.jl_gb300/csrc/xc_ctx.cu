@@ -82,9 +82,10 @@ extern "C" int xc_ctx_create(const xc_params* par, xc_ctx** out) {
   if (!par || !out) { xc_set_error("xc_ctx_create: null argument"); return XC_BAD_ARG; }
   *out = nullptr;
   if (par->Nz < 3 || par->Nx < 3 || !(par->h > 0) || !bc_ok(par->xBC) || !bc_ok(par->zBC) ||
-      scheme_halo(par->ADVN) < 0 || par->TINT < 0 || par->TINT > 3) {
-    xc_set_error("xc_ctx_create: bad parameters (Nz=%d Nx=%d h=%g ADVN=%d TINT=%d)", par->Nz,
-                 par->Nx, par->h, par->ADVN, par->TINT);
+      par->ADVN < XC_CENTR || par->ADVN > XC_TVDIM || par->TINT < 0 || par->TINT > 3 ||
+      par->weno_weights < 0 || par->weno_weights > 1) {
+    xc_set_error("xc_ctx_create: bad parameters (Nz=%d Nx=%d h=%g ADVN=%d TINT=%d weno_weights=%d)", par->Nz,
+                 par->Nx, par->h, par->ADVN, par->TINT, par->weno_weights);
     return XC_BAD_ARG;
   }
   int ndev = 0;
@@ -239,6 +240,7 @@ extern "C" int xc_phsevo(xc_ctx* c, int scheme, const double coefs[6], double dt
   XC_TRY(check_ctx(c));
   if (!coefs) { xc_set_error("xc_phsevo: null coefs"); return XC_BAD_ARG; }
   if (scheme < 0) scheme = c->p.ADVN;
+  if (scheme > XC_TVDIM) { xc_set_error("xc_phsevo: unknown scheme %d", scheme); return XC_BAD_ARG; }
   return phsevo_impl(c, scheme, coefs, dt, alpha);
 }
 
@@ -491,7 +493,7 @@ extern "C" int xc_bench_kernel(xc_ctx* c, int which, int iters, double out[4]) {
   int st = XC_OK;
   for (int it = -1; it < iters && st == XC_OK; ++it) {
     if (it == 0) cudaEventRecord(e0, c->stream);
-    st = stencil_advect_flux(X.p, X.ld, false, Nz, Nx, c->p.ADVN, c->p.xBC, c->p.zBC, Ux_face, Wx_face, c->p.h,
+    st = stencil_advect_flux(X.p, X.ld, false, Nz, Nx, advect_scheme(c->p.ADVN, c->p), c->p.xBC, c->p.zBC, Ux_face, Wx_face, c->p.h,
                              F(c, FLD_advn_X), qxi, qzi, c->stream);
   }
   cudaEventRecord(e1, c->stream);
@@ -503,7 +505,8 @@ extern "C" int xc_bench_kernel(xc_ctx* c, int which, int iters, double out[4]) {
   if (st != XC_OK) return st;
   const double cells = (double)Nz * Nx;
   // WENO5: two upwind reconstructions per cell (one x face, one z face) of
-  // about 66 flops with 6 divisions each, the flux products and the divergence
+  // about 66 flops with 4 divisions each (1 with weno_weights = 1), the flux
+  // products and the divergence
   const double fpc = c->p.ADVN == XC_WENO5 ? 150.0 : (c->p.ADVN == XC_QUICK ? 38.0 : 20.0);
   out[0] = ms / iters;
   out[1] = 48.0 * cells;     // read f, u, w; write adv, qx, qz (8 B each per cell)

@@ -227,6 +227,12 @@ int fetch_scalars(xc_ctx* c, int first, int n);
 // ---------------------------------------------------------------------------
 // entry points implemented per translation unit (status-returning, on c->stream)
 // ---------------------------------------------------------------------------
+// scheme code of WENO5 with its weights over a common denominator (one
+// division per reconstruction), selected by xc_params.weno_weights = 1
+constexpr int kWeno5OneDiv = 105;
+inline int advect_scheme(int scheme, const xc_params& p) {
+  return scheme == XC_WENO5 && p.weno_weights == 1 ? kWeno5OneDiv : scheme;
+}
 int stencil_advect_flux(const double* f, int ldf, bool halod, int Nz, int Nx, int scheme,
                         int xBC, int zBC, CView u, CView w, double h,
                         DView adv, DView qx_int, DView qz_int, cudaStream_t s);

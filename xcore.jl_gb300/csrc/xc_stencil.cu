@@ -43,6 +43,33 @@ __device__ __forceinline__ double weno5_poly(double fmm, double fm, double fc, d
   return ((w1 * p1 + w2 * p2) + w3 * p3) / ((w1 + w2) + w3);
 }
 
+// The same reconstruction with the weights over a common denominator: with
+// q_k = (eps + b_k)^2 the weights d_k / q_k are proportional to
+// n_1 = d_1 q_2 q_3, n_2 = d_2 q_1 q_3, n_3 = d_3 q_1 q_2, so the weighted
+// mean needs one division instead of four (an FP64 division costs about ten
+// times a multiply on this GPU).  Each q_k lies in [eps^2, (eps + b_k)^2]:
+// the products stay normal and finite for fields below about 1e70.
+__device__ __forceinline__ double weno5_poly_onediv(double fmm, double fm, double fc, double fp,
+                                                    double fpp) {
+  const double sixth = 1.0 / 6.0, quarter = 0.25, c1312 = 13.0 / 12.0;
+  const double eps_val = XC_EPS;
+  double p1 = sixth * ((2.0 * fmm - 7.0 * fm) + 11.0 * fc);
+  double p2 = sixth * ((-fm + 5.0 * fc) + 2.0 * fp);
+  double p3 = sixth * ((2.0 * fc + 5.0 * fp) - fpp);
+  double t = (fmm - 2.0 * fm) + fc, s = (fmm - 4.0 * fm) + 3.0 * fc;
+  double b1 = c1312 * (t * t) + quarter * (s * s);
+  t = (fm - 2.0 * fc) + fp;
+  s = fm - fp;
+  double b2 = c1312 * (t * t) + quarter * (s * s);
+  t = (fc - 2.0 * fp) + fpp;
+  s = (3.0 * fc - 4.0 * fp) + fpp;
+  double b3 = c1312 * (t * t) + quarter * (s * s);
+  double e1 = b1 + eps_val, e2 = b2 + eps_val, e3 = b3 + eps_val;
+  double q1 = e1 * e1, q2 = e2 * e2, q3 = e3 * e3;
+  double n1 = 0.1 * (q2 * q3), n2 = 0.6 * (q1 * q3), n3 = 0.3 * (q1 * q2);
+  return ((n1 * p1 + n2 * p2) + n3 * p3) / ((n1 + n2) + n3);
+}
+
 __device__ __forceinline__ double weno3_poly(double fm, double fc, double fp) {
   const double half = 0.5, eps_val = 1e-6;
   double p1 = half * (fc + fp);
@@ -83,7 +110,7 @@ __device__ __forceinline__ double face_flux(double s0, double s1, double s2, dou
     double pos = s2 + 0.25 * (s3 - s1);
     double neg = s3 + 0.25 * (s2 - s4);
     return vpos(v) * pos + vneg(v) * neg;
-  } else if (S == XC_WENO3 || S == XC_WENO5) {
+  } else if (S == XC_WENO3 || S == XC_WENO5 || S == kWeno5OneDiv) {
     // vpos(v) pos + vneg(v) neg has one weight exactly zero: only the upwind
     // reconstruction is evaluated.  The dropped term is (+0) x (finite) = +-0,
     // which changes no value (at most the sign of a zero result); v = +-0
@@ -93,7 +120,9 @@ __device__ __forceinline__ double face_flux(double s0, double s1, double s2, dou
     const bool up = v > 0.0;
     const double a0 = up ? s0 : s5, a1 = up ? s1 : s4, a2 = up ? s2 : s3, a3 = up ? s3 : s2,
                  a4 = up ? s4 : s1;
-    const double p = S == XC_WENO5 ? weno5_poly(a0, a1, a2, a3, a4) : weno3_poly(a1, a2, a3);
+    const double p = S == XC_WENO5        ? weno5_poly(a0, a1, a2, a3, a4)
+                     : S == kWeno5OneDiv ? weno5_poly_onediv(a0, a1, a2, a3, a4)
+                                         : weno3_poly(a1, a2, a3);
     if (up) return vpos(v) * p;
     if (v < 0.0) return vneg(v) * p;
     return v * 0.0;
@@ -105,7 +134,9 @@ __device__ __forceinline__ double face_flux(double s0, double s1, double s2, dou
   }
 }
 
-template <int S> struct Halo { static constexpr int G = (S == XC_WENO5) ? 3 : (S == XC_CENTR || S == XC_UPWD1) ? 1 : 2; };
+template <int S> struct Halo {
+  static constexpr int G = (S == XC_WENO5 || S == kWeno5OneDiv) ? 3 : (S == XC_CENTR || S == XC_UPWD1) ? 1 : 2;
+};
 
 __device__ __forceinline__ int map_bc(int k, int n, int bc) {
   if (bc == XC_PERIODIC) {
@@ -385,7 +416,7 @@ int scheme_halo(int scheme) {
   switch (scheme) {
     case XC_CENTR: case XC_UPWD1: return 1;
     case XC_QUICK: case XC_FROMM: case XC_WENO3: case XC_TVDIM: return 2;
-    case XC_WENO5: return 3;
+    case XC_WENO5: case kWeno5OneDiv: return 3;
     default: return -1;
   }
 }
@@ -407,6 +438,7 @@ int stencil_advect_flux(const double* f, int ldf, bool halod, int Nz, int Nx, in
     case XC_FROMM: return launch_advect<XC_FROMM>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
     case XC_WENO3: return launch_advect<XC_WENO3>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
     case XC_WENO5: return launch_advect<XC_WENO5>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
+    case kWeno5OneDiv: return launch_advect<kWeno5OneDiv>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
     default: return launch_advect<XC_TVDIM>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
   }
 }
@@ -450,6 +482,7 @@ int phsevo_impl(xc_ctx* c, int scheme, const double coefs[6], double dt, double 
   auto qx_int = [&](int id) { DView q = F(c, id); return DView{q.p + 1, q.ld}; };
   auto qz_int = [&](int id) { DView q = F(c, id); return DView{q.p + q.ld, q.ld}; };
   DView X = F(c, FLD_X), M = F(c, FLD_M);
+  scheme = advect_scheme(scheme, c->p);
   XC_TRY(stencil_advect_flux(X.p, X.ld, false, Nz, Nx, scheme, xBC, zBC, Ux_face, Wx_face, h,
                              F(c, FLD_advn_X), qx_int(FLD_qx_advn_X), qz_int(FLD_qz_advn_X), s));
   XC_TRY(stencil_advect_flux(M.p, M.ld, false, Nz, Nx, scheme, xBC, zBC, Um_face, Wm_face, h,
@@ -488,7 +521,7 @@ extern "C" int xc_fill_ghosts(double* f, int Nz, int Nx, int halo, int zBC, int 
 
 extern "C" int xc_advect(double* adv, const double* f_halo, const double* u, const double* w,
                          int Nz, int Nx, double h, int scheme, void* stream) {
-  int g = scheme_halo(scheme);
+  int g = scheme <= XC_TVDIM ? scheme_halo(scheme) : -1;   // the public scheme codes
   if (!adv || !f_halo || !u || !w || g < 0 || Nz < g || Nx < g) {
     xc_set_error("xc_advect: bad arguments (scheme=%d Nz=%d Nx=%d)", scheme, Nz, Nx);
     return XC_BAD_ARG;
@@ -502,7 +535,7 @@ extern "C" int xc_advect(double* adv, const double* f_halo, const double* u, con
 extern "C" int xc_advect_with_flux(double* adv, double* qx, double* qz, const double* f_halo,
                                    const double* u, const double* w, int Nz, int Nx, double h,
                                    int scheme, int xBC, int zBC, void* stream) {
-  int g = scheme_halo(scheme);
+  int g = scheme <= XC_TVDIM ? scheme_halo(scheme) : -1;   // the public scheme codes
   if (!adv || !qx || !qz || !f_halo || !u || !w || g < 0 || Nz < g || Nx < g || !bc_ok(xBC) ||
       !bc_ok(zBC)) {
     xc_set_error("xc_advect_with_flux: bad arguments (scheme=%d Nz=%d Nx=%d)", scheme, Nz, Nx);
@@ -519,7 +552,7 @@ extern "C" int xc_advect_with_flux(double* adv, double* qx, double* qz, const do
 extern "C" int xc_advect_centered_with_flux(double* adv, double* qx, double* qz, const double* f,
                                             const double* u, const double* w, int Nz, int Nx,
                                             double h, int scheme, int xBC, int zBC, void* stream) {
-  int g = scheme_halo(scheme);
+  int g = scheme <= XC_TVDIM ? scheme_halo(scheme) : -1;   // the public scheme codes
   if (!adv || !f || !u || !w || g < 0 || Nz < g || Nx < g || !bc_ok(xBC) || !bc_ok(zBC) ||
       ((qx == nullptr) != (qz == nullptr))) {
     xc_set_error("xc_advect_centered_with_flux: bad arguments (scheme=%d Nz=%d Nx=%d)", scheme, Nz, Nx);

@@ -2151,6 +2151,26 @@ struct SolveCfg {
   // FP32 velocity sweeps with four rows along z per thread (vel_sweep_rb_kernel;
   // opt-in: measured 20% slower at 1024^2 than one row per thread)
   bool row_block = false;
+  // the Hessenberg least-squares problem of FGMRES on the host, one
+  // synchronisation per Arnoldi step, instead of on the device
+  bool host_givens = false;
+};
+
+// The least-squares problem of (F)GMRES(m) on the device: the Hessenberg
+// columns, their Givens rotations, the rotated right-hand side g and the
+// iteration counters.  Written by one thread at the end of every Arnoldi
+// step, so the host needs no synchronisation between steps.
+struct KrylovDev {
+  double Hm[(kMaxRestart + 1) * kMaxRestart];   // column j at Hm[j * (kMaxRestart + 1)]
+  double cs[kMaxRestart], sn[kMaxRestart], gv[kMaxRestart + 1], yv[kMaxRestart];
+  double bnorm, stop, relres;
+  int its, maxit, kk, done, bad;
+};
+// what the host reads between steps (pinned, mapped into the device's
+// address space; written by the same thread after each step)
+struct KrylovStatus {
+  double relres;
+  int its, kk, done, bad;
 };
 
 }  // namespace
@@ -2208,6 +2228,16 @@ struct Hier {
   long long gnodes[2][kMaxRestart];
   unsigned long long gkey[2];
   int glast;
+  // the same steps as conditional graphs (a gate kernel, then the step and
+  // its Givens update only while the solve has not stopped), per key set;
+  // cnodes = kernels of the gate and of the body
+  cudaGraphExec_t cexec[2][kMaxRestart];
+  long long cnodes[2][kMaxRestart][2];
+  KrylovDev* kd;
+  KrylovStatus* ks_host;
+  KrylovStatus* ks_dev;
+  cudaEvent_t kev[2];
+  bool cond_broken;   // building a conditional graph failed: host Givens from then on
 };
 
 struct StokesWork {
@@ -2242,6 +2272,7 @@ struct StokesWork {
   double* nn_dv;        // 2 n: training samples' V-cycle result and its residual
   bool last_fp64_mg;    // the last solve set up the FP64 multigrid
   SolveCfg last_cfg;
+  long long dev_steps;  // Arnoldi steps of the current solve with the least-squares update on the device
 };
 
 namespace {
@@ -2310,14 +2341,26 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
   XC_CUDA_TRY(cudaMalloc(&H.rv, sizeof(T) * (g.NW + g.NU)));
   XC_CUDA_TRY(cudaMalloc(&H.rp, sizeof(T) * g.NP));
   XC_CUDA_TRY(cudaMalloc(&H.rin, sizeof(T) * g.Nz * g.Nx));
+  XC_CUDA_TRY(cudaMalloc(&H.kd, sizeof(KrylovDev)));
+  XC_CUDA_TRY(cudaMemset(H.kd, 0, sizeof(KrylovDev)));
+  XC_CUDA_TRY(cudaHostAlloc(&H.ks_host, sizeof(KrylovStatus), cudaHostAllocMapped));
+  std::memset(H.ks_host, 0, sizeof(KrylovStatus));
+  XC_CUDA_TRY(cudaHostGetDevicePointer((void**)&H.ks_dev, H.ks_host, 0));
+  for (int q = 0; q < 2; ++q) XC_CUDA_TRY(cudaEventCreateWithFlags(&H.kev[q], cudaEventDisableTiming));
   return XC_OK;
 }
 
 template <typename T>
 void free_hier(Hier<T>& H) {
   for (int e = 0; e < 2; ++e)
-    for (int q = 0; q < kMaxRestart; ++q)
+    for (int q = 0; q < kMaxRestart; ++q) {
       if (H.gexec[e][q]) { cudaGraphExecDestroy(H.gexec[e][q]); H.gexec[e][q] = nullptr; }
+      if (H.cexec[e][q]) { cudaGraphExecDestroy(H.cexec[e][q]); H.cexec[e][q] = nullptr; }
+    }
+  cudaFree(H.kd);
+  if (H.ks_host) cudaFreeHost(H.ks_host);
+  for (int q = 0; q < 2; ++q)
+    if (H.kev[q]) cudaEventDestroy(H.kev[q]);
   for (int l = 0; l < H.nv; ++l) {
     cudaFree(H.cw[l]); cudaFree(H.cu[l]); cudaFree(H.vx[l]); cudaFree(H.vx2[l]); cudaFree(H.vb[l]); cudaFree(H.vr[l]);
     cudaFree(H.feta[l]); cudaFree(H.fetaco[l]); cudaFree(H.fdw[l]); cudaFree(H.fdu[l]); cudaFree(H.fdbot[l]);
@@ -2757,7 +2800,7 @@ int apply_precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& c
 // hdev[2]; v_{k+1} = w / ||w||; the H column to the pinned host mirror.
 template <typename T>
 int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s,
-                     bool with_precond = true) {
+                     bool with_precond = true, bool host_copy = true) {
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   T* vk = H.V + (size_t)kk * n;
@@ -2774,9 +2817,110 @@ int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg
   }
   XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
   pdl(PDL_ON, normalize_kernel<T>, nblk(n), 256, s, n, w->hdev + 6, wv);
-  XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
+  if (host_copy)
+    XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
   XC_LAUNCH_CHECK();
   return XC_OK;
+}
+
+// ---- the FGMRES least-squares problem on the device --------------------------
+// A restart cycle starts from g = (beta, 0, ...); its counters carry the
+// iterations of earlier cycles of the same solve.
+__global__ void krylov_start_kernel(KrylovDev* kd, double beta, double bnorm, double stop, int maxit, int its) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = 0; i <= kMaxRestart; ++i) kd->gv[i] = 0.0;
+  kd->gv[0] = beta;
+  kd->bnorm = bnorm;
+  kd->stop = stop;
+  kd->relres = beta / bnorm;
+  kd->maxit = maxit;
+  kd->its = its;
+  kd->kk = 0;
+  kd->done = 0;
+  kd->bad = 0;
+}
+
+// the IF condition of an Arnoldi step's graph: run the step only while the
+// cycle has not met its target, broken down or used up its iterations
+__global__ void krylov_gate_kernel(const KrylovDev* kd, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  cudaGraphSetConditional(h, (kd->done == 0 && kd->its < kd->maxit) ? 1u : 0u);
+}
+
+// column kk of the Hessenberg matrix from the Gram-Schmidt coefficients (one
+// or two passes, summed; hd[8..], hd[8 + kMaxRestart..]) and ||w||^2 (hd[2]);
+// the earlier rotations applied to it, a new rotation zeroing its subdiagonal
+// entry, the residual estimate |g_{kk+1}| / ||rhs||.  The same operations as
+// the host's least-squares update.
+__global__ void krylov_givens_kernel(KrylovDev* kd, const double* __restrict__ hd, int two_pass, int kk,
+                                     KrylovStatus* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double* col = kd->Hm + (size_t)kk * (kMaxRestart + 1);
+  const double* h1 = hd + 8;
+  const double* h2 = hd + 8 + kMaxRestart;
+  for (int i = 0; i <= kk; ++i) col[i] = h1[i] + (two_pass ? h2[i] : 0.0);
+  const double hn = sqrt(hd[2]);
+  col[kk + 1] = hn;
+  for (int i = 0; i < kk; ++i) {
+    const double a = col[i], b = col[i + 1];
+    col[i] = kd->cs[i] * a + kd->sn[i] * b;
+    col[i + 1] = -kd->sn[i] * a + kd->cs[i] * b;
+  }
+  const double a = col[kk], b = col[kk + 1];
+  const double r = hypot(a, b);
+  kd->cs[kk] = r > 0 ? a / r : 1.0;
+  kd->sn[kk] = r > 0 ? b / r : 0.0;
+  col[kk] = r;
+  col[kk + 1] = 0.0;
+  kd->gv[kk + 1] = -kd->sn[kk] * kd->gv[kk];
+  kd->gv[kk] = kd->cs[kk] * kd->gv[kk];
+  const double relres = fabs(kd->gv[kk + 1]) / kd->bnorm;
+  const int bad = !isfinite(relres);
+  kd->its += 1;
+  kd->kk = kk + 1;
+  kd->relres = relres;
+  if (bad || relres <= kd->stop || hn == 0.0) kd->done = 1;
+  kd->bad |= bad;
+  status->relres = relres;
+  status->its = kd->its;
+  status->kk = kd->kk;
+  status->done = kd->done;
+  status->bad = kd->bad;
+  __threadfence_system();
+}
+
+// back substitution for the coefficients of the cycle's kk basis vectors
+// (to coef[0..kk)), and a final status for the host
+__global__ void krylov_solve_kernel(KrylovDev* kd, double* coef, KrylovStatus* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int kk = kd->kk;
+  for (int i = kk - 1; i >= 0; --i) {
+    double sacc = kd->gv[i];
+    for (int j = i + 1; j < kk; ++j) sacc -= kd->Hm[(size_t)j * (kMaxRestart + 1) + i] * kd->yv[j];
+    kd->yv[i] = sacc / kd->Hm[(size_t)i * (kMaxRestart + 1) + i];
+    coef[i] = kd->yv[i];
+  }
+  status->relres = kd->relres;
+  status->its = kd->its;
+  status->kk = kk;
+  status->done = kd->done;
+  status->bad = kd->bad;
+  __threadfence_system();
+}
+
+// x += Z coef over the kk basis vectors the cycle used (kk read on the device)
+template <typename T>
+__global__ void combine_dev_kernel(long long n, const KrylovDev* __restrict__ kd, const T* __restrict__ Z,
+                                   long long ldz, const double* __restrict__ coef, T* x) {
+  __shared__ T ys[kMaxRestart];
+  const int m = kd->kk;
+  if (threadIdx.x < m) ys[threadIdx.x] = (T)coef[threadIdx.x];
+  __syncthreads();
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  T s = x[t];
+  for (int k = 0; k < m; ++k) s += ys[k] * Z[(size_t)k * ldz + t];
+  x[t] = s;
 }
 
 unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
@@ -2793,8 +2937,10 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
 
 template <typename T>
 void drop_graphs(Hier<T>& H, int e) {
-  for (int q = 0; q < kMaxRestart; ++q)
+  for (int q = 0; q < kMaxRestart; ++q) {
     if (H.gexec[e][q]) { cudaGraphExecDestroy(H.gexec[e][q]); H.gexec[e][q] = nullptr; }
+    if (H.cexec[e][q]) { cudaGraphExecDestroy(H.cexec[e][q]); H.cexec[e][q] = nullptr; }
+  }
   H.gkey[e] = 0;
 }
 
@@ -2831,6 +2977,82 @@ int arnoldi_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cf
   }
   XC_CUDA_TRY(cudaGraphLaunch(gexec[kk], s));
   g_xc_launches.fetch_add(gnodes[kk]);
+  return XC_OK;
+}
+
+// Arnoldi step kk as a conditional graph: a gate kernel sets the IF condition
+// from the device least-squares state, and the body -- the step's launches
+// without the host copy, then the Givens update -- runs only while the cycle
+// goes on.  Returns XC_CUDA (with the reason) when the graph cannot be built.
+template <typename T>
+int build_cond_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s,
+                    cudaGraphExec_t* exec, long long nodes[2]) {
+  cudaGraph_t graph = nullptr;
+  XC_CUDA_TRY(cudaGraphCreate(&graph, 0));
+  auto fail = [&](cudaError_t e, const char* what) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    xc_set_error("conditional Arnoldi graph: %s: %s", what, cudaGetErrorString(e));
+    return XC_CUDA;
+  };
+  cudaGraphConditionalHandle handle;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e, "handle");
+  KrylovDev* kd = H.kd;
+  void* gate_args[2] = {&kd, &handle};
+  cudaKernelNodeParams kp = {};
+  kp.func = (void*)krylov_gate_kernel;
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(32);
+  kp.kernelParams = gate_args;
+  cudaGraphNode_t gate;
+  e = cudaGraphAddKernelNode(&gate, graph, nullptr, 0, &kp);
+  if (e != cudaSuccess) return fail(e, "gate node");
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  e = cudaGraphAddNode(&cnode, graph, &gate, nullptr, 1, &cp);
+  if (e != cudaSuccess) return fail(e, "conditional node");
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture");
+  const long long before = g_xc_thread_launches;
+  int st = arnoldi_launches<T>(w, H, k, cfg, kk, s, true, false);
+  if (st == XC_OK) {
+    krylov_givens_kernel<<<1, 32, 0, s>>>(H.kd, w->hdev, cfg.gs_passes > 1 ? 1 : 0, kk, H.ks_dev);
+    xc_count_launch();
+  }
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(s, &captured);
+  nodes[0] = 1;
+  nodes[1] = g_xc_thread_launches - before;
+  g_xc_thread_launches = before;
+  g_xc_launches.fetch_sub(nodes[1]);
+  if (st != XC_OK) { cudaGraphDestroy(graph); return st; }
+  if (e != cudaSuccess) return fail(e, "end capture");
+  e = cudaGraphInstantiate(exec, graph, 0);
+  if (e != cudaSuccess) { *exec = nullptr; return fail(e, "instantiate"); }
+  cudaGraphDestroy(graph);
+  return XC_OK;
+}
+
+// the conditional graph of step kk for this configuration, built on first use
+template <typename T>
+int cond_step(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, int kk, cudaStream_t s) {
+  const unsigned long long key = graph_key(k, cfg);
+  int e = H.gkey[0] == key ? 0 : (H.gkey[1] == key ? 1 : -1);
+  if (e < 0) {
+    e = 1 - H.glast;
+    drop_graphs(H, e);
+    H.gkey[e] = key;
+  }
+  H.glast = e;
+  if (!H.cexec[e][kk]) XC_TRY(build_cond_step<T>(w, H, k, cfg, kk, s, &H.cexec[e][kk], H.cnodes[e][kk]));
+  XC_CUDA_TRY(cudaGraphLaunch(H.cexec[e][kk], s));
+  g_xc_launches.fetch_add(H.cnodes[e][kk][0]);
   return XC_OK;
 }
 
@@ -2931,6 +3153,49 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
       if (!(relres > rtol) || its >= maxit) break;
       if (!std::isfinite(beta)) { *its_out = its; *relres_out = relres; xc_set_error("fgmres: non-finite residual"); return XC_NAN; }
       scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, H.V, H.V); xc_count_launch();
+    }
+    if (!cfg.host_givens && !H.cond_broken) {
+      // the cycle with the least-squares problem on the device: the host
+      // queues step kk + 1 before it looks at step kk's outcome, so the GPU
+      // never waits for it; a step queued after the cycle stopped is skipped
+      // by its gate
+      krylov_start_kernel<<<1, 32, 0, s>>>(H.kd, beta, bnorm, rtol * 0.5, maxit, its);
+      xc_count_launch();
+      const int its0 = its;
+      int launched = 0, st = XC_OK;
+      for (int kk = 0; kk < m; ++kk) {
+        st = cond_step<T>(w, H, k, cfg, kk, s);
+        if (st != XC_OK) break;
+        XC_CUDA_TRY(cudaEventRecord(H.kev[kk & 1], s));
+        ++launched;
+        if (kk >= 1) {
+          XC_CUDA_TRY(cudaEventSynchronize(H.kev[(kk - 1) & 1]));
+          const volatile KrylovStatus* ks = H.ks_host;
+          if (ks->done || ks->its >= maxit) break;
+        }
+      }
+      if (st != XC_OK && launched == 0 && its == its0) {
+        // no conditional graph could be built (nothing ran): host Givens
+        // for this hierarchy from now on
+        H.cond_broken = true;
+      } else {
+        if (st != XC_OK) return st;
+        krylov_solve_kernel<<<1, 32, 0, s>>>(H.kd, w->hdev + 8, H.ks_dev);
+        xc_count_launch();
+        combine_dev_kernel<T><<<nblk(n), 256, 0, s>>>(n, H.kd, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
+        XC_LAUNCH_CHECK();
+        XC_CUDA_TRY(cudaStreamSynchronize(s));
+        const volatile KrylovStatus* ks = H.ks_host;
+        const int ran = ks->its - its0;
+        const int e = H.glast;
+        for (int q = 0; q < ran && q < m; ++q) g_xc_launches.fetch_add(H.cnodes[e][q][1]);
+        w->dev_steps += ran;
+        its = ks->its;
+        relres = ks->relres;
+        if (ks->bad) { xc_set_error("fgmres: breakdown"); *its_out = its; *relres_out = relres; return XC_NAN; }
+        if ((flags & FG_TRUST_EST) && (relres <= rtol || its >= maxit)) break;
+        continue;
+      }
     }
     ls.start(beta);
     int kk = 0;
@@ -3285,6 +3550,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   const long long n = (long long)g.NW + g.NU + g.NP;
   cudaStream_t s = c->stream;
   const xc_params& p = c->p;
+  w->dev_steps = 0;
   XC_CUDA_TRY(cudaEventRecord(w->ev0, s));
   dim3 blk(32, 8);
   // MFS update + mean (fluidmech.jl:115-127)
@@ -3302,9 +3568,9 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
                                                               CF(c, FLD_rhou), w->fz, w->uz, w->wz, w->fx, w->ux,
                                                               w->wx); xc_count_launch();
   XC_LAUNCH_CHECK();
-  XC_TRY(stencil_advect_flux(w->fz, Nz - 1, false, Nz - 1, Nx, p.ADVN, p.xBC, p.zBC, CView{w->uz, Nz - 1},
+  XC_TRY(stencil_advect_flux(w->fz, Nz - 1, false, Nz - 1, Nx, advect_scheme(p.ADVN, p), p.xBC, p.zBC, CView{w->uz, Nz - 1},
                              CView{w->wz, Nz}, p.h, DView{w->advz, Nz - 1}, DView{nullptr, 0}, DView{nullptr, 0}, s));
-  XC_TRY(stencil_advect_flux(w->fx, Nz, false, Nz, Nx + 1, p.ADVN, p.xBC, p.zBC, CView{w->ux, Nz},
+  XC_TRY(stencil_advect_flux(w->fx, Nz, false, Nz, Nx + 1, advect_scheme(p.ADVN, p), p.xBC, p.zBC, CView{w->ux, Nz},
                              CView{w->wx, Nz + 1}, p.h, DView{w->advx, Nz}, DView{nullptr, 0}, DView{nullptr, 0}, s));
   // operator constants
   OpConst k;
@@ -3382,6 +3648,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   cfg.pdl = !o.serial_launch;
   cfg.tiled = o.tiled_sweep != 0;
   cfg.row_block = o.row_block_sweep != 0;
+  cfg.host_givens = o.host_givens != 0;
   cfg.stage_small = o.stage_small_levels != 0;
   cfg.direct_coarse = !o.jacobi_coarse;
   if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;
@@ -3530,6 +3797,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     stats->converged = relres <= o.rtol;
     stats->seconds = ms * 1e-3;
     stats->learned_fallbacks = fallbacks;
+    stats->device_givens_steps = (int)w->dev_steps;
   }
   if (o.learned != 0) XC_TRY(nn_check(w->net, s));
   if (status != XC_OK) return status;

@@ -34,6 +34,7 @@ struct XcParams
     G0::Cdouble; bnd_w::Cdouble; dt0::Cdouble
     ADVN::Cint; TINT::Cint; xBC::Cint; zBC::Cint
     sds::Cint; top_cnv::Cint; bot_cnv::Cint; open_cnv::Cint
+    weno_weights::Cint
 end
 
 struct SolverOpts
@@ -42,13 +43,14 @@ struct SolverOpts
     coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint; pressure_sweeps::Cint; inner_gs_passes::Cint
     serial_launch::Cint; coarse_viscosity_mean::Cint; tiled_sweep::Cint; post_sweeps::Cint; outer_solver::Cint
     fused_pressure_cells::Cint; stage_small_levels::Cint; jacobi_coarse::Cint; row_block_sweep::Cint; learned::Cint
+    host_givens::Cint
 end
 SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
-    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
 
 struct SolverStats
     iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
-    learned_fallbacks::Cint
+    learned_fallbacks::Cint; device_givens_steps::Cint
 end
 
 const MAX_SWEEPS = 64
@@ -71,13 +73,13 @@ check(st) = st == 0 ? nothing :
 row(m) = (Cdouble(m[1, 1]), Cdouble(m[1, 2]), Cdouble(m[2, 1]), Cdouble(m[2, 2]))
 
 function Context(par, grid, scales; xBC = :periodic, zBC = :closed, sds = -1, top_cnv = 1, bot_cnv = 1,
-                 open_cnv = false)
+                 open_cnv = false, weno_weights = 0)
     p = XcParams(grid.Nz, grid.Nx, grid.h, par.D, par.rhom0, par.rhox0, par.d0, par.g0, par.etam0, par.etax0,
                  row(par.AA), row(par.BB), row(par.CC), par.Xi, par.Ptop, par.alpha, par.gamma, par.CFL,
                  par.dtmax, par.etacntr, par.open_sgr,
                  scales.L0, scales.l0, scales.L0h, scales.l0h, scales.D0, scales.txi0, scales.G0, scales.bnd_w,
                  scales.dt0, SCHEMES[par.ADVN], TINTS[par.TINT], BCS[xBC], BCS[zBC], sds, top_cnv, bot_cnv,
-                 open_cnv)
+                 open_cnv, weno_weights)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:xc_ctx_create, LIB), Cint, (Ref{XcParams}, Ref{Ptr{Cvoid}}), p, h))
     ctx = Context(h[], grid.Nz, grid.Nx)
@@ -216,7 +218,7 @@ end
 # reduction in at most 30 iterations, one pressure-multigrid sweep
 step_solver_opts(solver::Symbol, rtol; learned = 0) =
     SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 5e-2, 30,
-               0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, learned)
+               0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, learned, 0)
 
 # status 2 (XC_NOT_CONVERGED) from a step means the step was completed but a
 # Stokes solve stopped at its cap: raise with the step statistics
