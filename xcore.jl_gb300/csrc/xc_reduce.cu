@@ -57,17 +57,16 @@ struct RedBatch {
   RedJob job[kMaxRedJobs];
 };
 
-__global__ void __launch_bounds__(RB) batch_reduce_kernel(RedBatch B, double* partials, unsigned* counters) {
-  __shared__ double sh[RB / 32];
-  __shared__ int last;
-  const RedJob& J = B.job[blockIdx.y];
-  if ((int)blockIdx.x >= J.nblk) return;
-  const int op = J.op;
-  const int comb = (op == RED_SUMSQ || op == RED_SUMSQDIFF || op == RED_SUMLOG || J.center) ? RED_SUM : op;
-  const double ctr = J.center ? *J.center : 0.0;
-  double acc = red_identity(comb);
-  // linear index t over rows x cols (column-major), advanced by a fixed
-  // stride without a per-element division
+// One thread's share of a reduction: the element transform and the combine
+// fixed at compile time.  (With the operation switched per element, the
+// compiler predicates every case, and on GB300's narrow FP64 pipe the
+// predicated-off FP64 instructions cost as much issue time as the live ones.)
+// The linear index t over rows x cols (column-major) advances by a fixed
+// stride without a per-element division.
+template <int OP, bool CENTER>
+__device__ __forceinline__ double red_thread(const RedJob& J, double ctr) {
+  constexpr int COMB = (OP == RED_SUMSQ || OP == RED_SUMSQDIFF || OP == RED_SUMLOG || CENTER) ? RED_SUM : OP;
+  double acc = red_identity(COMB);
   const long long n = (long long)J.rows * J.cols;
   const long long stride = (long long)J.nblk * RB;
   const int sq = (int)(stride / J.rows), sr = (int)(stride % J.rows);
@@ -76,22 +75,49 @@ __global__ void __launch_bounds__(RB) batch_reduce_kernel(RedBatch B, double* pa
   for (; t < n; t += stride) {
     const double a = J.a[(size_t)i * J.lda + j];
     double v;
-    if (J.center) {
+    if (CENTER) {
       const double d = a - ctr;
       v = d * d;
+    } else if (OP == RED_SUMSQ) {
+      v = a * a;
+    } else if (OP == RED_MAXABS) {
+      v = fabs(a);
+    } else if (OP == RED_SUMSQDIFF) {
+      const double d = a - J.b[(size_t)i * J.ldb + j];
+      v = d * d;
+    } else if (OP == RED_SUMLOG) {
+      v = log(jmax(a, J.floor));
     } else {
-      switch (op) {
-        case RED_SUMSQ: v = a * a; break;
-        case RED_MAXABS: v = fabs(a); break;
-        case RED_SUMSQDIFF: { const double d = a - J.b[(size_t)i * J.ldb + j]; v = d * d; } break;
-        case RED_SUMLOG: v = log(jmax(a, J.floor)); break;
-        default: v = a; break;
-      }
+      v = a;
     }
-    acc = red_combine(comb, acc, v);
+    acc = red_combine(COMB, acc, v);
     j += sr;
     i += sq;
     if (j >= J.rows) { j -= J.rows; ++i; }
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(RB) batch_reduce_kernel(RedBatch B, double* partials, unsigned* counters) {
+  __shared__ double sh[RB / 32];
+  __shared__ int last;
+  const RedJob& J = B.job[blockIdx.y];
+  if ((int)blockIdx.x >= J.nblk) return;
+  const int op = J.op;
+  const int comb = (op == RED_SUMSQ || op == RED_SUMSQDIFF || op == RED_SUMLOG || J.center) ? RED_SUM : op;
+  double acc;
+  if (J.center) {
+    acc = red_thread<RED_SUM, true>(J, *J.center);
+  } else {
+    switch (op) {   // uniform per CTA: a branch, not per-element predication
+      case RED_MAX: acc = red_thread<RED_MAX, false>(J, 0.0); break;
+      case RED_MIN: acc = red_thread<RED_MIN, false>(J, 0.0); break;
+      case RED_SUMSQ: acc = red_thread<RED_SUMSQ, false>(J, 0.0); break;
+      case RED_MAXABS: acc = red_thread<RED_MAXABS, false>(J, 0.0); break;
+      case RED_SUMSQDIFF: acc = red_thread<RED_SUMSQDIFF, false>(J, 0.0); break;
+      case RED_SUMLOG: acc = red_thread<RED_SUMLOG, false>(J, 0.0); break;
+      default: acc = red_thread<RED_SUM, false>(J, 0.0); break;
+    }
   }
   double r = block_reduce(comb, acc, sh);
   double* part = partials + (size_t)blockIdx.y * RG;

@@ -1852,7 +1852,10 @@ constexpr int KGMAX = 8 * kNumSMs;   // partial-sum slots: at most 8 CTAs of 256
 // GB300), then warps and the CTA combine them in FP64.  MAXK (8, 16, 32) is
 // picked by the host so that few accumulators keep the occupancy high; the
 // grid-stride loop takes two elements per step for more loads in flight.
-template <typename T, int MAXK>
+// EXACT: m == MAXK (instantiated for 1..8 basis vectors), so no accumulator
+// slot is predicated off -- a predicated-off FP64 FMA still takes an issue
+// slot on GB300's narrow FP64 pipe; otherwise m <= MAXK
+template <typename T, int MAXK, bool EXACT = false>
 __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
                                                       const T* __restrict__ w, double* part) {
   XC_PDL_WAIT();
@@ -1866,7 +1869,7 @@ __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const 
     const T w0 = w[t], w1 = w[t + stride];
 #pragma unroll
     for (int k = 0; k < MAXK; ++k)
-      if (k < m) {
+      if (EXACT || k < m) {
         const T* vk = V + (size_t)k * ldv;
         acc[k] += vk[t] * w0;
         acc[k] += vk[t + stride] * w1;
@@ -1876,15 +1879,18 @@ __global__ void __launch_bounds__(KB) multidot_kernel(long long n, int m, const 
     const T w0 = w[t];
 #pragma unroll
     for (int k = 0; k < MAXK; ++k)
-      if (k < m) acc[k] += V[(size_t)k * ldv + t] * w0;
+      if (EXACT || k < m) acc[k] += V[(size_t)k * ldv + t] * w0;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // the warp's 32 partial sums are added in the working precision (in FP64
+  // each would cost a conversion and five additions on the narrow FP64 pipe
+  // per thread); warps and CTAs are combined in FP64
 #pragma unroll
   for (int k = 0; k < MAXK; ++k) {
-    if (k < m) {
-      double v = (double)acc[k];
+    if (EXACT || k < m) {
+      T v = acc[k];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) sh[warp][k] = v;
+      if (lane == 0) sh[warp][k] = (double)v;
     }
   }
   __syncthreads();
@@ -1936,7 +1942,8 @@ __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, lo
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
   T s = w[t];
-  for (int k = 0; k < m; ++k) s -= hs[k] * V[(size_t)k * ldv + t];
+  const T* vk = V + t;
+  for (int k = 0; k < m; ++k, vk += ldv) s -= hs[k] * *vk;
   w[t] = s;
 }
 // x += sum_k y[k] Z[k]
@@ -1950,24 +1957,33 @@ __global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
   T s = x[t];
-  for (int k = 0; k < m; ++k) s += ys[k] * Z[(size_t)k * ldz + t];
+  const T* zk = Z + t;
+  for (int k = 0; k < m; ++k, zk += ldz) s += ys[k] * *zk;
   x[t] = s;
 }
 // v = w * inv with a scale factor computed once elsewhere (a per-CTA FP64
-// reciprocal in front of a barrier stalls every CTA of the grid)
+// reciprocal in front of a barrier stalls every CTA of the grid).  The factor
+// is converted to T once per CTA: a conversion from FP64 issues on GB300's
+// narrow FP64 pipe, and one per element made these FP32 kernels FP64-bound.
 template <typename T>
 __global__ void scale_kernel(long long n, const double* __restrict__ inv, const T* __restrict__ w, T* v) {
   XC_PDL_WAIT();
+  __shared__ T f;
+  if (threadIdx.x == 0) f = (T)__ldg(inv);
+  __syncthreads();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t < n) v[t] = w[t] * (T)__ldg(inv);
+  if (t < n) v[t] = w[t] * f;
 }
 // v *= inv (inv = 1/||v|| from norm_final_kernel; 1 on a zero norm, which the
 // host reports as breakdown)
 template <typename T>
 __global__ void normalize_kernel(long long n, const double* __restrict__ inv, T* v) {
   XC_PDL_WAIT();
+  __shared__ T f;
+  if (threadIdx.x == 0) f = (T)__ldg(inv);
+  __syncthreads();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t < n) v[t] = v[t] * (T)__ldg(inv);
+  if (t < n) v[t] = v[t] * f;
 }
 
 // ---------------------------------------------------------------------------
@@ -2151,9 +2167,9 @@ struct SolveCfg {
   // FP32 velocity sweeps with four rows along z per thread (vel_sweep_rb_kernel;
   // opt-in: measured 20% slower at 1024^2 than one row per thread)
   bool row_block = false;
-  // the Hessenberg least-squares problem of FGMRES on the host, one
-  // synchronisation per Arnoldi step, instead of on the device
-  bool host_givens = false;
+  // the Hessenberg least-squares problem of FGMRES on the device (conditional
+  // graphs) instead of on the host with one synchronisation per Arnoldi step
+  bool device_givens = false;
 };
 
 // The least-squares problem of (F)GMRES(m) on the device: the Hessenberg
@@ -2645,8 +2661,19 @@ template <typename T>
 int launch_multidot(long long n, int m, const T* V, long long ldv, const T* wv, double* part, cudaStream_t s) {
   const int* gr = g_md_grid[std::is_same<T, float>::value ? 0 : 1];
   int nb;
-  if (m <= 8) pdl(PDL_ON, multidot_kernel<T, 8>, (nb = gr[0]), KB, s, n, m, V, ldv, wv, part);
-  else if (m <= 16) pdl(PDL_ON, multidot_kernel<T, 16>, (nb = gr[1]), KB, s, n, m, V, ldv, wv, part);
+  nb = gr[0];
+  switch (m) {
+    case 1: pdl(PDL_ON, multidot_kernel<T, 1, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 2: pdl(PDL_ON, multidot_kernel<T, 2, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 3: pdl(PDL_ON, multidot_kernel<T, 3, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 4: pdl(PDL_ON, multidot_kernel<T, 4, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 5: pdl(PDL_ON, multidot_kernel<T, 5, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 6: pdl(PDL_ON, multidot_kernel<T, 6, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 7: pdl(PDL_ON, multidot_kernel<T, 7, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    case 8: pdl(PDL_ON, multidot_kernel<T, 8, true>, nb, KB, s, n, m, V, ldv, wv, part); return nb;
+    default: break;
+  }
+  if (m <= 16) pdl(PDL_ON, multidot_kernel<T, 16>, (nb = gr[1]), KB, s, n, m, V, ldv, wv, part);
   else pdl(PDL_ON, multidot_kernel<T, 32>, (nb = gr[2]), KB, s, n, m, V, ldv, wv, part);
   return nb;
 }
@@ -3154,7 +3181,7 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
       if (!std::isfinite(beta)) { *its_out = its; *relres_out = relres; xc_set_error("fgmres: non-finite residual"); return XC_NAN; }
       scale_kernel<T><<<nblk(n), 256, 0, s>>>(n, w->hdev + 6, H.V, H.V); xc_count_launch();
     }
-    if (!cfg.host_givens && !H.cond_broken) {
+    if (cfg.device_givens && !H.cond_broken) {
       // the cycle with the least-squares problem on the device: the host
       // queues step kk + 1 before it looks at step kk's outcome, so the GPU
       // never waits for it; a step queued after the cycle stopped is skipped
@@ -3648,7 +3675,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   cfg.pdl = !o.serial_launch;
   cfg.tiled = o.tiled_sweep != 0;
   cfg.row_block = o.row_block_sweep != 0;
-  cfg.host_givens = o.host_givens != 0;
+  cfg.device_givens = o.device_givens != 0;
   cfg.stage_small = o.stage_small_levels != 0;
   cfg.direct_coarse = !o.jacobi_coarse;
   if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;

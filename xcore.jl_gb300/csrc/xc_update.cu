@@ -27,7 +27,7 @@ __device__ __forceinline__ double clampd(double x, double lo, double hi) {
 }
 
 struct Rheo {
-  double A11, A12, A21, A22, B11, B12, B21, B22, iC11, iC12, iC21, iC22, ex, em;
+  double A11, A12, A21, A22, lB11, lB12, lB21, lB22, iC11, iC12, iC21, iC22, ex, em;   // lB = log(B)
   double lmx, lxm;   // log(em / ex), log(ex / em)
 };
 
@@ -53,11 +53,15 @@ __global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rho
   // extra precision, which costs about twice the FP64 work; the relative error
   // of exp(y log x) is |y log x| eps, below 2e-14 for these operands (f >= eps,
   // 1/C and the fractions Xf of order one), far inside the 1e-12 bound of
-  // these fields.
-  double s11 = exp(r.iC11 * log(f1 / r.B11)), s12 = exp(r.iC12 * log(f2 / r.B12));
-  double s21 = exp(r.iC21 * log(f1 / r.B21)), s22 = exp(r.iC22 * log(f2 / r.B22));
-  double n1 = s11 + s12, n2 = s21 + s22;
-  double Sf11 = s11 / n1, Sf12 = s12 / n1, Sf21 = s21 / n2, Sf22 = s22 / n2;
+  // these fields.  log(f / B) as log f - log B (log B once on the host) and
+  // the two normalisations as one reciprocal each: two logarithms and two
+  // divisions per cell instead of four and eight, with an absolute error of
+  // the exponent of a few eps |log f|.
+  const double lf1 = log(f1), lf2 = log(f2);
+  double s11 = exp(r.iC11 * (lf1 - r.lB11)), s12 = exp(r.iC12 * (lf2 - r.lB12));
+  double s21 = exp(r.iC21 * (lf1 - r.lB21)), s22 = exp(r.iC22 * (lf2 - r.lB22));
+  const double in1 = 1.0 / (s11 + s12), in2 = 1.0 / (s21 + s22);
+  double Sf11 = s11 * in1, Sf12 = s12 * in1, Sf21 = s21 * in2, Sf22 = s22 * in2;
   double a1 = r.A11 * Sf11 + r.A12 * Sf12;
   double a2 = r.A21 * Sf21 + r.A22 * Sf22;
   double Xf11 = a1 * f1 + (1.0 - a1) * Sf11;
@@ -397,7 +401,8 @@ int update_impl(xc_ctx* c) {
   const xc_params& p = c->p;
   cudaStream_t s = c->stream;
   dim3 blk(32, 8);
-  Rheo r{p.AA[0], p.AA[1], p.AA[2], p.AA[3], p.BB[0], p.BB[1], p.BB[2], p.BB[3],
+  Rheo r{p.AA[0], p.AA[1], p.AA[2], p.AA[3], std::log(p.BB[0]), std::log(p.BB[1]), std::log(p.BB[2]),
+         std::log(p.BB[3]),
          1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0,
          std::log(p.etam0 / p.etax0), std::log(p.etax0 / p.etam0)};
   volfrac_rheology_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(

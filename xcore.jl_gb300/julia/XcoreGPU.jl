@@ -43,7 +43,7 @@ struct SolverOpts
     coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint; pressure_sweeps::Cint; inner_gs_passes::Cint
     serial_launch::Cint; coarse_viscosity_mean::Cint; tiled_sweep::Cint; post_sweeps::Cint; outer_solver::Cint
     fused_pressure_cells::Cint; stage_small_levels::Cint; jacobi_coarse::Cint; row_block_sweep::Cint; learned::Cint
-    host_givens::Cint
+    device_givens::Cint
 end
 SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
     SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
