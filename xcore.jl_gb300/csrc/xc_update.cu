@@ -415,15 +415,24 @@ int update_impl(xc_ctx* c) {
       F(c, FLD_Drhox), F(c, FLD_chiw), F(c, FLD_muw), F(c, FLD_chiu), F(c, FLD_muu),
       F(c, FLD_x_w), F(c, FLD_m_w), F(c, FLD_x_u), F(c, FLD_m_u)); xc_count_launch();
   XC_LAUNCH_CHECK();
+  // update_pressure! (update.jl:111-138): the row means of rhow and the z
+  // prefix sum are chains of dependent FP64 additions in the reference's
+  // order (latency-bound, a few warps); nothing else of update! reads their
+  // results (Drho, Pl, Pt), so they run on the side stream beside the
+  // kinematics-to-stress kernels and are joined at the end
   double* rhoref = c->tmp[6];
   double* plcol = c->tmp[6] + (Nz + 8);
-  rowmean_kernel<<<(Nz + 1 + 31) / 32, 256, 0, s>>>(Nz, Nx, CF(c, FLD_rhow), rhoref); xc_count_launch();
-  pressure_scan_kernel<<<1, 256, 0, s>>>(Nz, p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
+  cudaStream_t side = c->side;
+  XC_CUDA_TRY(cudaEventRecord(c->ev_fork, s));
+  XC_CUDA_TRY(cudaStreamWaitEvent(side, c->ev_fork, 0));
+  rowmean_kernel<<<(Nz + 1 + 31) / 32, 256, 0, side>>>(Nz, Nx, CF(c, FLD_rhow), rhoref); xc_count_launch();
+  pressure_scan_kernel<<<1, 256, 0, side>>>(Nz, p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
   XC_LAUNCH_CHECK();
-  drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, s>>>(
+  drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, side>>>(
       Nz, Nx, p.Ptop, rhoref, plcol, CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
       F(c, FLD_Pt)); xc_count_launch();
   XC_LAUNCH_CHECK();
+  XC_CUDA_TRY(cudaEventRecord(c->ev_join, side));
   const double invh = 1.0 / p.h;
   kinematics_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
       Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
@@ -455,6 +464,7 @@ int update_impl(xc_ctx* c) {
       CF(c, FLD_exx), CF(c, FLD_ezz), F(c, FLD_txx), F(c, FLD_tzz), F(c, FLD_tII), CF(c, FLD_V),
       CF(c, FLD_kx), F(c, FLD_Ra)); xc_count_launch();
   XC_LAUNCH_CHECK();
+  XC_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_join, 0));   // update_pressure! on the side stream
   return XC_OK;
 }
 
