@@ -1931,6 +1931,37 @@ __global__ void norm_final_kernel(int nb, const double* __restrict__ part, doubl
     *inv = sh[0] > 0.0 ? 1.0 / sqrt(sh[0]) : 1.0;
   }
 }
+// w -= sum_k h[k] V[k] and ||w||^2 in the same pass: per-CTA partial sums
+// (working precision per thread and warp, FP64 across warps) to part[blk],
+// combined by norm_final_kernel.  Grid-stride over a grid of at most KGMAX
+// CTAs, so the partials fit the multi-dot scratch.
+template <typename T>
+__global__ void __launch_bounds__(KB) multiaxpy_norm_kernel(long long n, int m, const T* __restrict__ V,
+                                                            long long ldv, const double* __restrict__ h, T* w,
+                                                            double* part) {
+  XC_PDL_WAIT();
+  __shared__ T hs[32];
+  __shared__ double sh[KB / 32];
+  if (threadIdx.x < m) hs[threadIdx.x] = (T)h[threadIdx.x];
+  __syncthreads();
+  T acc = (T)0;
+  const long long stride = (long long)gridDim.x * KB;
+  for (long long t = blockIdx.x * (long long)KB + threadIdx.x; t < n; t += stride) {
+    T s = w[t];
+    const T* vk = V + t;
+    for (int k = 0; k < m; ++k, vk += ldv) s -= hs[k] * *vk;
+    w[t] = s;
+    acc += s * s;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = sh[0];
+    for (int q = 1; q < KB / 32; ++q) r += sh[q];
+    part[blockIdx.x] = r;
+  }
+}
 // w -= sum_k h[k] V[k]
 template <typename T>
 __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, long long ldv,
@@ -1946,18 +1977,25 @@ __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, lo
   for (int k = 0; k < m; ++k, vk += ldv) s -= hs[k] * *vk;
   w[t] = s;
 }
-// x += sum_k y[k] Z[k]
+// x += sum_k y[k] Z[k], or with dscl: x += (sum_k y[k] Z[k]) / dscl (the
+// basis held in physical variables, Z[k] = S z_k of the scaled system)
 template <typename T>
 __global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long long ldz,
-                               const double* __restrict__ y, T* x) {
+                               const double* __restrict__ y, T* x, const T* __restrict__ dscl) {
   XC_PDL_WAIT();
   __shared__ T ys[64];
   if (threadIdx.x < m) ys[threadIdx.x] = (T)y[threadIdx.x];
   __syncthreads();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  T s = x[t];
   const T* zk = Z + t;
+  if (dscl) {
+    T acc = (T)0;
+    for (int k = 0; k < m; ++k, zk += ldz) acc += ys[k] * *zk;
+    x[t] += acc / dscl[t];
+    return;
+  }
+  T s = x[t];
   for (int k = 0; k < m; ++k, zk += ldz) s += ys[k] * *zk;
   x[t] = s;
 }
@@ -2489,8 +2527,9 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   o = H.vx2[l];
   const int npost = cfg.nu_post;
   for (int q = 0; q < npost; ++q) {
-    if (final_out && q == npost - 1) {   // last sweep of the fine level straight into the scaled output
-      launch_sweep<T, 3>(cfg, g, k, op, a, H.vb[l], final_out, om, final_scl, s);
+    if (final_out && q == npost - 1) {   // last sweep of the fine level straight into the output
+      if (final_scl) launch_sweep<T, 3>(cfg, g, k, op, a, H.vb[l], final_out, om, final_scl, s);   // scaled
+      else launch_sweep<T, 1>(cfg, g, k, op, a, H.vb[l], final_out, om, final_scl, s);           // physical
       *final_done = true;
       XC_LAUNCH_CHECK();
       return XC_OK;
@@ -2593,9 +2632,11 @@ int vcycle_p(Hier<T>& H, const SolveCfg& cfg, int l, cudaStream_t s, T** res) {
 }
 
 // out = M^-1 v for the scaled system: out = S^-1 M_phys (S^-1 v)
+// phys_out: out = M_phys (S^-1 v) in physical variables, without the final
+// S^-1 (the caller applies the operator to it directly)
 template <typename T>
 int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* v, T* out,
-            cudaStream_t s) {
+            cudaStream_t s, bool phys_out = false) {
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   const long long nvv = (long long)g.NW + g.NU;
@@ -2615,9 +2656,12 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   pdl(PDL_ON, sub_grad_kernel<T>, nblk(nvv), 256, s, g, zp, v, H.scl, H.vb[0]);
   XC_LAUNCH_CHECK();
   bool done = false;
-  XC_TRY(vcycle_vel<T>(H, k, cfg, 0, s, out, H.scl, &done));
-  if (!done) pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, H.vx[0], H.scl, out);
-  pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, zp, H.scl + nvv, zp);
+  XC_TRY(vcycle_vel<T>(H, k, cfg, 0, s, out, phys_out ? nullptr : H.scl, &done));
+  if (!done) {
+    if (phys_out) XC_CUDA_TRY(cudaMemcpyAsync(out, H.vx[0], sizeof(T) * nvv, cudaMemcpyDeviceToDevice, s));
+    else pdl(PDL_ON, div_kernel<T>, nblk(nvv), 256, s, nvv, H.vx[0], H.scl, out);
+  }
+  if (!phys_out) pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, zp, H.scl + nvv, zp);
   XC_LAUNCH_CHECK();
   (void)n;
   return XC_OK;
@@ -2782,7 +2826,7 @@ __global__ void nn_target_kernel(Geo g, const double* __restrict__ y, float* out
 // z = M v for the configured preconditioner
 template <typename T>
 int apply_precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, const T* v, T* out,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool phys_out = false) {
   if constexpr (std::is_same<T, float>::value) {
     if (cfg.learned != 0) {
       const Geo& g = w->g;
@@ -2819,7 +2863,7 @@ int apply_precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& c
       return XC_OK;
     }
   }
-  return precond<T>(w, H, k, cfg, v, out, s);
+  return precond<T>(w, H, k, cfg, v, out, s, phys_out);
 }
 
 // The launches of one Arnoldi step k: z_k = M v_k; w = A z_k; two classical
@@ -2834,15 +2878,32 @@ int arnoldi_launches(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg
   T* zk = H.Z + (size_t)kk * n;
   T* wv = H.V + (size_t)(kk + 1) * n;
   if (kk + 1 > 32) { xc_set_error("fgmres: restart above 32 basis vectors"); return XC_BAD_ARG; }
-  if (with_precond) XC_TRY(apply_precond<T>(w, H, k, cfg, vk, zk, s));
-  XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
+  // with the multigrid preconditioner z_k stays in physical variables
+  // (Z[k] = S z_k): the operator takes it as it is, and the combine of the
+  // cycle's update applies S^-1 once, instead of an S^-1 pass after every
+  // preconditioner and an S pass before every operator
+  const bool zphys = with_precond && cfg.learned == 0;
+  if (with_precond) XC_TRY(apply_precond<T>(w, H, k, cfg, vk, zk, s, zphys));
+  if (zphys) {
+    pdl(PDL_ON, stokes_apply_kernel<T>, grid2(g), blk2(), s, g, k, vop(H, 0), (const T*)H.cp, (const T*)H.scl,
+        (const T*)zk, (const T*)nullptr, wv);
+  } else {
+    XC_TRY(apply_scaled<T>(w, H, k, zk, nullptr, wv, s));
+  }
   double* hd = w->hdev + 8;
   for (int pass = 0; pass < cfg.gs_passes; ++pass) {
     const int nb = launch_multidot<T>(n, kk + 1, H.V, n, wv, w->part, s);
     pdl(PDL_ON, multidot_final_kernel, kk + 1, KB, s, kk + 1, nb, w->part, hd + pass * kMaxRestart);
-    pdl(PDL_ON, multiaxpy_kernel<T>, nblk(n), 256, s, n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv);
+    if (pass + 1 < cfg.gs_passes) {
+      pdl(PDL_ON, multiaxpy_kernel<T>, nblk(n), 256, s, n, kk + 1, H.V, n, hd + pass * kMaxRestart, wv);
+    } else {
+      // the last pass also forms ||w||^2 (-> hdev[2], 1/||w|| -> hdev[6])
+      const int nbn = (int)std::min<long long>(nblk(n), (long long)KGMAX);
+      pdl(PDL_ON, multiaxpy_norm_kernel<T>, nbn, KB, s, n, kk + 1, (const T*)H.V, n,
+          (const double*)(hd + pass * kMaxRestart), wv, w->part);
+      pdl(PDL_ON, norm_final_kernel, 1, KB, s, nbn, (const double*)w->part, w->hdev + 2, w->hdev + 6);
+    }
   }
-  XC_TRY(dot_self<T>(w, H, wv, n, 2, s));
   pdl(PDL_ON, normalize_kernel<T>, nblk(n), 256, s, n, w->hdev + 6, wv);
   if (host_copy)
     XC_CUDA_TRY(cudaMemcpyAsync(w->hhost, w->hdev, sizeof(double) * (8 + 2 * kMaxRestart), cudaMemcpyDeviceToHost, s));
@@ -2938,15 +2999,23 @@ __global__ void krylov_solve_kernel(KrylovDev* kd, double* coef, KrylovStatus* s
 // x += Z coef over the kk basis vectors the cycle used (kk read on the device)
 template <typename T>
 __global__ void combine_dev_kernel(long long n, const KrylovDev* __restrict__ kd, const T* __restrict__ Z,
-                                   long long ldz, const double* __restrict__ coef, T* x) {
+                                   long long ldz, const double* __restrict__ coef, T* x,
+                                   const T* __restrict__ dscl) {
   __shared__ T ys[kMaxRestart];
   const int m = kd->kk;
   if (threadIdx.x < m) ys[threadIdx.x] = (T)coef[threadIdx.x];
   __syncthreads();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
+  const T* zk = Z + t;
+  if (dscl) {
+    T acc = (T)0;
+    for (int k = 0; k < m; ++k, zk += ldz) acc += ys[k] * *zk;
+    x[t] += acc / dscl[t];
+    return;
+  }
   T s = x[t];
-  for (int k = 0; k < m; ++k) s += ys[k] * Z[(size_t)k * ldz + t];
+  for (int k = 0; k < m; ++k, zk += ldz) s += ys[k] * *zk;
   x[t] = s;
 }
 
@@ -3209,7 +3278,9 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
         if (st != XC_OK) return st;
         krylov_solve_kernel<<<1, 32, 0, s>>>(H.kd, w->hdev + 8, H.ks_dev);
         xc_count_launch();
-        combine_dev_kernel<T><<<nblk(n), 256, 0, s>>>(n, H.kd, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
+        combine_dev_kernel<T><<<nblk(n), 256, 0, s>>>(n, H.kd, H.Z, n, w->hdev + 8, H.y,
+                                                      cfg.learned == 0 ? (const T*)H.scl : nullptr);
+        xc_count_launch();
         XC_LAUNCH_CHECK();
         XC_CUDA_TRY(cudaStreamSynchronize(s));
         const volatile KrylovStatus* ks = H.ks_host;
@@ -3241,7 +3312,9 @@ int fgmres(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, con
     // back substitution and update y += Z yv
     ls.solve(kk);
     XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 8, ls.yv.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
-    combine_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
+    combine_kernel<T><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y,
+                                              cfg.learned == 0 ? (const T*)H.scl : nullptr);
+    xc_count_launch();
     XC_LAUNCH_CHECK();
     if ((flags & FG_TRUST_EST) && (relres <= rtol || its >= maxit)) break;
   }
@@ -3308,7 +3381,8 @@ int fgmres_outer(StokesWork* w, const OpConst& k, const SolveCfg& cfg, const Sol
     if (status != XC_OK) break;
     ls.solve(kk);
     XC_CUDA_TRY(cudaMemcpyAsync(w->hdev + 8, ls.yv.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
-    combine_kernel<double><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y); xc_count_launch();
+    combine_kernel<double><<<nblk(n), 256, 0, s>>>(n, kk, H.Z, n, w->hdev + 8, H.y, (const double*)nullptr);
+    xc_count_launch();
     XC_LAUNCH_CHECK();
   }
   *its_out = its;
