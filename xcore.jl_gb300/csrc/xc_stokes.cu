@@ -1769,54 +1769,57 @@ __global__ void p_kcoef_kernel(Geo g, const double* __restrict__ rhow, const dou
 
 // pressure part of the preconditioner, before / after the interior solve:
 // ghost elimination of the residual (P ghost rows P_g - P_n = r_g) and the
-// ghost values of the result
+// ghost values of the result (P_g = r_g + P_neighbour, fluidmech.jl:403-417).
+// The physical pressure residual r = v_p / scl_p is formed where it is read
+// (no r array, no separate division pass), and the interior cells, ghost
+// columns and ghost rows are written by one launch: a ghost entry recomputes
+// the interior or ghost-column value it copies with the same operations (the
+// ghost rows of columns 0 and Nx+1 read ghost-column values).
 template <typename T>
-__global__ void p_gather_kernel(Geo g, const T* __restrict__ kx, const T* __restrict__ kr,
-                                const T* __restrict__ rp, T* rin) {
+__global__ void p_gather_fused_kernel(Geo g, const T* __restrict__ kx, const T* __restrict__ kr,
+                                      const T* __restrict__ vp, const T* __restrict__ sp, T* rin) {
   XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
   if (t >= Nz * Nx) return;
   int j = t % Nz, i = t / Nz;
-  T v = rp[(size_t)(i + 1) * lp + j + 1];
-  if (i == 0) v += kx[j] * rp[j + 1];
-  if (i == Nx - 1) v += kr[j] * rp[(size_t)(Nx + 1) * lp + j + 1];
+  const size_t o = (size_t)(i + 1) * lp + j + 1;
+  T v = vp[o] / sp[o];
+  if (i == 0) v += kx[j] * (vp[j + 1] / sp[j + 1]);
+  if (i == Nx - 1) {
+    const size_t q = (size_t)(Nx + 1) * lp + j + 1;
+    v += kr[j] * (vp[q] / sp[q]);
+  }
   rin[t] = v;
 }
 
 template <typename T>
-__global__ void p_scatter_kernel(Geo g, const T* __restrict__ z, const T* __restrict__ rp,
-                                 const T* __restrict__ etarho, T cmass, T* zp) {
+__global__ void p_scatter_fused_kernel(Geo g, const T* __restrict__ z, const T* __restrict__ vp,
+                                       const T* __restrict__ sp, const T* __restrict__ etarho, T cmass,
+                                       int open_bottom, T* zp) {
   XC_PDL_WAIT();
-  // interior cells: z + cmass * (eta/rho) * r
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int Nz = g.Nz, lp = Nz + 2;
-  if (t >= Nz * g.Nx) return;
-  int j = t % Nz, i = t / Nz;
-  size_t o = (size_t)(i + 1) * lp + j + 1;
-  zp[o] = z[t] + cmass * etarho[t] * rp[o];
-}
-// ghost columns then ghost rows: P_g = r_g + P_neighbour (fluidmech.jl:403-417)
-template <typename T>
-__global__ void p_scatter_cols_kernel(Geo g, const T* __restrict__ rp, T* zp, int open_bottom) {
-  XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx, lp = Nz + 2;
-  if (j < 1 || j > Nz) return;
-  const bool id = open_bottom && j == Nz;   // P = 0 rows of the open bottom
-  zp[j] = id ? rp[j] : rp[j] + zp[(size_t)Nx * lp + j];
-  zp[(size_t)(Nx + 1) * lp + j] = id ? rp[(size_t)(Nx + 1) * lp + j]
-                                     : rp[(size_t)(Nx + 1) * lp + j] + zp[(size_t)lp + j];
-}
-template <typename T>
-__global__ void p_scatter_rows_kernel(Geo g, const T* __restrict__ rp, T* zp) {
-  XC_PDL_WAIT();
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int Nz = g.Nz, lp = Nz + 2;
-  if (i >= g.Nx + 2) return;
-  size_t o = (size_t)i * lp;
-  zp[o] = rp[o] + zp[o + 1];
-  zp[o + Nz + 1] = rp[o + Nz + 1] + zp[o + Nz];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= lp * (Nx + 2)) return;
+  const int j = t % lp, i = t / lp;
+  auto r = [&](int jj, int ii) {
+    const size_t o = (size_t)ii * lp + jj;
+    return vp[o] / sp[o];
+  };
+  auto zint = [&](int jj, int ii) {   // interior cell (1..Nz, 1..Nx)
+    const int c = (ii - 1) * Nz + (jj - 1);
+    return z[c] + cmass * etarho[c] * r(jj, ii);
+  };
+  auto zcol = [&](int jj, int ii) {   // ghost column ii = 0 or Nx+1, rows 1..Nz
+    if (open_bottom && jj == Nz) return r(jj, ii);   // P = 0 rows of the open bottom
+    return r(jj, ii) + zint(jj, ii == 0 ? Nx : 1);
+  };
+  T out;
+  const bool col_in = i >= 1 && i <= Nx;
+  if (j >= 1 && j <= Nz) out = col_in ? zint(j, i) : zcol(j, i);
+  else if (j == 0) out = r(0, i) + (col_in ? zint(1, i) : zcol(1, i));
+  else out = r(Nz + 1, i) + (col_in ? zint(Nz, i) : zcol(Nz, i));
+  zp[t] = out;
 }
 
 // velocity right-hand side of the preconditioner: rv = S^-1 v - GG z_p on the
@@ -2273,7 +2276,6 @@ struct Hier {
   T* t;
   T* y;           // current iterate (scaled unknowns)
   T* rv;          // preconditioner scratch (velocity part, physical)
-  T* rp;          // preconditioner scratch (pressure, physical full layout)
   T* rin;         // interior pressure rhs
   // captured graphs per Arnoldi index for two configuration keys (the
   // learned preconditioner and its multigrid fallback alternate within one
@@ -2393,7 +2395,6 @@ int alloc_hier(StokesWork* w, Hier<T>& H, int m) {
   XC_CUDA_TRY(cudaMalloc(&H.t, sizeof(T) * n));
   XC_CUDA_TRY(cudaMalloc(&H.y, sizeof(T) * n));
   XC_CUDA_TRY(cudaMalloc(&H.rv, sizeof(T) * (g.NW + g.NU)));
-  XC_CUDA_TRY(cudaMalloc(&H.rp, sizeof(T) * g.NP));
   XC_CUDA_TRY(cudaMalloc(&H.rin, sizeof(T) * g.Nz * g.Nx));
   XC_CUDA_TRY(cudaMalloc(&H.kd, sizeof(KrylovDev)));
   XC_CUDA_TRY(cudaMemset(H.kd, 0, sizeof(KrylovDev)));
@@ -2423,7 +2424,7 @@ void free_hier(Hier<T>& H) {
     cudaFree(H.kx[l]); cudaFree(H.kz[l]); cudaFree(H.px[l]); cudaFree(H.px2[l]); cudaFree(H.pb[l]); cudaFree(H.pr[l]);
   }
   cudaFree(H.kr); cudaFree(H.cp); cudaFree(H.scl); cudaFree(H.etarho); cudaFree(H.V); cudaFree(H.Z);
-  cudaFree(H.w); cudaFree(H.t); cudaFree(H.y); cudaFree(H.rv); cudaFree(H.rp); cudaFree(H.rin);
+  cudaFree(H.w); cudaFree(H.t); cudaFree(H.y); cudaFree(H.rv); cudaFree(H.rin);
   cudaFree(H.vinv); cudaFree(H.pinv); cudaFree(H.dok);
   H.nv = H.np_lv = 0;
 }
@@ -2642,16 +2643,15 @@ int precond(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg, co
   const long long nvv = (long long)g.NW + g.NU;
   // physical residual r = S^-1 v: pressure part into rp here, velocity part
   // into vb[0] by sub_grad_kernel below
-  pdl(PDL_ON, div_kernel<T>, nblk(g.NP), 256, s, g.NP, v + nvv, H.scl + nvv, H.rp);
   // pressure: interior solve with ghost elimination
-  pdl(PDL_ON, p_gather_kernel<T>, nblk(g.Nz * g.Nx), 256, s, g, H.kx[0], H.kr, H.rp, H.pb[0]);
+  pdl(PDL_ON, p_gather_fused_kernel<T>, nblk(g.Nz * g.Nx), 256, s, g, (const T*)H.kx[0], (const T*)H.kr,
+      v + nvv, (const T*)(H.scl + nvv), H.pb[0]);
   XC_LAUNCH_CHECK();
   T* px0 = nullptr;
   XC_TRY(vcycle_p<T>(H, cfg, 0, s, &px0));
   T* zp = out + nvv;   // physical z_p written directly into out, rescaled below
-  pdl(PDL_ON, p_scatter_kernel<T>, nblk((long long)g.Nz * g.Nx), 256, s, g, px0, H.rp, H.etarho, (T)cfg.cmass, zp);
-  pdl(PDL_ON, p_scatter_cols_kernel<T>, nblk(g.Nz + 1), 256, s, g, H.rp, zp, k.open_cnv);
-  pdl(PDL_ON, p_scatter_rows_kernel<T>, nblk(g.Nx + 2), 256, s, g, H.rp, zp);
+  pdl(PDL_ON, p_scatter_fused_kernel<T>, nblk(g.NP), 256, s, g, (const T*)px0, v + nvv, (const T*)(H.scl + nvv),
+      (const T*)H.etarho, (T)cfg.cmass, k.open_cnv, zp);
   // velocity: rhs r_v - GG z_p, one V-cycle
   pdl(PDL_ON, sub_grad_kernel<T>, nblk(nvv), 256, s, g, zp, v, H.scl, H.vb[0]);
   XC_LAUNCH_CHECK();
