@@ -151,6 +151,13 @@ typedef struct xc_solver_opts {
                               iterations; measured 7% slower at 1024^2: an IF node costs more
                               than the host round trip it removes).  0: on the host, one
                               synchronisation per Arnoldi step */
+  int cluster_cells;       /* velocity multigrid levels below the finest with more than small_cells
+                              and at most this many cells run their part of the V-cycle in one
+                              launch of a thread-block cluster (16 CTAs; cluster barriers between
+                              the operations, the same per-unknown operations as the per-level
+                              launches).  0 or -1: none (default; measured 1.7% slower at 1024^2
+                              with 16384, even with 4096: the programmatic launches already hide
+                              most of the per-level launch gaps) */
 } xc_solver_opts;
 
 typedef struct xc_solver_stats {

@@ -319,3 +319,25 @@ def test_device_givens_respects_the_iteration_cap():
         ds.close()
         its = int(str(e.value).split(" after ")[1].split()[0])
         assert its == maxit, (maxit, str(e.value))
+
+
+@pytest.mark.parametrize("N", [128, 200, 256])
+def test_cluster_vcycle_matches_the_per_level_launches(N):
+    """cluster_cells: the velocity levels between the one-CTA size and 128^2
+    (below the finest) run in one thread-block-cluster launch with the same
+    per-unknown operations as the per-level launches: the same iterations to
+    the same solution (200 coarsens through odd sizes)."""
+    par, g, sc, ns, st, dt, rng = realistic_state(N=N, Nx=N, steps=1)
+    coefs = O.time_coefs("bd2im", 2)
+    out = {}
+    for cc in (0, 16384):
+        ds = device_state(par, g, sc, st)
+        info = ds.fluidmech(coefs, dt, solver="mixed", rtol=1e-9, maxit=600, inner_rtol=5e-2, inner_maxit=30,
+                            pressure_sweeps=1, cluster_cells=cc)
+        assert info["converged"], (cc, info)
+        out[cc] = (info, ds["W"], ds["U"], ds["P"])
+        ds.close()
+    (ia, *fa), (ib, *fb) = out[0], out[16384]
+    assert abs(ia["iterations"] - ib["iterations"]) <= 1, (ia, ib)
+    for a, b in zip(fa, fb):
+        assert np.abs(a - b).max() <= 1e-7 * np.abs(a).max()

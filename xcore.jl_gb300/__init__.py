@@ -84,7 +84,7 @@ class SolverOpts(ctypes.Structure):
                 ("fused_pressure_cells", ctypes.c_int),
                 ("stage_small_levels", ctypes.c_int),
                 ("jacobi_coarse", ctypes.c_int), ("row_block_sweep", ctypes.c_int), ("learned", ctypes.c_int),
-                ("device_givens", ctypes.c_int)]
+                ("device_givens", ctypes.c_int), ("cluster_cells", ctypes.c_int)]
 
     @classmethod
     def make(cls, solver="fgmres64", rtol=1e-10, maxit=500, restart=30, inner_rtol=1e-4, inner_maxit=60,
@@ -92,14 +92,16 @@ class SolverOpts(ctypes.Structure):
              coarse_cells=0, coarse_sweeps=0, small_cells=0, pressure_sweeps=0, inner_gs_passes=0,
              serial_launch=False, coarse_viscosity_mean=0, tiled_sweep=False, post_sweeps=0, outer_solver=0,
              fused_pressure_cells=0, stage_small_levels=False,
-             jacobi_coarse=False, row_block_sweep=False, learned=0, device_givens=False):
+             jacobi_coarse=False, row_block_sweep=False, learned=0, device_givens=False,
+             cluster_cells=0):
         return cls(SOLVERS[solver], float(rtol), int(maxit), int(restart), float(inner_rtol), int(inner_maxit),
                    int(smooth_sweeps), float(omega_velocity), float(schur_mass), int(bool(schur_full_diagonal)),
                    int(coarse_cells), int(coarse_sweeps), int(small_cells), int(pressure_sweeps),
                    int(inner_gs_passes), int(bool(serial_launch)), int(coarse_viscosity_mean),
                    int(bool(tiled_sweep)), int(post_sweeps), int(outer_solver),
                    int(fused_pressure_cells), int(bool(stage_small_levels)),
-                   int(bool(jacobi_coarse)), int(bool(row_block_sweep)), int(learned), int(bool(device_givens)))
+                   int(bool(jacobi_coarse)), int(bool(row_block_sweep)), int(learned), int(bool(device_givens)),
+                   int(cluster_cells))
 
 
 class SolverStats(ctypes.Structure):

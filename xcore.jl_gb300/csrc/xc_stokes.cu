@@ -1557,6 +1557,35 @@ __device__ __forceinline__ void cta_copy(T* dst, const T* src, long long n) {
 }
 constexpr size_t kStageMaxBytes = 160 * 1024;
 
+// the V-cycle of levels l0..lc (lc the coarsest) by one CTA: nu sweeps
+// before and after each coarse correction, the coarsest solved directly
+template <typename T>
+__device__ void vel_vcycle_cta(const VelLevels<T>& L, const OpConst& kf, int l0, int lc, int nu, T om, int csweeps,
+                               const T* inv, const int* inv_ok) {
+  for (int l = l0; l < lc; ++l) {
+    const OpConst k = level_const(kf, l);
+    const Geo& g = L.g[l];
+    const Geo& c = L.g[l + 1];
+    vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, true);
+    const long long n = (long long)g.NW + g.NU;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x)
+      vel_residual_at<T>(g, k, L.op[l], L.x[l], L.b[l], L.r[l], t);
+    __syncthreads();
+    const long long nc = (long long)c.NW + c.NU;
+    for (long long t = threadIdx.x; t < nc; t += blockDim.x) vel_restrict_at<T>(g, c, L.r[l], L.b[l + 1], t);
+    __syncthreads();
+  }
+  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.op[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om, inv, inv_ok);
+  for (int l = lc - 1; l >= l0; --l) {
+    const OpConst k = level_const(kf, l);
+    const Geo& g = L.g[l];
+    const long long n = (long long)g.NW + g.NU;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_prolong_at<T>(g, L.g[l + 1], k, L.x[l + 1], L.x[l], t);
+    __syncthreads();
+    vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, false);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> Lg, OpConst kf, int l0, int lc, int nu,
                                                                 T om, int csweeps, int staged, const T* inv,
@@ -1606,29 +1635,95 @@ __global__ void __launch_bounds__(1024) vel_vcycle_small_kernel(VelLevels<T> Lg,
     cta_copy<T>(L.b[l0], Lg.b[l0], (long long)L.g[l0].NW + L.g[l0].NU);
     __syncthreads();
   }
-  for (int l = l0; l < lc; ++l) {
+  vel_vcycle_cta<T>(L, kf, l0, lc, nu, om, csweeps, inv, inv_ok);
+  if (staged) cta_copy<T>(Lg.x[l0], L.x[l0], (long long)L.g[l0].NW + L.g[l0].NU);
+}
+
+
+// ---- thread-block-cluster V-cycle of the middle levels ---------------------
+// Levels of up to a few ten thousand cells are too small to fill the GPU and
+// each of their operations costs a launch; one cluster of CTAs (16 where the
+// GPU allows, else 8) runs all of them in one launch, the CTAs dividing each
+// level's unknowns and meeting at cluster barriers between the operations
+// (the barrier's release / acquire makes every global-memory write before it
+// visible to the whole cluster after it).  The operations are the per-unknown
+// bodies of the separate launches, so the results are the same.  The levels
+// below the one-CTA size are then handled by CTA 0 alone, as the one-CTA
+// kernel would.  Every loop bound is uniform across the cluster and no thread
+// leaves early, so every thread reaches every barrier.
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_rank_u32() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_size_u32() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+
+// vel_smooth_cta over the cluster (unknowns t0, t0 + ts, ...)
+template <typename T>
+__device__ void vel_smooth_cluster(const Geo& g, const OpConst& k, const VOp<T>& op, T* x, T* x2, const T* b, T om,
+                                   int sweeps, bool from_zero, long long t0, long long ts) {
+  const long long n = (long long)g.NW + g.NU;
+  T* a = x;
+  T* o = x2;
+  int q = 0;
+  if (from_zero) {
+    for (long long t = t0; t < n; t += ts) vel_jacobi_at<T>(g, k, op, x, b, x, om, 1, t);
+    cluster_barrier();
+    q = 1;
+  }
+  for (; q < sweeps; ++q) {
+    for (long long t = t0; t < n; t += ts) vel_jacobi_at<T>(g, k, op, a, b, o, om, 0, t);
+    cluster_barrier();
+    T* tmp = a; a = o; o = tmp;
+  }
+  if (a != x) {
+    for (long long t = t0; t < n; t += ts) x[t] = a[t];
+    cluster_barrier();
+  }
+}
+
+// levels l0..ls-1 over the cluster (nu sweeps before, nu_post after each
+// coarse correction, as the per-level launches do), ls..lc by CTA 0
+template <typename T>
+__global__ void __launch_bounds__(1024) vel_vcycle_cluster_kernel(VelLevels<T> Lg, OpConst kf, int l0, int ls, int lc,
+                                                                  int nu, int nu_post, T om, int csweeps,
+                                                                  const T* inv, const int* inv_ok) {
+  XC_PDL_WAIT();
+  __shared__ VelLevels<T> L;
+  if (threadIdx.x == 0) L = Lg;
+  __syncthreads();
+  const unsigned rank = cluster_rank_u32();
+  const long long t0 = (long long)rank * blockDim.x + threadIdx.x;
+  const long long ts = (long long)cluster_size_u32() * blockDim.x;
+  for (int l = l0; l < ls; ++l) {
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
     const Geo& c = L.g[l + 1];
-    vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, true);
+    vel_smooth_cluster<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, true, t0, ts);
     const long long n = (long long)g.NW + g.NU;
-    for (long long t = threadIdx.x; t < n; t += blockDim.x)
-      vel_residual_at<T>(g, k, L.op[l], L.x[l], L.b[l], L.r[l], t);
-    __syncthreads();
+    for (long long t = t0; t < n; t += ts) vel_residual_at<T>(g, k, L.op[l], L.x[l], L.b[l], L.r[l], t);
+    cluster_barrier();
     const long long nc = (long long)c.NW + c.NU;
-    for (long long t = threadIdx.x; t < nc; t += blockDim.x) vel_restrict_at<T>(g, c, L.r[l], L.b[l + 1], t);
-    __syncthreads();
+    for (long long t = t0; t < nc; t += ts) vel_restrict_at<T>(g, c, L.r[l], L.b[l + 1], t);
+    cluster_barrier();
   }
-  vel_coarse_cta<T>(L.g[lc], level_const(kf, lc), L.op[lc], L.x[lc], L.x2[lc], L.b[lc], csweeps, om, inv, inv_ok);
-  for (int l = lc - 1; l >= l0; --l) {
+  if (rank == 0) vel_vcycle_cta<T>(L, kf, ls, lc, nu, om, csweeps, inv, inv_ok);
+  cluster_barrier();
+  for (int l = ls - 1; l >= l0; --l) {
     const OpConst k = level_const(kf, l);
     const Geo& g = L.g[l];
     const long long n = (long long)g.NW + g.NU;
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) vel_prolong_at<T>(g, L.g[l + 1], k, L.x[l + 1], L.x[l], t);
-    __syncthreads();
-    vel_smooth_cta<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu, false);
+    for (long long t = t0; t < n; t += ts) vel_prolong_at<T>(g, L.g[l + 1], k, L.x[l + 1], L.x[l], t);
+    cluster_barrier();
+    vel_smooth_cluster<T>(g, k, L.op[l], L.x[l], L.x2[l], L.b[l], om, nu_post, false, t0, ts);
   }
-  if (staged) cta_copy<T>(Lg.x[l0], L.x[l0], (long long)L.g[l0].NW + L.g[l0].NU);
 }
 
 template <typename T>
@@ -2211,6 +2306,10 @@ struct SolveCfg {
   // the Hessenberg least-squares problem of FGMRES on the device (conditional
   // graphs) instead of on the host with one synchronisation per Arnoldi step
   bool device_givens = false;
+  // velocity levels of more than small_cells and at most this many cells
+  // (below the finest) run in one thread-block-cluster launch (0: none;
+  // opt-in: measured no faster than the programmatic per-level launches)
+  long long cluster_cells = 0;
 };
 
 // The least-squares problem of (F)GMRES(m) on the device: the Hessenberg
@@ -2478,6 +2577,41 @@ void launch_sweep(const SolveCfg& cfg, const Geo& g, const OpConst& k, const VOp
   pdl(PDL_ON, vel_sweep2d_kernel<T, MODE>, grid2(g), blk2(), s, g, k, op, xi, b, out, om, dscl);
 }
 
+// CTAs per cluster of the cluster V-cycle (16 where the device schedules
+// clusters of 16 CTAs of 1024 threads, else 8; 0: clusters unavailable),
+// per precision, found once per process
+int g_vcluster[2] = {-1, -1};
+std::mutex g_vcluster_mu;
+template <typename T>
+int vel_cluster_size() {
+  const int p = std::is_same<T, float>::value ? 0 : 1;
+  std::lock_guard<std::mutex> lock(g_vcluster_mu);
+  if (g_vcluster[p] >= 0) return g_vcluster[p];
+  int best = 0;
+  cudaFuncSetAttribute(vel_vcycle_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  for (int cs : {16, 8}) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(cs);
+    lc.blockDim = dim3(1024);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, vel_vcycle_cluster_kernel<T>, &lc) == cudaSuccess &&
+        nclusters >= 1) {
+      best = cs;
+      break;
+    }
+  }
+  cudaGetLastError();
+  g_vcluster[p] = best;
+  return best;
+}
+
 template <typename T>
 int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaStream_t s, T* final_out = nullptr,
                const T* final_scl = nullptr, bool* final_done = nullptr) {
@@ -2485,6 +2619,41 @@ int vcycle_vel(Hier<T>& H, const OpConst& kf, const SolveCfg& cfg, int l, cudaSt
   const long long n = (long long)g.NW + g.NU;
   const T om = (T)cfg.omega_v;
   const OpConst k = level_const(kf, l);
+  const long long cells = (long long)g.Nz * g.Nx;
+  if (l > 0 && cfg.cluster_cells > 0 && cells <= cfg.cluster_cells && cells > cfg.small_cells &&
+      !vel_coarsest(H, cfg, l)) {
+    const int cs = vel_cluster_size<T>();
+    if (cs > 0) {
+      int ls = l;
+      while (!vel_coarsest(H, cfg, ls) && (long long)H.vg[ls].Nz * H.vg[ls].Nx > cfg.small_cells) ++ls;
+      int lc = ls;
+      while (!vel_coarsest(H, cfg, lc)) ++lc;
+      VelLevels<T> L;
+      for (int q = 0; q <= lc; ++q) {
+        L.g[q] = H.vg[q]; L.op[q] = vop(H, q);
+        L.x[q] = H.vx[q]; L.x2[q] = H.vx2[q]; L.b[q] = H.vb[q]; L.r[q] = H.vr[q];
+      }
+      cudaLaunchConfig_t lcfg = {};
+      lcfg.gridDim = dim3(cs);
+      lcfg.blockDim = dim3(1024);
+      lcfg.stream = s;
+      cudaLaunchAttribute at[2];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = cs;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      at[1].val.programmaticStreamSerializationAllowed = 1;
+      lcfg.attrs = at;
+      lcfg.numAttrs = PDL_ON ? 2 : 1;
+      XC_CUDA_TRY(cudaLaunchKernelEx(&lcfg, vel_vcycle_cluster_kernel<T>, L, kf, l, ls, lc, cfg.nu, cfg.nu_post, om,
+                                     coarse_sweeps(cfg, H.vg[lc].Nz, H.vg[lc].Nx),
+                                     (const T*)(H.vdirect ? H.vinv : nullptr), (const int*)H.dok));
+      xc_count_launch();
+      XC_LAUNCH_CHECK();
+      return XC_OK;
+    }
+  }
   if (!vel_coarsest(H, cfg, l) && (long long)g.Nz * g.Nx <= cfg.small_cells) {
     int lc = l;
     while (!vel_coarsest(H, cfg, lc)) ++lc;
@@ -3026,7 +3195,7 @@ unsigned long long graph_key(const OpConst& k, const SolveCfg& cfg) {
     std::memcpy(&b, &v, sizeof(b));
     h = (h ^ b) * 1099511628211ULL;
   };
-  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0); mix((double)cfg.learned); mix(cfg.row_block ? 1.0 : 0.0);
+  mix(cfg.omega_v); mix(cfg.omega_p); mix(cfg.nu); mix(cfg.nu_post); mix(cfg.coarse_sweeps); mix(cfg.coarse_cells); mix(cfg.small_cells); mix(cfg.nu_p); mix(cfg.gs_passes); mix(cfg.pdl ? 1.0 : 0.0); mix(cfg.tiled ? 1.0 : 0.0); mix(cfg.cmass); mix(cfg.kplane); mix((double)cfg.pfuse_cells); mix(cfg.stage_small ? 1.0 : 0.0); mix(cfg.direct_coarse ? 1.0 : 0.0); mix((double)cfg.learned); mix(cfg.row_block ? 1.0 : 0.0); mix((double)cfg.cluster_cells);
   mix(k.mms); mix(k.pin_u); mix(k.pin_p); mix(k.open_cnv); mix(k.sds); mix(k.top_cnv); mix(k.bot_cnv);
   return h | 1ULL;
 }
@@ -3750,6 +3919,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   cfg.tiled = o.tiled_sweep != 0;
   cfg.row_block = o.row_block_sweep != 0;
   cfg.device_givens = o.device_givens != 0;
+  cfg.cluster_cells = o.cluster_cells < 0 ? 0 : (o.cluster_cells > 0 ? o.cluster_cells : 0);
   cfg.stage_small = o.stage_small_levels != 0;
   cfg.direct_coarse = !o.jacobi_coarse;
   if (o.fused_pressure_cells != 0) cfg.pfuse_cells = o.fused_pressure_cells < 0 ? 0 : o.fused_pressure_cells;

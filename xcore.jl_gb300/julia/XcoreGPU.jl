@@ -43,10 +43,10 @@ struct SolverOpts
     coarse_cells::Cint; coarse_sweeps::Cint; small_cells::Cint; pressure_sweeps::Cint; inner_gs_passes::Cint
     serial_launch::Cint; coarse_viscosity_mean::Cint; tiled_sweep::Cint; post_sweeps::Cint; outer_solver::Cint
     fused_pressure_cells::Cint; stage_small_levels::Cint; jacobi_coarse::Cint; row_block_sweep::Cint; learned::Cint
-    device_givens::Cint
+    device_givens::Cint; cluster_cells::Cint
 end
 SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit) =
-    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    SolverOpts(kind, rtol, maxit, restart, inner_rtol, inner_maxit, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
 
 struct SolverStats
     iterations::Cint; refinements::Cint; rel_residual::Cdouble; converged::Cint; seconds::Cdouble
@@ -218,7 +218,7 @@ end
 # reduction in at most 30 iterations, one pressure-multigrid sweep
 step_solver_opts(solver::Symbol, rtol; learned = 0) =
     SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 5e-2, 30,
-               0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, learned, 0)
+               0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, learned, 0, 0)
 
 # status 2 (XC_NOT_CONVERGED) from a step means the step was completed but a
 # Stokes solve stopped at its cap: raise with the step statistics
