@@ -2075,6 +2075,22 @@ __global__ void multiaxpy_kernel(long long n, int m, const T* __restrict__ V, lo
   for (int k = 0; k < m; ++k, vk += ldv) s -= hs[k] * *vk;
   w[t] = s;
 }
+// sum_k y[k] zk[k * ldz] with four independent partial sums, so the loads of
+// four basis vectors are in flight at once (a single running sum over a
+// runtime-length loop issued them one after another)
+template <typename T>
+__device__ __forceinline__ T combine_sum(const T* ys, int m, const T* zk, long long ldz) {
+  T a0 = (T)0, a1 = (T)0, a2 = (T)0, a3 = (T)0;
+  int k = 0;
+  for (; k + 4 <= m; k += 4, zk += 4 * ldz) {
+    a0 += ys[k] * zk[0];
+    a1 += ys[k + 1] * zk[ldz];
+    a2 += ys[k + 2] * zk[2 * ldz];
+    a3 += ys[k + 3] * zk[3 * ldz];
+  }
+  for (; k < m; ++k, zk += ldz) a0 += ys[k] * *zk;
+  return (a0 + a1) + (a2 + a3);
+}
 // x += sum_k y[k] Z[k], or with dscl: x += (sum_k y[k] Z[k]) / dscl (the
 // basis held in physical variables, Z[k] = S z_k of the scaled system)
 template <typename T>
@@ -2088,9 +2104,7 @@ __global__ void combine_kernel(long long n, int m, const T* __restrict__ Z, long
   if (t >= n) return;
   const T* zk = Z + t;
   if (dscl) {
-    T acc = (T)0;
-    for (int k = 0; k < m; ++k, zk += ldz) acc += ys[k] * *zk;
-    x[t] += acc / dscl[t];
+    x[t] += combine_sum<T>(ys, m, zk, ldz) / dscl[t];
     return;
   }
   T s = x[t];
@@ -2147,6 +2161,7 @@ __global__ void mom_prep_kernel(int Nz, int Nx, CView W, CView U, CView rhow, CV
 
 struct RhsArgs {
   double a1, a2, a3, dt, g0, D, h, oc;
+  double idt;   // 1 / dt
   int mms;
   int pin_p, pin_u;
 };
@@ -2157,37 +2172,42 @@ __global__ void rhs_kernel(Geo g, RhsArgs a, CView Drho, CView rhoWo, CView rhoW
                            const double* __restrict__ src_u, const double* __restrict__ src_p,
                            double pin_p_val, double pin_u_val, double* RR) {
   XC_PDL_WAIT();
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // 32-bit indices (the unknown count is checked below 2^31 at setup) and
+  // the division by dt as a product with 1/dt: a 64-bit integer division and
+  // an FP64 division per row were most of this kernel's time on GB300.  RR
+  // is the solve's right-hand side only, so a last-bit difference in it is
+  // far inside the solver's tolerance.
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Nz = g.Nz, Nx = g.Nx;
-  const long long n = (long long)g.NW + g.NU + g.NP;
+  const int n = g.NW + g.NU + g.NP;
   if (t >= n) return;
   double v = 0.0;
   if (t < g.NW) {
-    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    const int j = t % (Nz + 1), i = t / (Nz + 1);
     if (i >= 1 && i <= Nx) {
       if (j == Nz) {
         double mfbg = (*mfs_mean) * a.D / a.h;
         v = a.oc * AT(MFS, Nz - 1, i - 1) + (1.0 - a.oc) * mfbg;
       } else if (j >= 1) {
-        v = (AT(Drho, j, i - 1) * a.g0 + (a.a2 * AT(rhoWo, j, i - 1) + a.a3 * AT(rhoWoo, j, i - 1)) / a.dt) -
+        v = (AT(Drho, j, i - 1) * a.g0 + (a.a2 * AT(rhoWo, j, i - 1) + a.a3 * AT(rhoWoo, j, i - 1)) * a.idt) -
             advz[(size_t)(i - 1) * (Nz - 1) + j - 1];
         if (a.mms) v = v + src_w[t];
       }
     }
-  } else if (t < (long long)g.NW + g.NU) {
-    long long u = t - g.NW;
-    int j = (int)(u % (Nz + 2)), i = (int)(u / (Nz + 2));
+  } else if (t < g.NW + g.NU) {
+    const int u = t - g.NW;
+    const int j = u % (Nz + 2), i = u / (Nz + 2);
     if (j >= 1 && j <= Nz) {
       double ad;
       if (i == 0 || i == Nx) ad = (advx[(size_t)j - 1] + advx[(size_t)Nx * Nz + j - 1]) / 2.0;
       else ad = advx[(size_t)i * Nz + j - 1];
-      v = (a.a2 * AT(rhoUo, j - 1, i) + a.a3 * AT(rhoUoo, j - 1, i)) / a.dt - ad;
+      v = (a.a2 * AT(rhoUo, j - 1, i) + a.a3 * AT(rhoUoo, j - 1, i)) * a.idt - ad;
       if (a.mms) v = v + src_u[u];
-      if (a.mms && (int)u == a.pin_u) v = pin_u_val;
+      if (a.mms && u == a.pin_u) v = pin_u_val;
     }
   } else {
-    int p = (int)(t - g.NW - g.NU);
-    int j = p % (Nz + 2), i = p / (Nz + 2);
+    const int p = t - g.NW - g.NU;
+    const int j = p % (Nz + 2), i = p / (Nz + 2);
     if (j >= 1 && j <= Nz && i >= 1 && i <= Nx) {
       v = AT(MFS, j - 1, i - 1);
       if (a.mms) v = v + src_p[p];
@@ -2224,20 +2244,26 @@ __global__ void scl_kernel(Geo g, OpConst k, const double* __restrict__ cw, cons
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long n = (long long)g.NW + g.NU + g.NP;
   if (t >= n) return;
-  double d, extra = 0.0;
-  if (t < g.NW) d = cw[t];
-  else if (t < (long long)g.NW + g.NU) d = cu[t - g.NW];
+  // scl = 1 / (sqrt|d| + sqrt(eta / rho)) (fluidmech.jl:496-501), with
+  // sqrt(eta / rho) only on the pressure rows.  The velocity rows and the
+  // interior pressure rows (d = 0) take one reciprocal square root, the
+  // pressure rows one division: the scaling only conditions the solve, so
+  // rounding differences in it move the solution by far less than the
+  // solve's tolerance, and FP64 division and square root are slow here.
+  double s;
+  if (t < g.NW) s = rsqrt(fabs(cw[t]));
+  else if (t < (long long)g.NW + g.NU) s = rsqrt(fabs(cu[t - g.NW]));
   else {
-    int p = (int)(t - g.NW - g.NU);
-    int j = p % (g.Nz + 2), i = p / (g.Nz + 2);
-    bool interior = j >= 1 && j <= g.Nz && i >= 1 && i <= g.Nx;
-    d = interior ? 0.0 : 1.0;
+    const int p = (int)(t - g.NW - g.NU);
+    const int j = p % (g.Nz + 2), i = p / (g.Nz + 2);
+    const bool interior = j >= 1 && j <= g.Nz && i >= 1 && i <= g.Nx;
+    double d = interior ? 0.0 : 1.0;
     if (p == k.pin_p || (k.open_cnv && j == g.Nz)) d = 1.0;
-    double sp = interior ? AT(rho, j - 1, i - 1) / AT(eta, j - 1, i - 1) : 1.0;
-    extra = sqrt(1.0 / sp);
-    if (interior) etarho[(size_t)(i - 1) * g.Nz + j - 1] = 1.0 / sp;
+    const double er = interior ? AT(eta, j - 1, i - 1) / AT(rho, j - 1, i - 1) : 1.0;   // eta / rho
+    if (interior) etarho[(size_t)(i - 1) * g.Nz + j - 1] = er;
+    s = d == 0.0 ? rsqrt(er) : 1.0 / (sqrt(d) + sqrt(er));
   }
-  scl[t] = 1.0 / (sqrt(fabs(d)) + extra);
+  scl[t] = s;
 }
 
 // write the solution back (x is the physical unknown vector)
@@ -3178,9 +3204,7 @@ __global__ void combine_dev_kernel(long long n, const KrylovDev* __restrict__ kd
   if (t >= n) return;
   const T* zk = Z + t;
   if (dscl) {
-    T acc = (T)0;
-    for (int k = 0; k < m; ++k, zk += ldz) acc += ys[k] * *zk;
-    x[t] += acc / dscl[t];
+    x[t] += combine_sum<T>(ys, m, zk, ldz) / dscl[t];
     return;
   }
   T s = x[t];
@@ -3882,7 +3906,8 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     XC_CUDA_TRY(cudaMemcpyAsync(w->srcu, mms->src_U, sizeof(double) * g.NU, cudaMemcpyHostToDevice, s));
     XC_CUDA_TRY(cudaMemcpyAsync(w->srcp, mms->src_P, sizeof(double) * g.NP, cudaMemcpyHostToDevice, s));
   }
-  RhsArgs ra{coefs[0], coefs[1], coefs[2], dt, p.g0, p.D, p.h, k.open_cnv ? 1.0 : 0.0, mms ? 1 : 0, k.pin_p, k.pin_u};
+  RhsArgs ra{coefs[0], coefs[1], coefs[2], dt, p.g0, p.D, p.h, k.open_cnv ? 1.0 : 0.0, 1.0 / dt, mms ? 1 : 0, k.pin_p,
+             k.pin_u};
   rhs_kernel<<<nblk(n), 256, 0, s>>>(g, ra, CF(c, FLD_Drho), CF(c, FLD_rhoWo), CF(c, FLD_rhoWoo), CF(c, FLD_rhoUo),
                                      CF(c, FLD_rhoUoo), CF(c, FLD_MFS), w->advz, w->advx, c->dscal + SC_MFS_MEAN,
                                      w->srcw, w->srcu, w->srcp, pin_p_val, pin_u_val, w->RR); xc_count_launch();
