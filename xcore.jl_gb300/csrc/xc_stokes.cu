@@ -3613,10 +3613,12 @@ int setup_hier(StokesWork* w, Hier<T>& H, const OpConst& k, const SolveCfg& cfg,
   const Geo& g = w->g;
   const long long n = (long long)g.NW + g.NU + g.NP;
   double* cpd = w->d.cp;
-  p_coef_kernel<<<nblk(g.NP), 256, 0, s>>>(g, (const double*)c->field[FLD_rhow], (const double*)c->field[FLD_rhou],
-                                           cpd); xc_count_launch();
-  XC_LAUNCH_CHECK();
-  if ((void*)&H != (void*)&w->d) {
+  if ((void*)&H == (void*)&w->d) {
+    // the FP64 hierarchy is always set up first; the FP32 one converts its planes
+    p_coef_kernel<<<nblk(g.NP), 256, 0, s>>>(g, (const double*)c->field[FLD_rhow],
+                                             (const double*)c->field[FLD_rhou], cpd); xc_count_launch();
+    XC_LAUNCH_CHECK();
+  } else {
     convert_kernel<double, T><<<nblk(4LL * g.NP), 256, 0, s>>>(4LL * g.NP, cpd, H.cp); xc_count_launch();
     convert_kernel<double, T><<<nblk(n), 256, 0, s>>>(n, w->d.scl, H.scl); xc_count_launch();
     convert_kernel<double, T><<<nblk((long long)g.Nz * g.Nx), 256, 0, s>>>((long long)g.Nz * g.Nx, w->d.etarho,
