@@ -270,13 +270,18 @@ __global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double i2L0h, d
 // raw sum sq dev, flt mean, flt sum sq dev} per field
 // (the two standard deviations, the same for every cell, are formed once per
 // block by the same operations)
+// (the ratio raw std / filtered std, the same for every cell, is formed once
+// per block: the per-cell FP64 division of (v - mean) raw / flt becomes a
+// product, within the 1e-12 tolerance of these fields)
 __global__ void rescale_kernel(int Nz, int Nx, DView f0, DView f1, DView f2, const double* st) {
-  __shared__ double sd[6];
+  __shared__ double ratio[3];
+  __shared__ int use[3];
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     const double nm1 = (double)Nz * (double)Nx - 1.0;
     for (int q = 0; q < 3; ++q) {
-      sd[2 * q] = sqrt(st[4 * q + 1] / nm1);
-      sd[2 * q + 1] = sqrt(st[4 * q + 3] / nm1);
+      const double raw_std = sqrt(st[4 * q + 1] / nm1), flt_std = sqrt(st[4 * q + 3] / nm1);
+      use[q] = flt_std > XC_EPS;
+      ratio[q] = raw_std / flt_std;
     }
   }
   __syncthreads();
@@ -286,10 +291,9 @@ __global__ void rescale_kernel(int Nz, int Nx, DView f0, DView f1, DView f2, con
   DView fs[3] = {f0, f1, f2};
   for (int q = 0; q < 3; ++q) {
     const double* s = st + 4 * q;
-    const double raw_std = sd[2 * q], flt_std = sd[2 * q + 1];
-    if (flt_std > XC_EPS) {
+    if (use[q]) {
       double v = AT(fs[q], j, i);
-      AT(fs[q], j, i) = (((v - s[2]) * raw_std) / flt_std) + s[0];
+      AT(fs[q], j, i) = ((v - s[2]) * ratio[q]) + s[0];
     }
   }
 }

@@ -254,12 +254,17 @@ __global__ void blend_segvisc_kernel(int Nz, int Nx, const double* min_etai, dou
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
+  // The harmonic cap 1 / (1/emax + 1/etai) as emax etai / (emax + etai) and
+  // (v D0) / (en / r) as (v D0) r / en: one FP64 division each instead of
+  // three and two (a division costs about ten FP64 instructions on this GPU;
+  // these fields carry the 1e-12 tolerance)
   double emax = (*min_etai) * etacntr;
-  double e = 1.0 / (1.0 / emax + 1.0 / AT(etai, j, i));
+  const double ei = AT(etai, j, i);
+  double e = (emax * ei) / (emax + ei);
   double en = 0.5 * e + 0.5 * AT(eta, j, i);
   AT(eta, j, i) = en;
   double r = AT(rho, j, i), v = AT(V, j, i);
-  AT(ReD, j, i) = (v * D0) / (en / r);
+  AT(ReD, j, i) = ((v * D0) * r) / en;
   double vxc = AT(vx, j, i), em = AT(etamix, j, i);
   double Re = ((vxc * l0) * r) / em;
   double f = 1.0 - exp(-Re);
@@ -281,11 +286,13 @@ __global__ void etas_blend_kernel(int Nz, int Nx, const double* min_etasi, doubl
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
+  // one division each, as in blend_segvisc_kernel
   double emax = (*min_etasi) * etacntr;
-  double e = 1.0 / (1.0 / emax + 1.0 / AT(etasi, j, i));
+  const double ei = AT(etasi, j, i);
+  double e = (emax * ei) / (emax + ei);
   double en = 0.5 * e + 0.5 * AT(etas, j, i);
   AT(etas, j, i) = en;
-  AT(Red, j, i) = (AT(vx, j, i) * d0) / (en / AT(rho, j, i));
+  AT(Red, j, i) = ((AT(vx, j, i) * d0) * AT(rho, j, i)) / en;
 }
 
 // compute_corner_eta! (update.jl:411-426, always periodic x / closed z as
