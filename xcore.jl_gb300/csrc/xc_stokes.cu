@@ -87,6 +87,7 @@ Geo make_geo(int Nz, int Nx, double h) {
 // row-local scalars of the operator
 struct OpConst {
   double a1, gamma, dt, g0;
+  double idt;          // 1 / dt (the coefficient kernels multiply instead of dividing per row)
   int sds, top_cnv, bot_cnv;
   int sailor;          // 0 in MMS mode (fluidmech.jl:218, 293)
   int pin_p;           // flat P index (0..NP-1) of the pressure pin
@@ -113,10 +114,12 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
   XC_PDL_WAIT();
   const int Nz = g.Nz, Nx = g.Nx;
   const double invh = g.invh, invh2 = invh * invh;
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // 32-bit row indices (a level's unknowns are checked below 2^31 at setup):
+  // a 64-bit integer division per row cost more than the coefficients
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
   const double c23 = 2.0 / 3.0, c13 = 1.0 / 3.0;
   if (t < g.NW) {
-    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    int j = t % (Nz + 1), i = t / (Nz + 1);
     double c[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (i == 0 || i == Nx + 1 || j == 0) {
       c[0] = 1.0;
@@ -132,7 +135,7 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
     } else {
       double C1 = etaco[(size_t)(i - 1) * (Nz + 1) + j], C2 = etaco[(size_t)i * (Nz + 1) + j];
       double P1 = eta[(size_t)(i - 1) * Nz + (j - 1)], P2 = eta[(size_t)(i - 1) * Nz + j];
-      double iner = k.a1 * rhow[(size_t)(i - 1) * (Nz + 1) + j] / k.dt;
+      double iner = k.a1 * rhow[(size_t)(i - 1) * (Nz + 1) + j] * k.idt;
       double d = iner + (c23 * (P1 + P2) * invh2 + 0.5 * (C1 + C2) * invh2);
       double sail = 0.0;
       if (k.sailor) {
@@ -165,7 +168,7 @@ __global__ void vel_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
       int ib = (i == Nx) ? 0 : i;               // icx[i+1]
       double C1 = etaco[(size_t)i * (Nz + 1) + j - 1], C2 = etaco[(size_t)i * (Nz + 1) + j];
       double P1 = eta[(size_t)ia * Nz + j - 1], P2 = eta[(size_t)ib * Nz + j - 1];
-      double iner = (k.a1 + k.gamma) * rhou[(size_t)i * Nz + j - 1] / k.dt;
+      double iner = (k.a1 + k.gamma) * rhou[(size_t)i * Nz + j - 1] * k.idt;
       double d = iner + (c23 * (P1 + P2) * invh2 + 0.5 * (C1 + C2) * invh2);
       double sail = 0.0;
       if (k.sailor) {
@@ -252,16 +255,16 @@ __global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
   XC_PDL_WAIT();
   const int Nz = g.Nz, Nx = g.Nx;
   const double invh = g.invh;
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t < (long long)Nz * Nx) feta[t] = (T)eta[t];
-  if (t < (long long)(Nz + 1) * (Nx + 1)) fetaco[t] = (T)etaco[t];
+  int t = blockIdx.x * blockDim.x + threadIdx.x;   // 32-bit row indices, as vel_coef_kernel
+  if (t < Nz * Nx) feta[t] = (T)eta[t];
+  if (t < (Nz + 1) * (Nx + 1)) fetaco[t] = (T)etaco[t];
   if (t < g.NW) {
-    int j = (int)(t % (Nz + 1)), i = (int)(t / (Nz + 1));
+    int j = t % (Nz + 1), i = t / (Nz + 1);
     double v = 1.0;
     if (i >= 1 && i <= Nx && j == Nz) {
       v = rhow[(size_t)(i - 1) * (Nz + 1) + Nz] * invh;
     } else if (i >= 1 && i <= Nx && j >= 1 && j < Nz) {
-      v = k.a1 * rhow[(size_t)(i - 1) * (Nz + 1) + j] / k.dt;
+      v = k.a1 * rhow[(size_t)(i - 1) * (Nz + 1) + j] * k.idt;
       if (k.sailor) v += (rho[(size_t)(i - 1) * Nz + j] - rho[(size_t)(i - 1) * Nz + j - 1]) * invh * k.g0 * k.dt;
     }
     dw[t] = (T)v;
@@ -276,7 +279,7 @@ __global__ void fly_coef_kernel(Geo g, OpConst k, const double* __restrict__ eta
     double v = 1.0;
     if (j >= 1 && j <= Nz) {
       int ia = (i == 0) ? Nx - 1 : i - 1, ib = (i == Nx) ? 0 : i;
-      v = (k.a1 + k.gamma) * rhou[(size_t)i * Nz + j - 1] / k.dt;
+      v = (k.a1 + k.gamma) * rhou[(size_t)i * Nz + j - 1] * k.idt;
       if (k.sailor) v += (rho[(size_t)ib * Nz + j - 1] - rho[(size_t)ia * Nz + j - 1]) * invh * k.g0 * k.dt;
     }
     du[t] = (T)v;
@@ -1087,9 +1090,16 @@ __device__ void gj_invert_cta(R* M, int n, int* piv, int* ok, R* fcol, double* r
       for (int i = lane; i < n; i += 32) fcol[i] = M[i * n + k];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-      const int i = e / n, c = e - i * n;
-      if (i != k) M[e] = (c == k ? (R)0 : M[e]) - fcol[i] * M[k * n + c];
+    // thread (row group, column): column c = tid mod 64 of rows tid / 64,
+    // + blockDim / 64, ... (n <= 64; no index division per entry, the pivot
+    // row's entry of the column read once); the same update of each entry
+    {
+      const int c = threadIdx.x & 63, rs = blockDim.x >> 6;
+      if (c < n) {
+        const R mk = M[k * n + c];
+        for (int i = threadIdx.x >> 6; i < n; i += rs)
+          if (i != k) M[i * n + c] = (c == k ? (R)0 : M[i * n + c]) - fcol[i] * mk;
+      }
     }
     __syncthreads();
   }
@@ -3870,7 +3880,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
                              CView{w->wx, Nz + 1}, p.h, DView{w->advx, Nz}, DView{nullptr, 0}, DView{nullptr, 0}, s));
   // operator constants
   OpConst k;
-  k.a1 = coefs[0]; k.gamma = p.gamma; k.dt = dt; k.g0 = p.g0;
+  k.a1 = coefs[0]; k.gamma = p.gamma; k.dt = dt; k.g0 = p.g0; k.idt = 1.0 / dt;
   k.sds = p.sds; k.top_cnv = p.top_cnv; k.bot_cnv = p.bot_cnv;
   k.sailor = mms ? 0 : 1;
   k.mms = mms ? 1 : 0;
