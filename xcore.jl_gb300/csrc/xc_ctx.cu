@@ -396,15 +396,24 @@ static int step_impl(xc_ctx* c, int step, double dt, int fixed_sweeps, double rt
     // initial state) left -- V, vx, fReL, ke, ks, chi, the face fractions and
     // the stored noise -- none of which phsevo! or fluidmech! write, and
     // neither of them reads its results: it runs on the side stream beside
-    // the latency-bound Stokes solve, and update_phase_velocities! waits for it
-    XC_CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
-    XC_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-    int nst = noise_impl(c, dt, it == 1, it == 1 ? re : nullptr, it == 1 ? rs : nullptr, c->side,
-                         c->red_partials_side);
-    if (nst != XC_OK) { join(); return finish(nst); }
+    // the latency-bound iterations of the Stokes solve (forked once the
+    // solve's FP64 right-hand side and setup are enqueued), and
+    // update_phase_velocities! waits for it
+    bool forked = false;
+    int nst = XC_OK;
+    const std::function<int()> fork_noise = [&]() -> int {
+      forked = true;
+      XC_CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
+      XC_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+      nst = noise_impl(c, dt, it == 1, it == 1 ? re : nullptr, it == 1 ? rs : nullptr, c->side,
+                       c->red_partials_side);
+      return XC_OK;
+    };
     xc_solver_stats ss;
     std::memset(&ss, 0, sizeof(ss));
-    st = fluidmech_impl(c, coefs, dt, opts, &ss, nullptr);
+    st = fluidmech_impl(c, coefs, dt, opts, &ss, nullptr, &fork_noise);
+    if (!forked) fork_noise();   // a solve that returned before its iterations
+    if (nst != XC_OK) { join(); return finish(nst); }
     XC_TRY(finish(join()));
     // a solve that stopped at its iteration cap leaves a usable iterate; the
     // step goes on as the reference's would and reports it at the end

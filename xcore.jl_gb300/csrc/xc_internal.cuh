@@ -1,6 +1,8 @@
 // Internal declarations shared by the translation units of libxcore_gb300.
 #pragma once
 
+#include <functional>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <atomic>
@@ -264,8 +266,12 @@ int stokes_create(xc_ctx* c);
 void stokes_destroy(xc_ctx* c);
 struct MmsData { const double *src_W, *src_U, *src_P, *W_exact, *U_exact, *P_exact; };
 int stokes_bench(xc_ctx* c, int which, int iters, double out[4]);
+// before_solve (may be null) is called once on the host after the solve's
+// right-hand side and setup have been enqueued and before its iterations:
+// the step forks noise! there, so that it runs beside the latency-bound
+// iterations rather than beside the FP64 assembly kernels
 int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_opts* opts,
-                   xc_solver_stats* stats, const MmsData* mms);
+                   xc_solver_stats* stats, const MmsData* mms, const std::function<int()>* before_solve = nullptr);
 
 // machine epsilon of Float64 and its square root (eps(T), sqrt(eps(T)))
 #define XC_EPS 2.220446049250313080847e-16

@@ -3840,7 +3840,7 @@ extern "C" int xc_stokes_apply_scaled(xc_ctx* c, const float* v, float* y) {
 }
 
 int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_opts* opts,
-                   xc_solver_stats* stats, const MmsData* mms) {
+                   xc_solver_stats* stats, const MmsData* mms, const std::function<int()>* before_solve) {
   StokesWork* w = c->stokes;
   if (!w || !w->ok) { xc_set_error("fluidmech: grid too small for the Stokes solver (need Nz, Nx >= 4)"); return XC_BAD_ARG; }
   xc_solver_opts o;
@@ -4006,6 +4006,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
   if (o.kind == XC_SOLVER_MIXED) {
     if (!w->f_alloc) { XC_TRY(alloc_hier<float>(w, w->f, 30)); w->f_alloc = true; }
     XC_TRY(setup_hier<float>(w, w->f, k, cfg, c, s));
+    if (before_solve) XC_TRY((*before_solve)());
     if (o.outer_solver == 1) {
       div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, w->d.y); xc_count_launch();
       status = fgmres_outer(w, k, cfg, icfg, w->r, o.rtol, o.maxit, o.inner_rtol, o.inner_maxit, &its,
@@ -4079,6 +4080,7 @@ int fluidmech_impl(xc_ctx* c, const double coefs[6], double dt, const xc_solver_
     }
     }
   } else {
+    if (before_solve) XC_TRY((*before_solve)());
     div_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->x, w->d.scl, w->d.y); xc_count_launch();
     status = fgmres<double>(w, w->d, k, cfg, w->r, o.rtol, o.maxit, &its, &relres, s);
     mul_kernel<double><<<nblk(n), 256, 0, s>>>(n, w->d.y, w->d.scl, w->x); xc_count_launch();
