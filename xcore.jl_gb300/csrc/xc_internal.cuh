@@ -2,6 +2,7 @@
 #pragma once
 
 #include <functional>
+#include <utility>
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -104,6 +105,32 @@ extern thread_local long long g_xc_thread_launches;
 inline void xc_count_launch() {
   ++g_xc_thread_launches;
   g_xc_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+// Programmatic dependent launch: a kernel that begins with XC_PDL_WAIT()
+// waits there for the grid before it on the stream to finish and flush its
+// memory (a no-op when launched without the attribute), so it may be launched
+// with programmatic stream serialization -- scheduled while the previous
+// kernel drains instead of after it, hiding the launch gap.
+#define XC_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+
+// launch with programmatic stream serialization (the kernel must begin with
+// XC_PDL_WAIT()), counted like a plain launch
+template <typename... KArgs, typename... Args>
+inline void xc_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                      Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+  xc_count_launch();
 }
 
 #define XC_TRY(expr)               \

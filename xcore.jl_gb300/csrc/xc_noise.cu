@@ -165,6 +165,7 @@ __device__ __forceinline__ int bitrev(int i, int logM) { return __brev(i) >> (32
 __global__ void line_filter_kernel(CView in, DView out, int rows, int cols, int axis, int M,
                                    int logM, const double* __restrict__ khat,
                                    const double2* __restrict__ tw, int P) {
+  XC_PDL_WAIT();
   extern __shared__ double2 buf[];
   const int L = axis == 0 ? rows : cols;
   const int nlines = axis == 0 ? cols : rows;
@@ -229,8 +230,8 @@ int run_line_filter(const LineFilter& lf, CView in, DView out, int rows, int col
   if (smem > 48 * 1024)
     XC_CUDA_TRY(cudaFuncSetAttribute(line_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int threads = lf.M * P >= 1024 ? 512 : 256;
-  line_filter_kernel<<<(npairs + P - 1) / P, threads, smem, s>>>(in, out, rows, cols, axis, lf.M,
-                                                                 lf.logM, lf.khat, lf.tw, P); xc_count_launch();
+  xc_launch(line_filter_kernel, (npairs + P - 1) / P, threads, smem, s, in, out, rows, cols, axis, lf.M,
+                                                                 lf.logM, lf.khat, lf.tw, P);
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -240,6 +241,7 @@ __global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double i2L0h, d
                           double dt, double cdt, double fL, double fl, CView V, CView vx, CView fReL, CView ke, CView chi,
                           CView ks, CView psieo, CView psixo, CView psiso, CView re, CView rs,
                           DView psie, DView psix, DView psis) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -274,6 +276,7 @@ __global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double i2L0h, d
 // per block: the per-cell FP64 division of (v - mean) raw / flt becomes a
 // product, within the 1e-12 tolerance of these fields)
 __global__ void rescale_kernel(int Nz, int Nx, DView f0, DView f1, DView f2, const double* st) {
+  XC_PDL_WAIT();
   __shared__ double ratio[3];
   __shared__ int use[3];
   if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -320,6 +323,7 @@ __device__ __forceinline__ double exp_tail(double y) { return y < -38.0 ? 0.0 : 
 __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CView chiw,
                                CView muw, CView chiu, CView muu, DView xieu, DView xiew,
                                DView xixu, DView xixw, DView xisu, DView xisw) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz + 1 || i > Nx + 1) return;
@@ -344,6 +348,7 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
 // speed magnitudes (noise.jl:223-236)
 __global__ void speeds_kernel(int Nz, int Nx, CView xisw, CView xisu, CView xixw, CView xixu,
                               CView xiew, CView xieu, DView xis, DView xix, DView xie) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -398,12 +403,12 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
     if (rs) XC_CUDA_TRY(cudaMemcpyAsync(c->field[FLD_rs], rs, nb, cudaMemcpyHostToDevice, s));
   }
   dim3 blk(32, 8);
-  ou_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, p.Xi, p.L0h, 2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt, 1.0 / (1e2 * dt), np->fL, np->fl, CF(c, FLD_V),
+  xc_launch(ou_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, p.Xi, p.L0h, 2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt,
+      1.0 / (1e2 * dt), np->fL, np->fl, CF(c, FLD_V),
       CF(c, FLD_vx),
       CF(c, FLD_fReL), CF(c, FLD_ke), CF(c, FLD_chi), CF(c, FLD_ks), CF(c, FLD_psieo),
       CF(c, FLD_psixo), CF(c, FLD_psiso), CF(c, FLD_re), CF(c, FLD_rs), F(c, FLD_psie),
-      F(c, FLD_psix), F(c, FLD_psis)); xc_count_launch();
+      F(c, FLD_psix), F(c, FLD_psis));
   XC_LAUNCH_CHECK();
   // filtered fields in tmp[2..4], z-pass intermediate in tmp[5]
   DView flt[3] = {DView{c->tmp[2], Nz}, DView{c->tmp[3], Nz}, DView{c->tmp[4], Nz}};
@@ -429,16 +434,16 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
   }
   XC_TRY(reduce_batch(c, means, 6, s, partials));
   XC_TRY(reduce_batch(c, devs, 6, s, partials));
-  rescale_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(Nz, Nx, flt[0], flt[1], flt[2], st); xc_count_launch();
+  xc_launch(rescale_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, flt[0], flt[1], flt[2], st);
   XC_LAUNCH_CHECK();
-  stagger_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, s>>>(
-      Nz, Nx, CView{flt[0].p, Nz}, CView{flt[1].p, Nz}, CView{flt[2].p, Nz}, CF(c, FLD_chiw),
+  xc_launch(stagger_kernel, grid2d(Nz + 2, Nx + 2, blk), blk, 0, s, Nz, Nx, CView{flt[0].p, Nz},
+      CView{flt[1].p, Nz}, CView{flt[2].p, Nz}, CF(c, FLD_chiw),
       CF(c, FLD_muw), CF(c, FLD_chiu), CF(c, FLD_muu), F(c, FLD_xieu), F(c, FLD_xiew),
-      F(c, FLD_xixu), F(c, FLD_xixw), F(c, FLD_xisu), F(c, FLD_xisw)); xc_count_launch();
+      F(c, FLD_xixu), F(c, FLD_xixw), F(c, FLD_xisu), F(c, FLD_xisw));
   XC_LAUNCH_CHECK();
-  speeds_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, CF(c, FLD_xisw), CF(c, FLD_xisu), CF(c, FLD_xixw), CF(c, FLD_xixu), CF(c, FLD_xiew),
-      CF(c, FLD_xieu), F(c, FLD_xis), F(c, FLD_xix), F(c, FLD_xie)); xc_count_launch();
+  xc_launch(speeds_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, CF(c, FLD_xisw), CF(c, FLD_xisu),
+      CF(c, FLD_xixw), CF(c, FLD_xixu), CF(c, FLD_xiew),
+      CF(c, FLD_xieu), F(c, FLD_xis), F(c, FLD_xix), F(c, FLD_xie));
   XC_LAUNCH_CHECK();
   return XC_OK;
 }

@@ -99,6 +99,7 @@ __device__ __forceinline__ double red_thread(const RedJob& J, double ctr) {
 }
 
 __global__ void __launch_bounds__(RB) batch_reduce_kernel(RedBatch B, double* partials, unsigned* counters) {
+  XC_PDL_WAIT();
   __shared__ double sh[RB / 32];
   __shared__ int last;
   const RedJob& J = B.job[blockIdx.y];
@@ -171,7 +172,7 @@ int reduce_batch(xc_ctx* c, const RedJob* jobs, int njobs, cudaStream_t s, doubl
       B.job[k].nblk = blocks_for((long long)B.job[k].rows * B.job[k].cols);
       gx = B.job[k].nblk > gx ? B.job[k].nblk : gx;
     }
-    batch_reduce_kernel<<<dim3((unsigned)gx, (unsigned)nj), RB, 0, s>>>(B, part, counters); xc_count_launch();
+    xc_launch(batch_reduce_kernel, dim3((unsigned)gx, (unsigned)nj), RB, 0, s, B, part, counters);
     XC_LAUNCH_CHECK();
   }
   return XC_OK;

@@ -167,6 +167,7 @@ template <int S, bool HALOD>
 __global__ void __launch_bounds__(NT) advect_tile_kernel(
     const double* __restrict__ f, int ldf, int Nz, int Nx, int xBC, int zBC,
     CView u, CView w, double invh, DView adv, DView qx, DView qz) {
+  XC_PDL_WAIT();
   constexpr int G = Halo<S>::G;
   constexpr int HZ = TZ + 2 * G, HX = TX + 2 * G;
   __shared__ double sf[HX][HZ];
@@ -261,6 +262,7 @@ template <bool HALOD>
 __global__ void __launch_bounds__(NT) diffus_tile_kernel(
     const double* __restrict__ f, const double* __restrict__ k1, const double* __restrict__ k2,
     int ld, int Nz, int Nx, int xBC, int zBC, double invh, DView dff, DView qx, DView qz) {
+  XC_PDL_WAIT();
   constexpr int G = 1;
   constexpr int HZ = TZ + 2 * G, HX = TX + 2 * G;
   __shared__ double sf[HX][HZ];
@@ -333,6 +335,7 @@ __global__ void __launch_bounds__(NT) diffus_tile_kernel(
 // MATLAB-sized boundary rows/cols of the face-flux arrays (advect.jl:779-795,
 // diffus.jl:194-208): qz cols 0 / Nx+1 and qx rows 0 / Nz+1.
 __global__ void pad_fluxes_kernel(DView qx, DView qz, int Nz, int Nx, int xBC, int zBC) {
+  XC_PDL_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < Nz + 1) {   // qz (Nz+1, Nx+2)
     if (xBC == XC_PERIODIC && Nx > 1) {
@@ -357,6 +360,7 @@ __global__ void pad_fluxes_kernel(DView qx, DView qz, int Nz, int Nx, int xBC, i
 // ghost ring of a halo'd array (ghosts.jl:18-51; for N >= halo the x-then-z
 // fill equals reading the BC-mapped interior cell, corners included)
 __global__ void fill_ghosts_kernel(double* f, int Nz, int Nx, int g, int zBC, int xBC) {
+  XC_PDL_WAIT();
   const int rows = Nz + 2 * g, cols = Nx + 2 * g;
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)rows * cols) return;
@@ -374,6 +378,7 @@ __global__ void phsevo_tail_kernel(int Nz, int Nx, double a1, double a2, double 
                                    CView rho, CView advn_X, CView advn_M, DView advn_rho,
                                    CView dffn_X, CView bndshape, DView Gx, DView dXdt,
                                    CView dXdto, CView dXdtoo) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -404,9 +409,9 @@ int launch_advect(const double* f, int ldf, bool halod, int Nz, int Nx, int xBC,
   // the last tile of each axis also writes the closing face (index Nz / Nx)
   dim3 grid((Nz + TZ - 1) / TZ, (Nx + TX - 1) / TX);
   if (halod) {
-    advect_tile_kernel<S, true><<<grid, NT, 0, s>>>(f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz); xc_count_launch();
+    xc_launch(advect_tile_kernel<S, true>, grid, NT, 0, s, f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz);
   } else {
-    advect_tile_kernel<S, false><<<grid, NT, 0, s>>>(f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz); xc_count_launch();
+    xc_launch(advect_tile_kernel<S, false>, grid, NT, 0, s, f, ldf, Nz, Nx, xBC, zBC, u, w, invh, adv, qx, qz);
   }
   XC_LAUNCH_CHECK();
   return XC_OK;
@@ -440,7 +445,8 @@ int stencil_advect_flux(const double* f, int ldf, bool halod, int Nz, int Nx, in
     case XC_FROMM: return launch_advect<XC_FROMM>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
     case XC_WENO3: return launch_advect<XC_WENO3>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
     case XC_WENO5: return launch_advect<XC_WENO5>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
-    case kWeno5OneDiv: return launch_advect<kWeno5OneDiv>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
+    case kWeno5OneDiv:
+      return launch_advect<kWeno5OneDiv>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
     default: return launch_advect<XC_TVDIM>(f, ldf, halod, Nz, Nx, xBC, zBC, u, w, invh, adv, qx_int, qz_int, s);
   }
 }
@@ -451,9 +457,9 @@ static int diffus_launch(const double* f, const double* k1, const double* k2, in
   dim3 grid((Nz + TZ - 1) / TZ, (Nx + TX - 1) / TX);
   double invh = 1.0 / h;
   if (halod) {
-    diffus_tile_kernel<true><<<grid, NT, 0, s>>>(f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz); xc_count_launch();
+    xc_launch(diffus_tile_kernel<true>, grid, NT, 0, s, f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz);
   } else {
-    diffus_tile_kernel<false><<<grid, NT, 0, s>>>(f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz); xc_count_launch();
+    xc_launch(diffus_tile_kernel<false>, grid, NT, 0, s, f, k1, k2, ld, Nz, Nx, xBC, zBC, invh, dff, qx, qz);
   }
   XC_LAUNCH_CHECK();
   return XC_OK;
@@ -467,7 +473,7 @@ int stencil_diffus_flux(const double* f, const double* k, int ld, bool halod, in
 
 int pad_face_fluxes(DView qx, DView qz, int Nz, int Nx, int xBC, int zBC, cudaStream_t s) {
   int n = (Nz > Nx ? Nz : Nx) + 1;
-  pad_fluxes_kernel<<<(n + 255) / 256, 256, 0, s>>>(qx, qz, Nz, Nx, xBC, zBC); xc_count_launch();
+  xc_launch(pad_fluxes_kernel, (n + 255) / 256, 256, 0, s, qx, qz, Nz, Nx, xBC, zBC);
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -496,11 +502,11 @@ int phsevo_impl(xc_ctx* c, int scheme, const double coefs[6], double dt, double 
   XC_TRY(pad_face_fluxes(F(c, FLD_qx_advn_M), F(c, FLD_qz_advn_M), Nz, Nx, xBC, zBC, s));
   XC_TRY(pad_face_fluxes(F(c, FLD_qx_dffn_X), F(c, FLD_qz_dffn_X), Nz, Nx, xBC, zBC, s));
   dim3 blk(32, 8);
-  phsevo_tail_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, coefs[0], coefs[1], coefs[2], coefs[3], coefs[4], coefs[5], dt, alpha, c->p.G0,
+  xc_launch(phsevo_tail_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, coefs[0], coefs[1], coefs[2], coefs[3],
+      coefs[4], coefs[5], dt, alpha, c->p.G0,
       X, CF(c, FLD_Xo), CF(c, FLD_Xoo), M, F(c, FLD_x), F(c, FLD_m), CF(c, FLD_rho),
       CF(c, FLD_advn_X), CF(c, FLD_advn_M), F(c, FLD_advn_rho), CF(c, FLD_dffn_X),
-      CF(c, FLD_bndshape), F(c, FLD_Gx), F(c, FLD_dXdt), CF(c, FLD_dXdto), CF(c, FLD_dXdtoo)); xc_count_launch();
+      CF(c, FLD_bndshape), F(c, FLD_Gx), F(c, FLD_dXdt), CF(c, FLD_dXdto), CF(c, FLD_dXdtoo));
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -516,7 +522,7 @@ extern "C" int xc_fill_ghosts(double* f, int Nz, int Nx, int halo, int zBC, int 
     return XC_BAD_ARG;
   }
   long long n = (long long)(Nz + 2 * halo) * (Nx + 2 * halo);
-  fill_ghosts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(f, Nz, Nx, halo, zBC, xBC); xc_count_launch();
+  xc_launch(fill_ghosts_kernel, (unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream, f, Nz, Nx, halo, zBC, xBC);
   XC_LAUNCH_CHECK();
   return XC_OK;
 }

@@ -32,12 +32,9 @@
 
 namespace {
 
-// Programmatic dependent launch: every kernel of this unit first waits for the
-// grid it depends on to finish and flush its memory (a no-op when launched
-// without the attribute), so the solver's graph-captured launches may be
-// issued with programmatic serialization -- the next kernel is scheduled while
-// the previous one drains instead of after it, hiding the launch gap.
-#define XC_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+// Every kernel of this unit begins with XC_PDL_WAIT() (xc_internal.cuh), so the
+// solver's graph-captured launches may be issued with programmatic
+// serialization.
 
 // programmatic launches on (the default) or off for the solves of this thread
 thread_local bool g_xc_pdl = true;

@@ -36,6 +36,7 @@ struct Rheo {
 __global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rhox0, Rheo r,
                                         CView x, CView m, DView rho, DView chi, DView mu,
                                         uint8_t* hasx, uint8_t* hasm, DView etamix) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -84,6 +85,7 @@ __global__ void interp_kernel(int Nz, int Nx, int xBC, int zBC, double rhom0, do
                               DView rhou, DView Drhom, DView Drhox, DView chiw, DView muw,
                               DView chiu, DView muu, DView x_w, DView m_w, DView x_u,
                               DView m_u) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz + 1 || i > Nx + 1) return;
@@ -127,6 +129,7 @@ __global__ void interp_kernel(int Nz, int Nx, int xBC, int zBC, double rhom0, do
 // order.  Same additions as a thread walking its row alone.
 constexpr int kRowTile = 128;
 __global__ void __launch_bounds__(256) rowmean_kernel(int Nz, int Nx, CView rhow, double* rhoref) {
+  XC_PDL_WAIT();
   __shared__ double tile[kRowTile][33];
   const int j0 = blockIdx.x * 32;
   const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;   // row in the block, column phase
@@ -153,6 +156,7 @@ __global__ void __launch_bounds__(256) rowmean_kernel(int Nz, int Nx, CView rhow
 constexpr int kScanChunk = 4096;
 __global__ void __launch_bounds__(256) pressure_scan_kernel(int Nz, double g0, double h, double Ptop,
                                                             const double* rhoref, double* plcol) {
+  XC_PDL_WAIT();
   __shared__ double q[kScanChunk];
   double p = 0.0;
   for (int j0 = 0; j0 < Nz; j0 += kScanChunk) {
@@ -178,6 +182,7 @@ __global__ void __launch_bounds__(256) pressure_scan_kernel(int Nz, double g0, d
 __global__ void drho_pressure_kernel(int Nz, int Nx, double Ptop, const double* rhoref,
                                      const double* plcol, CView rhow, DView Drho, CView P,
                                      DView Pl, DView Pt) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz || i >= Nx) return;
@@ -199,6 +204,7 @@ __device__ __forceinline__ double exz_at(CView W, CView U, int j, int i, double 
 __global__ void kinematics_kernel(int Nz, int Nx, double invh, CView W, CView U, CView wx,
                                   CView wm, DView exz, DView exx, DView ezz, DView Div_V,
                                   DView eII, DView V, DView vx, DView vm) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz || i > Nx) return;
@@ -228,6 +234,7 @@ __global__ void kinematics_kernel(int Nz, int Nx, double invh, CView W, CView U,
 __global__ void viscblend_kernel(int Nz, int Nx, double L0, CView etamix, CView eII, CView rho,
                                  CView V, DView etai, DView etae, DView ke, DView kx, DView ReL,
                                  DView fReL) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -251,6 +258,7 @@ __global__ void blend_segvisc_kernel(int Nz, int Nx, const double* min_etai, dou
                                      CView rho, DView ReD, CView vx, CView etamix, CView ke,
                                      CView fReL, DView Rel, DView fRel, DView ks, DView etat,
                                      DView etasi, DView kx, DView Rc) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -283,6 +291,7 @@ __global__ void blend_segvisc_kernel(int Nz, int Nx, const double* min_etai, dou
 __global__ void etas_blend_kernel(int Nz, int Nx, const double* min_etasi, double etacntr,
                                   double d0, CView etasi, DView etas, CView vx, CView rho,
                                   DView Red) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j >= Nz || i >= Nx) return;
@@ -299,6 +308,7 @@ __global__ void etas_blend_kernel(int Nz, int Nx, const double* min_etasi, doubl
 // update_viscosity! calls it, update.jl:341) and etasw (update.jl:405-407)
 __global__ void corner_eta_etasw_kernel(int Nz, int Nx, int zBC, CView eta, DView etaco,
                                         CView etas, DView etasw) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz || i > Nx) return;
@@ -318,6 +328,7 @@ __global__ void corner_eta_etasw_kernel(int Nz, int Nx, int zBC, CView eta, DVie
 __global__ void stress_kernel(int Nz, int Nx, double D0, CView etaco, CView exz, DView txz,
                               CView eta, CView exx, CView ezz, DView txx, DView tzz, DView tII,
                               CView V, CView kx, DView Ra) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz || i > Nx) return;
@@ -343,6 +354,7 @@ __global__ void phase_velocities_kernel(int Nz, int Nx, int xBC, int zBC, double
                                         CView xisw, CView xixw, CView xiew, CView xisu,
                                         CView xixu, CView xieu, DView wx, DView wm, DView Wx,
                                         DView Wm, DView Ux, DView Um) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz + 1 || i > Nx + 1) return;
@@ -379,6 +391,7 @@ __global__ void store_previous_kernel(int Nz, int Nx, DView X, DView Xo, DView X
                                       DView drhodto, DView drhodtoo, CView rhow, CView W,
                                       DView rhoWo, DView rhoWoo, CView rhou, CView U,
                                       DView rhoUo, DView rhoUoo) {
+  XC_PDL_WAIT();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (j > Nz || i > Nx) return;
@@ -412,15 +425,15 @@ int update_impl(xc_ctx* c) {
          std::log(p.BB[3]),
          1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0,
          std::log(p.etam0 / p.etax0), std::log(p.etax0 / p.etam0)};
-  volfrac_rheology_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
-      F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix)); xc_count_launch();
+  xc_launch(volfrac_rheology_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x),
+      CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
+      F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix));
   XC_LAUNCH_CHECK();
-  interp_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, s>>>(
-      Nz, Nx, p.xBC, p.zBC, p.rhom0, p.rhox0, CF(c, FLD_rho), CF(c, FLD_chi), CF(c, FLD_mu),
+  xc_launch(interp_kernel, grid2d(Nz + 2, Nx + 2, blk), blk, 0, s, Nz, Nx, p.xBC, p.zBC, p.rhom0, p.rhox0,
+      CF(c, FLD_rho), CF(c, FLD_chi), CF(c, FLD_mu),
       CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rhow), F(c, FLD_rhou), F(c, FLD_Drhom),
       F(c, FLD_Drhox), F(c, FLD_chiw), F(c, FLD_muw), F(c, FLD_chiu), F(c, FLD_muu),
-      F(c, FLD_x_w), F(c, FLD_m_w), F(c, FLD_x_u), F(c, FLD_m_u)); xc_count_launch();
+      F(c, FLD_x_w), F(c, FLD_m_w), F(c, FLD_x_u), F(c, FLD_m_u));
   XC_LAUNCH_CHECK();
   // update_pressure! (update.jl:111-138): the row means of rhow and the z
   // prefix sum are chains of dependent FP64 additions in the reference's
@@ -432,44 +445,44 @@ int update_impl(xc_ctx* c) {
   cudaStream_t side = c->side;
   XC_CUDA_TRY(cudaEventRecord(c->ev_fork, s));
   XC_CUDA_TRY(cudaStreamWaitEvent(side, c->ev_fork, 0));
-  rowmean_kernel<<<(Nz + 1 + 31) / 32, 256, 0, side>>>(Nz, Nx, CF(c, FLD_rhow), rhoref); xc_count_launch();
-  pressure_scan_kernel<<<1, 256, 0, side>>>(Nz, p.g0, p.h, p.Ptop, rhoref, plcol); xc_count_launch();
+  xc_launch(rowmean_kernel, (Nz + 1 + 31) / 32, 256, 0, side, Nz, Nx, CF(c, FLD_rhow), rhoref);
+  xc_launch(pressure_scan_kernel, 1, 256, 0, side, Nz, p.g0, p.h, p.Ptop, rhoref, plcol);
   XC_LAUNCH_CHECK();
-  drho_pressure_kernel<<<grid2d(Nz + 1, Nx, blk), blk, 0, side>>>(
-      Nz, Nx, p.Ptop, rhoref, plcol, CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
-      F(c, FLD_Pt)); xc_count_launch();
+  xc_launch(drho_pressure_kernel, grid2d(Nz + 1, Nx, blk), blk, 0, side, Nz, Nx, p.Ptop, rhoref, plcol,
+      CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
+      F(c, FLD_Pt));
   XC_LAUNCH_CHECK();
   XC_CUDA_TRY(cudaEventRecord(c->ev_join, side));
   const double invh = 1.0 / p.h;
-  kinematics_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
-      Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
+  xc_launch(kinematics_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, s, Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U),
+      CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
       F(c, FLD_exx), F(c, FLD_ezz), F(c, FLD_Div_V), F(c, FLD_eII), F(c, FLD_V), F(c, FLD_vx),
-      F(c, FLD_vm)); xc_count_launch();
+      F(c, FLD_vm));
   XC_LAUNCH_CHECK();
   DView etai{c->tmp[0], Nz}, etasi{c->tmp[1], Nz};
-  viscblend_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, p.L0, CF(c, FLD_etamix), CF(c, FLD_eII), CF(c, FLD_rho), CF(c, FLD_V), etai,
-      F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL)); xc_count_launch();
+  xc_launch(viscblend_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, p.L0, CF(c, FLD_etamix), CF(c, FLD_eII),
+      CF(c, FLD_rho), CF(c, FLD_V), etai,
+      F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL));
   XC_LAUNCH_CHECK();
   XC_TRY(reduce_view(c, RED_MIN, CView{etai.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETA));
-  blend_segvisc_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, c->dscal + SC_EMAX_ETA, p.etacntr, p.D0, p.l0, CView{etai.p, Nz}, F(c, FLD_eta),
+  xc_launch(blend_segvisc_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx,
+      c->dscal + SC_EMAX_ETA, p.etacntr, p.D0, p.l0, CView{etai.p, Nz}, F(c, FLD_eta),
       CF(c, FLD_V), CF(c, FLD_rho), F(c, FLD_ReD), CF(c, FLD_vx), CF(c, FLD_etamix),
       CF(c, FLD_ke), CF(c, FLD_fReL), F(c, FLD_Rel), F(c, FLD_fRel), F(c, FLD_ks),
-      F(c, FLD_etat), etasi, F(c, FLD_kx), F(c, FLD_Rc)); xc_count_launch();
+      F(c, FLD_etat), etasi, F(c, FLD_kx), F(c, FLD_Rc));
   XC_LAUNCH_CHECK();
   XC_TRY(reduce_view(c, RED_MIN, CView{etasi.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETAS));
-  etas_blend_kernel<<<grid2d(Nz, Nx, blk), blk, 0, s>>>(
-      Nz, Nx, c->dscal + SC_EMAX_ETAS, p.etacntr, p.d0, CView{etasi.p, Nz}, F(c, FLD_etas),
-      CF(c, FLD_vx), CF(c, FLD_rho), F(c, FLD_Red)); xc_count_launch();
+  xc_launch(etas_blend_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx,
+      c->dscal + SC_EMAX_ETAS, p.etacntr, p.d0, CView{etasi.p, Nz}, F(c, FLD_etas),
+      CF(c, FLD_vx), CF(c, FLD_rho), F(c, FLD_Red));
   XC_LAUNCH_CHECK();
-  corner_eta_etasw_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
-      Nz, Nx, p.zBC, CF(c, FLD_eta), F(c, FLD_etaco), CF(c, FLD_etas), F(c, FLD_etasw)); xc_count_launch();
+  xc_launch(corner_eta_etasw_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, s, Nz, Nx, p.zBC, CF(c, FLD_eta),
+      F(c, FLD_etaco), CF(c, FLD_etas), F(c, FLD_etasw));
   XC_LAUNCH_CHECK();
-  stress_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, s>>>(
-      Nz, Nx, p.D0, CF(c, FLD_etaco), CF(c, FLD_exz), F(c, FLD_txz), CF(c, FLD_eta),
+  xc_launch(stress_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, s, Nz, Nx, p.D0, CF(c, FLD_etaco), CF(c, FLD_exz),
+      F(c, FLD_txz), CF(c, FLD_eta),
       CF(c, FLD_exx), CF(c, FLD_ezz), F(c, FLD_txx), F(c, FLD_tzz), F(c, FLD_tII), CF(c, FLD_V),
-      CF(c, FLD_kx), F(c, FLD_Ra)); xc_count_launch();
+      CF(c, FLD_kx), F(c, FLD_Ra));
   XC_LAUNCH_CHECK();
   XC_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_join, 0));   // update_pressure! on the side stream
   return XC_OK;
@@ -478,12 +491,12 @@ int update_impl(xc_ctx* c) {
 int phase_velocities_impl(xc_ctx* c) {
   const int Nz = c->Nz, Nx = c->Nx;
   dim3 blk(32, 8);
-  phase_velocities_kernel<<<grid2d(Nz + 2, Nx + 2, blk), blk, 0, c->stream>>>(
-      Nz, Nx, c->p.xBC, c->p.zBC, c->p.d0, c->p.g0, CF(c, FLD_etasw), CF(c, FLD_Drhox),
+  xc_launch(phase_velocities_kernel, grid2d(Nz + 2, Nx + 2, blk), blk, 0,
+      c->stream, Nz, Nx, c->p.xBC, c->p.zBC, c->p.d0, c->p.g0, CF(c, FLD_etasw), CF(c, FLD_Drhox),
       CF(c, FLD_bndtaperw), CF(c, FLD_x_w), CF(c, FLD_m_w), CF(c, FLD_x_u), CF(c, FLD_m_u),
       CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_xisw), CF(c, FLD_xixw), CF(c, FLD_xiew),
       CF(c, FLD_xisu), CF(c, FLD_xixu), CF(c, FLD_xieu), F(c, FLD_wx), F(c, FLD_wm),
-      F(c, FLD_Wx), F(c, FLD_Wm), F(c, FLD_Ux), F(c, FLD_Um)); xc_count_launch();
+      F(c, FLD_Wx), F(c, FLD_Wm), F(c, FLD_Ux), F(c, FLD_Um));
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
@@ -491,12 +504,12 @@ int phase_velocities_impl(xc_ctx* c) {
 int store_previous_impl(xc_ctx* c) {
   const int Nz = c->Nz, Nx = c->Nx;
   dim3 blk(32, 8);
-  store_previous_kernel<<<grid2d(Nz + 1, Nx + 1, blk), blk, 0, c->stream>>>(
-      Nz, Nx, F(c, FLD_X), F(c, FLD_Xo), F(c, FLD_Xoo), F(c, FLD_M), F(c, FLD_Mo), F(c, FLD_Moo),
+  xc_launch(store_previous_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, c->stream, Nz, Nx, F(c, FLD_X), F(c,
+      FLD_Xo), F(c, FLD_Xoo), F(c, FLD_M), F(c, FLD_Mo), F(c, FLD_Moo),
       F(c, FLD_dXdt), F(c, FLD_dXdto), F(c, FLD_dXdtoo), F(c, FLD_rho), F(c, FLD_rhoo),
       F(c, FLD_rhooo), F(c, FLD_drhodt), F(c, FLD_drhodto), F(c, FLD_drhodtoo), CF(c, FLD_rhow),
       CF(c, FLD_W), F(c, FLD_rhoWo), F(c, FLD_rhoWoo), CF(c, FLD_rhou), CF(c, FLD_U),
-      F(c, FLD_rhoUo), F(c, FLD_rhoUoo)); xc_count_launch();
+      F(c, FLD_rhoUo), F(c, FLD_rhoUoo));
   XC_LAUNCH_CHECK();
   return XC_OK;
 }
