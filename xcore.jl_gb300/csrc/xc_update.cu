@@ -240,7 +240,7 @@ __global__ void viscblend_kernel(int Nz, int Nx, double L0, CView etamix, CView 
   if (j >= Nz || i >= Nx) return;
   double r = AT(rho, j, i), em = AT(etamix, j, i);
   double k = (AT(eII, j, i) * L0) * L0;
-  double Re = (AT(V, j, i) * L0) / (em / r);
+  double Re = ((AT(V, j, i) * L0) * r) / em;   // (V L0) / (em / r) with one division (1e-12 fields)
   double f = 1.0 - exp(-Re);
   double ee = (f * k) * r;
   AT(etai, j, i) = em + ee;
