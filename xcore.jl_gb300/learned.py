@@ -155,13 +155,13 @@ def inject_viscosity(state: "xc.State", contrast, rng):
     return eta
 
 
-def workload_state(N, seed=0):
+def workload_state(N, seed=0, etacntr=1e4):
     """A State of the 1024^2 mixed-precision workload's physics at N^2
-    (lognormal crystal fraction, etacntr 1e4), initialised, one phsevo! done
-    so every Stokes input is populated."""
+    (lognormal crystal fraction, viscosity contrast cap etacntr), initialised,
+    one phsevo! done so every Stokes input is populated."""
     D = 10.0
     h = D / N
-    par = xc.Parameters(D=D, N=N, L=D, etam0=10.0, x0=0.1, Da=0.0, L0=3 * h, l0=3 * h, etacntr=1e4,
+    par = xc.Parameters(D=D, N=N, L=D, etam0=10.0, x0=0.1, Da=0.0, L0=3 * h, l0=3 * h, etacntr=float(etacntr),
                         ADVN="weno5", TINT="bd2im")
     st = xc.State(par)
     rng = np.random.default_rng(seed)
@@ -235,12 +235,16 @@ def train(net: Network, inputs, targets, steps=2000, lr=2e-3, seed=0, log=None):
 SOLVE = dict(solver="mixed", rtol=1e-9, maxit=600, inner_rtol=5e-2, inner_maxit=30, pressure_sweeps=1)
 
 
-def evaluate(params, N, seed=7, modes=(0, 1, 2), repeats=3):
+def evaluate(params, N, seed=7, modes=(0, 1, 2), repeats=3, contrast=None):
     """The mixed solve of one Stokes system of the workload at N^2 with each
     preconditioner mode: inner iterations, learned fallbacks, final FP64
     residual and the device time of the solve (median of `repeats` after one
-    untimed solve that captures the graphs)."""
+    untimed solve that captures the graphs).  contrast: the viscosity replaced
+    by a smoothed random field of that contrast (inject_viscosity, the form of
+    the training pairs) instead of the workload's rheology."""
     st, coefs, dt = workload_state(N, seed)
+    if contrast is not None:
+        inject_viscosity(st, contrast, np.random.default_rng(seed))
     use(st, params)
     snap = {k: st[k] for k in ("W", "U", "P", "MFS", "drhodt")}
     out = {}
@@ -300,6 +304,10 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--bench-forward", type=int, default=None, metavar="N",
                     help="only time the network's forward pass at N^2 and exit")
+    ap.add_argument("--evaluate", type=int, default=None, metavar="N",
+                    help="only evaluate the saved network (--out) at N^2 against the multigrid and exit")
+    ap.add_argument("--contrast", type=float, default=None,
+                    help="--evaluate with a smoothed random viscosity of this contrast instead of the workload's")
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--N", type=int, default=256)
     ap.add_argument("--samples", type=int, default=2048)
@@ -313,6 +321,13 @@ def main(argv=None):
     if a.bench_forward:
         import json
         log(json.dumps(bench_forward(a.bench_forward)))
+        return
+    if a.evaluate:
+        import json
+        rep = evaluate(load_params(a.out), a.evaluate, contrast=a.contrast)
+        keep = ("iterations", "refinements", "rel_residual", "converged", "learned_fallbacks", "median_ms", "error")
+        log(json.dumps({"N": a.evaluate, "contrast": a.contrast,
+                        "modes": {str(m): {k: v for k, v in r.items() if k in keep} for m, r in rep.items()}}))
         return
     inputs, targets = generate(a.N, a.samples, seed=a.seed, after_vcycle=True, log=log)
     # the loss of predicting zero, for reference: the targets have unit RMS
