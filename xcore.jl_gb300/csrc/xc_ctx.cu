@@ -4,6 +4,8 @@
 #include <cstdarg>
 #include <cstring>
 #include <vector>
+#include <unordered_map>
+#include <mutex>
 
 #include "xc_internal.cuh"
 
@@ -45,6 +47,32 @@ void xc_set_error(const char* fmt, ...) {
 }
 
 extern "C" const char* xc_last_error(void) { return g_err; }
+
+unsigned persistent_grid(const void* kernel, int rows, int cols) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> per_sm;   // resident CTAs of 256 threads per SM
+  static int sms = 0;
+  int b = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (sms == 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    }
+    auto it = per_sm.find(kernel);
+    if (it == per_sm.end()) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0) != cudaSuccess || b < 1) b = 1;
+      cudaGetLastError();
+      per_sm[kernel] = b;
+    } else {
+      b = it->second;
+    }
+  }
+  const long long tiles = (long long)((rows + 31) / 32) * ((cols + 7) / 8);
+  const long long wave = (long long)sms * b;
+  return (unsigned)(tiles < wave ? tiles : wave);
+}
 extern "C" const char* xc_version(void) { return "xcore_gb300 0.1 (sm_103a)"; }
 
 extern "C" int xc_field_count(void) { return FLD_COUNT; }

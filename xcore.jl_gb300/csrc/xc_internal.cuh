@@ -213,6 +213,19 @@ inline dim3 grid2d(int rows, int cols, dim3 blk) {
   return dim3((unsigned)((rows + blk.x - 1) / blk.x), (unsigned)((cols + blk.y - 1) / blk.y));
 }
 
+// Persistent 2-D launches of 32 x 8 threads: a grid of one wave -- as many
+// CTAs as the SMs hold at the kernel's occupancy -- strides over the 32 x 8
+// tiles of a rows x cols domain, so no last wave runs partly empty (the
+// FP64 kernels of the path run 3-4 waves of their data-sized grids).  f(j, i)
+// is the body of one cell; a `return` in it ends that cell.
+template <typename F>
+__device__ __forceinline__ void for_tiles(int rows, int cols, F&& f) {
+  const int nbx = (rows + 31) / 32, nt = nbx * ((cols + 7) / 8);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) f((t % nbx) * 32 + (int)threadIdx.x, (t / nbx) * 8 + (int)threadIdx.y);
+}
+// CTAs of such a launch of `kernel` over rows x cols
+unsigned persistent_grid(const void* kernel, int rows, int cols);
+
 // Julia's max / min of two Float64 (a NaN argument gives NaN; CUDA's fmax /
 // fmin return the other argument instead)
 __host__ __device__ __forceinline__ double jmax(double a, double b) {

@@ -242,30 +242,30 @@ __global__ void ou_kernel(int Nz, int Nx, double Xi, double L0h, double i2L0h, d
                           CView ks, CView psieo, CView psixo, CView psiso, CView re, CView rs,
                           DView psie, DView psix, DView psis) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  // The reference's twelve divisions (noise.jl:160-176) folded to five with
-  // the same values up to rounding (these fields carry the 1e-12 tolerance):
-  // 1/tau_e = 2 (V + eps) / L0h and 1/tau_s = 2 (vx + eps) / l0h as
-  // products, and tau' = 1 / (1/tau + c) + dt with c = 1 / (100 dt) entering
-  // only as -dt / tau' = -dt u / (1 + dt u), u = 1/tau + c.  An FP64 division
-  // costs about ten FP64 instructions on this GPU's narrow FP64 pipe.
-  const double ve = AT(V, j, i) + XC_EPS, vs = AT(vx, j, i) + XC_EPS;
-  const double taue = L0h / (2.0 * ve);
-  const double itaue = ve * i2L0h, itaus = vs * i2l0h;   // i2L0h = 2 / L0h, i2l0h = 2 / l0h
-  double St = txi0 / (taue + XC_EPS);
-  double fr = AT(fReL, j, i), k = AT(ke, j, i), ch = AT(chi, j, i);
-  double sge = Xi * sqrt(jmax(0.0, (fr * k) * itaue));
-  double sgx = Xi * sqrt(jmax(0.0, ((((ch * fr) * k) * itaue) * St) / (1.0 + St * St)));
-  double sgs = Xi * sqrt(jmax(0.0, (ch * AT(ks, j, i)) * itaus));
-  const double ue = itaue + cdt, us = itaus + cdt;   // cdt = 1 / (100 dt)
-  double Fte = exp(((-dt) * ue) / (1.0 + dt * ue)), Fts = exp(((-dt) * us) / (1.0 + dt * us));
-  double ae = sqrt(jmax(0.0, 1.0 - Fte * Fte)), as = sqrt(jmax(0.0, 1.0 - Fts * Fts));
-  double r1 = AT(re, j, i), r2 = AT(rs, j, i);
-  AT(psie, j, i) = Fte * AT(psieo, j, i) + ((ae * sge) * fL) * r1;
-  AT(psix, j, i) = Fte * AT(psixo, j, i) + ((ae * sgx) * fL) * r1;
-  AT(psis, j, i) = Fts * AT(psiso, j, i) + ((as * sgs) * fl) * r2;
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    // The reference's twelve divisions (noise.jl:160-176) folded to five with
+    // the same values up to rounding (these fields carry the 1e-12 tolerance):
+    // 1/tau_e = 2 (V + eps) / L0h and 1/tau_s = 2 (vx + eps) / l0h as
+    // products, and tau' = 1 / (1/tau + c) + dt with c = 1 / (100 dt) entering
+    // only as -dt / tau' = -dt u / (1 + dt u), u = 1/tau + c.  An FP64 division
+    // costs about ten FP64 instructions on this GPU's narrow FP64 pipe.
+    const double ve = AT(V, j, i) + XC_EPS, vs = AT(vx, j, i) + XC_EPS;
+    const double taue = L0h / (2.0 * ve);
+    const double itaue = ve * i2L0h, itaus = vs * i2l0h;   // i2L0h = 2 / L0h, i2l0h = 2 / l0h
+    double St = txi0 / (taue + XC_EPS);
+    double fr = AT(fReL, j, i), k = AT(ke, j, i), ch = AT(chi, j, i);
+    double sge = Xi * sqrt(jmax(0.0, (fr * k) * itaue));
+    double sgx = Xi * sqrt(jmax(0.0, ((((ch * fr) * k) * itaue) * St) / (1.0 + St * St)));
+    double sgs = Xi * sqrt(jmax(0.0, (ch * AT(ks, j, i)) * itaus));
+    const double ue = itaue + cdt, us = itaus + cdt;   // cdt = 1 / (100 dt)
+    double Fte = exp(((-dt) * ue) / (1.0 + dt * ue)), Fts = exp(((-dt) * us) / (1.0 + dt * us));
+    double ae = sqrt(jmax(0.0, 1.0 - Fte * Fte)), as = sqrt(jmax(0.0, 1.0 - Fts * Fts));
+    double r1 = AT(re, j, i), r2 = AT(rs, j, i);
+    AT(psie, j, i) = Fte * AT(psieo, j, i) + ((ae * sge) * fL) * r1;
+    AT(psix, j, i) = Fte * AT(psixo, j, i) + ((ae * sgx) * fL) * r1;
+    AT(psis, j, i) = Fts * AT(psiso, j, i) + ((as * sgs) * fl) * r2;
+  });
 }
 
 // re-standardise to the raw mean/std (noise.jl:261-267); st = {raw mean,
@@ -324,25 +324,25 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
                                CView muw, CView chiu, CView muu, DView xieu, DView xiew,
                                DView xixu, DView xixw, DView xisu, DView xisw) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz + 1 || i > Nx + 1) return;
-  if (i <= Nx) {   // (Nz+2, Nx+1): xieu = xieu_int[icz, :], xixu, xisu
-    int jj = icz_c(j, Nz);
-    AT(xieu, j, i) = corner_avg(pe, jj + 1, i, Nz, Nx) - corner_avg(pe, jj, i, Nz, Nx);
-    double a = AT(chiu, j, i), b = AT(muu, j, i);
-    double tap = (1.0 - exp_tail((-a) / 1e-4)) * (1.0 - exp_tail((-jmax(0.0, b - 0.4)) / 0.05));
-    AT(xixu, j, i) = (-(ext(px, j, i + 1, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
-    AT(xisu, j, i) = (-(ext(ps, j, i + 1, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
-  }
-  if (j <= Nz) {   // (Nz+1, Nx+2): xiew = xiew_int[:, icx], xixw, xisw
-    int ii = icx_p(i, Nx);
-    AT(xiew, j, i) = -(corner_avg(pe, j, ii + 1, Nz, Nx) - corner_avg(pe, j, ii, Nz, Nx));
-    double a = AT(chiw, j, i), b = AT(muw, j, i);
-    double tap = (1.0 - exp_tail((-a) / 1e-4)) * (1.0 - exp_tail((-jmax(0.0, b - 0.4)) / 0.05));
-    AT(xixw, j, i) = (-(ext(px, j + 1, i, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
-    AT(xisw, j, i) = (-(ext(ps, j + 1, i, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
-  }
+  for_tiles(Nz + 2, Nx + 2, [&](int j, int i) {
+    if (j > Nz + 1 || i > Nx + 1) return;
+    if (i <= Nx) {   // (Nz+2, Nx+1): xieu = xieu_int[icz, :], xixu, xisu
+      int jj = icz_c(j, Nz);
+      AT(xieu, j, i) = corner_avg(pe, jj + 1, i, Nz, Nx) - corner_avg(pe, jj, i, Nz, Nx);
+      double a = AT(chiu, j, i), b = AT(muu, j, i);
+      double tap = (1.0 - exp_tail((-a) / 1e-4)) * (1.0 - exp_tail((-jmax(0.0, b - 0.4)) / 0.05));
+      AT(xixu, j, i) = (-(ext(px, j, i + 1, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
+      AT(xisu, j, i) = (-(ext(ps, j, i + 1, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
+    }
+    if (j <= Nz) {   // (Nz+1, Nx+2): xiew = xiew_int[:, icx], xixw, xisw
+      int ii = icx_p(i, Nx);
+      AT(xiew, j, i) = -(corner_avg(pe, j, ii + 1, Nz, Nx) - corner_avg(pe, j, ii, Nz, Nx));
+      double a = AT(chiw, j, i), b = AT(muw, j, i);
+      double tap = (1.0 - exp_tail((-a) / 1e-4)) * (1.0 - exp_tail((-jmax(0.0, b - 0.4)) / 0.05));
+      AT(xixw, j, i) = (-(ext(px, j + 1, i, Nz, Nx) - ext(px, j, i, Nz, Nx))) * tap;
+      AT(xisw, j, i) = (-(ext(ps, j + 1, i, Nz, Nx) - ext(ps, j, i, Nz, Nx))) * tap;
+    }
+  });
 }
 
 // speed magnitudes (noise.jl:223-236)
@@ -403,7 +403,7 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
     if (rs) XC_CUDA_TRY(cudaMemcpyAsync(c->field[FLD_rs], rs, nb, cudaMemcpyHostToDevice, s));
   }
   dim3 blk(32, 8);
-  xc_launch(ou_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, p.Xi, p.L0h, 2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt,
+  xc_launch(ou_kernel, dim3(persistent_grid((const void*)ou_kernel, Nz, Nx)), blk, 0, s, Nz, Nx, p.Xi, p.L0h, 2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt,
       1.0 / (1e2 * dt), np->fL, np->fl, CF(c, FLD_V),
       CF(c, FLD_vx),
       CF(c, FLD_fReL), CF(c, FLD_ke), CF(c, FLD_chi), CF(c, FLD_ks), CF(c, FLD_psieo),
@@ -436,7 +436,7 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
   XC_TRY(reduce_batch(c, devs, 6, s, partials));
   xc_launch(rescale_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, flt[0], flt[1], flt[2], st);
   XC_LAUNCH_CHECK();
-  xc_launch(stagger_kernel, grid2d(Nz + 2, Nx + 2, blk), blk, 0, s, Nz, Nx, CView{flt[0].p, Nz},
+  xc_launch(stagger_kernel, dim3(persistent_grid((const void*)stagger_kernel, Nz + 2, Nx + 2)), blk, 0, s, Nz, Nx, CView{flt[0].p, Nz},
       CView{flt[1].p, Nz}, CView{flt[2].p, Nz}, CF(c, FLD_chiw),
       CF(c, FLD_muw), CF(c, FLD_chiu), CF(c, FLD_muu), F(c, FLD_xieu), F(c, FLD_xiew),
       F(c, FLD_xixu), F(c, FLD_xixw), F(c, FLD_xisu), F(c, FLD_xisw));

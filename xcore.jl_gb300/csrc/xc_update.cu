@@ -37,45 +37,45 @@ __global__ void volfrac_rheology_kernel(int Nz, int Nx, double rhom0, double rho
                                         CView x, CView m, DView rho, DView chi, DView mu,
                                         uint8_t* hasx, uint8_t* hasm, DView etamix) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  double xc = AT(x, j, i), mc = AT(m, j, i);
-  double rh = 1.0 / (mc / rhom0 + xc / rhox0);
-  AT(rho, j, i) = rh;
-  double f1 = clampd((xc * rh) / rhox0, XC_EPS, 1.0 - XC_EPS);
-  double f2 = clampd((mc * rh) / rhom0, XC_EPS, 1.0 - XC_EPS);
-  AT(chi, j, i) = f1;
-  AT(mu, j, i) = f2;
-  size_t o = (size_t)i * Nz + j;
-  hasx[o] = xc >= XC_SQRT_EPS;
-  hasm[o] = mc >= XC_SQRT_EPS;
-  // The powers of update.jl:153-171 as exp(y log x): pow carries its log in
-  // extra precision, which costs about twice the FP64 work; the relative error
-  // of exp(y log x) is |y log x| eps, below 2e-14 for these operands (f >= eps,
-  // 1/C and the fractions Xf of order one), far inside the 1e-12 bound of
-  // these fields.  log(f / B) as log f - log B (log B once on the host) and
-  // the two normalisations as one reciprocal each: two logarithms and two
-  // divisions per cell instead of four and eight, with an absolute error of
-  // the exponent of a few eps |log f|.
-  const double lf1 = log(f1), lf2 = log(f2);
-  double s11 = exp(r.iC11 * (lf1 - r.lB11)), s12 = exp(r.iC12 * (lf2 - r.lB12));
-  double s21 = exp(r.iC21 * (lf1 - r.lB21)), s22 = exp(r.iC22 * (lf2 - r.lB22));
-  const double in1 = 1.0 / (s11 + s12), in2 = 1.0 / (s21 + s22);
-  double Sf11 = s11 * in1, Sf12 = s12 * in1, Sf21 = s21 * in2, Sf22 = s22 * in2;
-  double a1 = r.A11 * Sf11 + r.A12 * Sf12;
-  double a2 = r.A21 * Sf21 + r.A22 * Sf22;
-  double Xf11 = a1 * f1 + (1.0 - a1) * Sf11;
-  double Xf12 = a1 * f2 + (1.0 - a1) * Sf12;
-  double Xf21 = a2 * f1 + (1.0 - a2) * Sf21;
-  double Xf22 = a2 * f2 + (1.0 - a2) * Sf22;
-  // update.jl:170-171 multiply by pow(ex/ex, Xf11) and pow(em/em, Xf22): with
-  // positive finite ex, em those are pow(1, y) = 1 exactly, and x * 1 = x, so
-  // the two FP64 pow calls are left out without changing a bit
-  double thtv1 = exp(Xf12 * r.lmx);
-  double thtv2 = exp(Xf21 * r.lxm);
-  double etaf1 = r.ex * thtv1, etaf2 = r.em * thtv2;
-  AT(etamix, j, i) = f1 * etaf1 + f2 * etaf2;
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    double xc = AT(x, j, i), mc = AT(m, j, i);
+    double rh = 1.0 / (mc / rhom0 + xc / rhox0);
+    AT(rho, j, i) = rh;
+    double f1 = clampd((xc * rh) / rhox0, XC_EPS, 1.0 - XC_EPS);
+    double f2 = clampd((mc * rh) / rhom0, XC_EPS, 1.0 - XC_EPS);
+    AT(chi, j, i) = f1;
+    AT(mu, j, i) = f2;
+    size_t o = (size_t)i * Nz + j;
+    hasx[o] = xc >= XC_SQRT_EPS;
+    hasm[o] = mc >= XC_SQRT_EPS;
+    // The powers of update.jl:153-171 as exp(y log x): pow carries its log in
+    // extra precision, which costs about twice the FP64 work; the relative error
+    // of exp(y log x) is |y log x| eps, below 2e-14 for these operands (f >= eps,
+    // 1/C and the fractions Xf of order one), far inside the 1e-12 bound of
+    // these fields.  log(f / B) as log f - log B (log B once on the host) and
+    // the two normalisations as one reciprocal each: two logarithms and two
+    // divisions per cell instead of four and eight, with an absolute error of
+    // the exponent of a few eps |log f|.
+    const double lf1 = log(f1), lf2 = log(f2);
+    double s11 = exp(r.iC11 * (lf1 - r.lB11)), s12 = exp(r.iC12 * (lf2 - r.lB12));
+    double s21 = exp(r.iC21 * (lf1 - r.lB21)), s22 = exp(r.iC22 * (lf2 - r.lB22));
+    const double in1 = 1.0 / (s11 + s12), in2 = 1.0 / (s21 + s22);
+    double Sf11 = s11 * in1, Sf12 = s12 * in1, Sf21 = s21 * in2, Sf22 = s22 * in2;
+    double a1 = r.A11 * Sf11 + r.A12 * Sf12;
+    double a2 = r.A21 * Sf21 + r.A22 * Sf22;
+    double Xf11 = a1 * f1 + (1.0 - a1) * Sf11;
+    double Xf12 = a1 * f2 + (1.0 - a1) * Sf12;
+    double Xf21 = a2 * f1 + (1.0 - a2) * Sf21;
+    double Xf22 = a2 * f2 + (1.0 - a2) * Sf22;
+    // update.jl:170-171 multiply by pow(ex/ex, Xf11) and pow(em/em, Xf22): with
+    // positive finite ex, em those are pow(1, y) = 1 exactly, and x * 1 = x, so
+    // the two FP64 pow calls are left out without changing a bit
+    double thtv1 = exp(Xf12 * r.lmx);
+    double thtv2 = exp(Xf21 * r.lxm);
+    double etaf1 = r.ex * thtv1, etaf2 = r.em * thtv2;
+    AT(etamix, j, i) = f1 * etaf1 + f2 * etaf2;
+  });
 }
 
 // update_interpolations! (update.jl:73-107) without the row mean; one thread
@@ -205,29 +205,29 @@ __global__ void kinematics_kernel(int Nz, int Nx, double invh, CView W, CView U,
                                   CView wm, DView exz, DView exx, DView ezz, DView Div_V,
                                   DView eII, DView V, DView vx, DView vm) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz || i > Nx) return;
-  AT(exz, j, i) = exz_at(W, U, j, i, invh);
-  if (j >= Nz || i >= Nx) return;
-  double Ux_c = (AT(U, j + 1, i + 1) - AT(U, j + 1, i)) * invh;
-  double Wz_c = (AT(W, j + 1, i + 1) - AT(W, j, i + 1)) * invh;
-  double div = Ux_c + Wz_c;
-  AT(Div_V, j, i) = div;
-  double ex = Ux_c - div / 3.0, ez = Wz_c - div / 3.0;
-  AT(exx, j, i) = ex;
-  AT(ezz, j, i) = ez;
-  double e1 = exz_at(W, U, j, i, invh), e2 = exz_at(W, U, j + 1, i, invh);
-  double e3 = exz_at(W, U, j, i + 1, invh), e4 = exz_at(W, U, j + 1, i + 1, invh);
-  double exz_sq = (((e1 * e1 + e2 * e2) + e3 * e3) + e4 * e4) / 4.0;
-  AT(eII, j, i) = sqrt((XC_EPS + (ex * ex + ez * ez) / 2.0) + exz_sq);
-  double wc = (AT(W, j, i + 1) + AT(W, j + 1, i + 1)) / 2.0;
-  double uc = (AT(U, j + 1, i) + AT(U, j + 1, i + 1)) / 2.0;
-  AT(V, j, i) = sqrt(wc * wc + uc * uc);
-  double t = (AT(wx, j, i + 1) + AT(wx, j + 1, i + 1)) / 2.0;
-  AT(vx, j, i) = sqrt(t * t + XC_EPS);
-  t = (AT(wm, j, i + 1) + AT(wm, j + 1, i + 1)) / 2.0;
-  AT(vm, j, i) = sqrt(t * t + XC_EPS);
+  for_tiles(Nz + 1, Nx + 1, [&](int j, int i) {
+    if (j > Nz || i > Nx) return;
+    AT(exz, j, i) = exz_at(W, U, j, i, invh);
+    if (j >= Nz || i >= Nx) return;
+    double Ux_c = (AT(U, j + 1, i + 1) - AT(U, j + 1, i)) * invh;
+    double Wz_c = (AT(W, j + 1, i + 1) - AT(W, j, i + 1)) * invh;
+    double div = Ux_c + Wz_c;
+    AT(Div_V, j, i) = div;
+    double ex = Ux_c - div / 3.0, ez = Wz_c - div / 3.0;
+    AT(exx, j, i) = ex;
+    AT(ezz, j, i) = ez;
+    double e1 = exz_at(W, U, j, i, invh), e2 = exz_at(W, U, j + 1, i, invh);
+    double e3 = exz_at(W, U, j, i + 1, invh), e4 = exz_at(W, U, j + 1, i + 1, invh);
+    double exz_sq = (((e1 * e1 + e2 * e2) + e3 * e3) + e4 * e4) / 4.0;
+    AT(eII, j, i) = sqrt((XC_EPS + (ex * ex + ez * ez) / 2.0) + exz_sq);
+    double wc = (AT(W, j, i + 1) + AT(W, j + 1, i + 1)) / 2.0;
+    double uc = (AT(U, j + 1, i) + AT(U, j + 1, i + 1)) / 2.0;
+    AT(V, j, i) = sqrt(wc * wc + uc * uc);
+    double t = (AT(wx, j, i + 1) + AT(wx, j + 1, i + 1)) / 2.0;
+    AT(vx, j, i) = sqrt(t * t + XC_EPS);
+    t = (AT(wm, j, i + 1) + AT(wm, j + 1, i + 1)) / 2.0;
+    AT(vm, j, i) = sqrt(t * t + XC_EPS);
+  });
 }
 
 // compute_viscblend_kernel! (update.jl:286-308); etai -> scratch
@@ -259,32 +259,32 @@ __global__ void blend_segvisc_kernel(int Nz, int Nx, const double* min_etai, dou
                                      CView fReL, DView Rel, DView fRel, DView ks, DView etat,
                                      DView etasi, DView kx, DView Rc) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  // The harmonic cap 1 / (1/emax + 1/etai) as emax etai / (emax + etai) and
-  // (v D0) / (en / r) as (v D0) r / en: one FP64 division each instead of
-  // three and two (a division costs about ten FP64 instructions on this GPU;
-  // these fields carry the 1e-12 tolerance)
-  double emax = (*min_etai) * etacntr;
-  const double ei = AT(etai, j, i);
-  double e = (emax * ei) / (emax + ei);
-  double en = 0.5 * e + 0.5 * AT(eta, j, i);
-  AT(eta, j, i) = en;
-  double r = AT(rho, j, i), v = AT(V, j, i);
-  AT(ReD, j, i) = ((v * D0) * r) / en;
-  double vxc = AT(vx, j, i), em = AT(etamix, j, i);
-  double Re = ((vxc * l0) * r) / em;
-  double f = 1.0 - exp(-Re);
-  double k = vxc * l0;
-  double et = (f * k) * r;
-  AT(etasi, j, i) = em + et;
-  AT(Rel, j, i) = Re;
-  AT(fRel, j, i) = f;
-  AT(ks, j, i) = k;
-  AT(etat, j, i) = et;
-  AT(kx, j, i) = k + AT(fReL, j, i) * AT(ke, j, i);
-  AT(Rc, j, i) = v / jmax(vxc, XC_EPS);
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    // The harmonic cap 1 / (1/emax + 1/etai) as emax etai / (emax + etai) and
+    // (v D0) / (en / r) as (v D0) r / en: one FP64 division each instead of
+    // three and two (a division costs about ten FP64 instructions on this GPU;
+    // these fields carry the 1e-12 tolerance)
+    double emax = (*min_etai) * etacntr;
+    const double ei = AT(etai, j, i);
+    double e = (emax * ei) / (emax + ei);
+    double en = 0.5 * e + 0.5 * AT(eta, j, i);
+    AT(eta, j, i) = en;
+    double r = AT(rho, j, i), v = AT(V, j, i);
+    AT(ReD, j, i) = ((v * D0) * r) / en;
+    double vxc = AT(vx, j, i), em = AT(etamix, j, i);
+    double Re = ((vxc * l0) * r) / em;
+    double f = 1.0 - exp(-Re);
+    double k = vxc * l0;
+    double et = (f * k) * r;
+    AT(etasi, j, i) = em + et;
+    AT(Rel, j, i) = Re;
+    AT(fRel, j, i) = f;
+    AT(ks, j, i) = k;
+    AT(etat, j, i) = et;
+    AT(kx, j, i) = k + AT(fReL, j, i) * AT(ke, j, i);
+    AT(Rc, j, i) = v / jmax(vxc, XC_EPS);
+  });
 }
 
 // cap + blend of etas and Red (update.jl:396-402)
@@ -425,7 +425,7 @@ int update_impl(xc_ctx* c) {
          std::log(p.BB[3]),
          1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0,
          std::log(p.etam0 / p.etax0), std::log(p.etax0 / p.etam0)};
-  xc_launch(volfrac_rheology_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x),
+  xc_launch(volfrac_rheology_kernel, dim3(persistent_grid((const void*)volfrac_rheology_kernel, Nz, Nx)), blk, 0, s, Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x),
       CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
       F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix));
   XC_LAUNCH_CHECK();
@@ -454,7 +454,7 @@ int update_impl(xc_ctx* c) {
   XC_LAUNCH_CHECK();
   XC_CUDA_TRY(cudaEventRecord(c->ev_join, side));
   const double invh = 1.0 / p.h;
-  xc_launch(kinematics_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, s, Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U),
+  xc_launch(kinematics_kernel, dim3(persistent_grid((const void*)kinematics_kernel, Nz + 1, Nx + 1)), blk, 0, s, Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U),
       CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
       F(c, FLD_exx), F(c, FLD_ezz), F(c, FLD_Div_V), F(c, FLD_eII), F(c, FLD_V), F(c, FLD_vx),
       F(c, FLD_vm));
@@ -465,7 +465,7 @@ int update_impl(xc_ctx* c) {
       F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL));
   XC_LAUNCH_CHECK();
   XC_TRY(reduce_view(c, RED_MIN, CView{etai.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETA));
-  xc_launch(blend_segvisc_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx,
+  xc_launch(blend_segvisc_kernel, dim3(persistent_grid((const void*)blend_segvisc_kernel, Nz, Nx)), blk, 0, s, Nz, Nx,
       c->dscal + SC_EMAX_ETA, p.etacntr, p.D0, p.l0, CView{etai.p, Nz}, F(c, FLD_eta),
       CF(c, FLD_V), CF(c, FLD_rho), F(c, FLD_ReD), CF(c, FLD_vx), CF(c, FLD_etamix),
       CF(c, FLD_ke), CF(c, FLD_fReL), F(c, FLD_Rel), F(c, FLD_fRel), F(c, FLD_ks),
