@@ -221,7 +221,8 @@ inline dim3 grid2d(int rows, int cols, dim3 blk) {
 template <typename F>
 __device__ __forceinline__ void for_tiles(int rows, int cols, F&& f) {
   const int nbx = (rows + 31) / 32, nt = nbx * ((cols + 7) / 8);
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) f((t % nbx) * 32 + (int)threadIdx.x, (t / nbx) * 8 + (int)threadIdx.y);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x)
+    f((t % nbx) * 32 + (int)threadIdx.x, (t / nbx) * 8 + (int)threadIdx.y);
 }
 // CTAs of such a launch of `kernel` over rows x cols
 unsigned persistent_grid(const void* kernel, int rows, int cols);

@@ -349,18 +349,18 @@ __global__ void stagger_kernel(int Nz, int Nx, CView pe, CView px, CView ps, CVi
 __global__ void speeds_kernel(int Nz, int Nx, CView xisw, CView xisu, CView xixw, CView xixu,
                               CView xiew, CView xieu, DView xis, DView xix, DView xie) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  double wz = (AT(xisw, j, i + 1) + AT(xisw, j + 1, i + 1)) / 2.0;
-  double wx = (AT(xisu, j + 1, i) + AT(xisu, j + 1, i + 1)) / 2.0;
-  AT(xis, j, i) = sqrt(wz * wz + wx * wx);
-  wz = (AT(xixw, j, i + 1) + AT(xixw, j + 1, i + 1)) / 2.0;
-  wx = (AT(xixu, j + 1, i) + AT(xixu, j + 1, i + 1)) / 2.0;
-  AT(xix, j, i) = sqrt(wz * wz + wx * wx);
-  wz = (AT(xiew, j, i + 1) + AT(xiew, j + 1, i + 1)) / 2.0;
-  wx = (AT(xieu, j + 1, i) + AT(xieu, j + 1, i + 1)) / 2.0;
-  AT(xie, j, i) = sqrt(wz * wz + wx * wx);
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    double wz = (AT(xisw, j, i + 1) + AT(xisw, j + 1, i + 1)) / 2.0;
+    double wx = (AT(xisu, j + 1, i) + AT(xisu, j + 1, i + 1)) / 2.0;
+    AT(xis, j, i) = sqrt(wz * wz + wx * wx);
+    wz = (AT(xixw, j, i + 1) + AT(xixw, j + 1, i + 1)) / 2.0;
+    wx = (AT(xixu, j + 1, i) + AT(xixu, j + 1, i + 1)) / 2.0;
+    AT(xix, j, i) = sqrt(wz * wz + wx * wx);
+    wz = (AT(xiew, j, i + 1) + AT(xiew, j + 1, i + 1)) / 2.0;
+    wx = (AT(xieu, j + 1, i) + AT(xieu, j + 1, i + 1)) / 2.0;
+    AT(xie, j, i) = sqrt(wz * wz + wx * wx);
+  });
 }
 
 }  // namespace
@@ -403,7 +403,8 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
     if (rs) XC_CUDA_TRY(cudaMemcpyAsync(c->field[FLD_rs], rs, nb, cudaMemcpyHostToDevice, s));
   }
   dim3 blk(32, 8);
-  xc_launch(ou_kernel, dim3(persistent_grid((const void*)ou_kernel, Nz, Nx)), blk, 0, s, Nz, Nx, p.Xi, p.L0h, 2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt,
+  xc_launch(ou_kernel, dim3(persistent_grid((const void*)ou_kernel, Nz, Nx)), blk, 0, s, Nz, Nx, p.Xi, p.L0h,
+      2.0 / p.L0h, 2.0 / p.l0h, p.txi0, dt,
       1.0 / (1e2 * dt), np->fL, np->fl, CF(c, FLD_V),
       CF(c, FLD_vx),
       CF(c, FLD_fReL), CF(c, FLD_ke), CF(c, FLD_chi), CF(c, FLD_ks), CF(c, FLD_psieo),
@@ -436,12 +437,14 @@ int noise_impl(xc_ctx* c, double dt, int first_iter, const double* re, const dou
   XC_TRY(reduce_batch(c, devs, 6, s, partials));
   xc_launch(rescale_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, flt[0], flt[1], flt[2], st);
   XC_LAUNCH_CHECK();
-  xc_launch(stagger_kernel, dim3(persistent_grid((const void*)stagger_kernel, Nz + 2, Nx + 2)), blk, 0, s, Nz, Nx, CView{flt[0].p, Nz},
+  xc_launch(stagger_kernel, dim3(persistent_grid((const void*)stagger_kernel, Nz + 2, Nx + 2)), blk, 0, s, Nz, Nx,
+      CView{flt[0].p, Nz},
       CView{flt[1].p, Nz}, CView{flt[2].p, Nz}, CF(c, FLD_chiw),
       CF(c, FLD_muw), CF(c, FLD_chiu), CF(c, FLD_muu), F(c, FLD_xieu), F(c, FLD_xiew),
       F(c, FLD_xixu), F(c, FLD_xixw), F(c, FLD_xisu), F(c, FLD_xisw));
   XC_LAUNCH_CHECK();
-  xc_launch(speeds_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, CF(c, FLD_xisw), CF(c, FLD_xisu),
+  xc_launch(speeds_kernel, dim3(persistent_grid((const void*)speeds_kernel, Nz, Nx)), blk, 0, s, Nz, Nx,
+      CF(c, FLD_xisw), CF(c, FLD_xisu),
       CF(c, FLD_xixw), CF(c, FLD_xixu), CF(c, FLD_xiew),
       CF(c, FLD_xieu), F(c, FLD_xis), F(c, FLD_xix), F(c, FLD_xie));
   XC_LAUNCH_CHECK();

@@ -379,28 +379,28 @@ __global__ void phsevo_tail_kernel(int Nz, int Nx, double a1, double a2, double 
                                    CView dffn_X, CView bndshape, DView Gx, DView dXdt,
                                    CView dXdto, CView dXdtoo) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  double aX = AT(advn_X, j, i);
-  AT(advn_rho, j, i) = aX + AT(advn_M, j, i);
-  double gx = (G0 * (1.0 - AT(x, j, i))) * AT(bndshape, j, i);
-  AT(Gx, j, i) = gx;
-  double dxdt = (-aX + AT(dffn_X, j, i)) + gx;
-  AT(dXdt, j, i) = dxdt;
-  double Xc = AT(X, j, i);
-  double res = ((a1 * Xc - a2 * AT(Xo, j, i)) - a3 * AT(Xoo, j, i)) -
-               (((b1 * dxdt + b2 * AT(dXdto, j, i)) + b3 * AT(dXdtoo, j, i)) * dt);
-  double upd = ((-alpha) * res) / a1;
-  double Xn = Xc + upd;
-  double r = AT(rho, j, i);
-  double lo = r * XC_EPS, hi = r * (1.0 - XC_EPS);
-  Xn = Xn > hi ? hi : (Xn < lo ? lo : Xn);
-  AT(X, j, i) = Xn;
-  double Mn = r - Xn;
-  AT(M, j, i) = Mn;
-  AT(x, j, i) = Xn / r;
-  AT(m, j, i) = Mn / r;
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    double aX = AT(advn_X, j, i);
+    AT(advn_rho, j, i) = aX + AT(advn_M, j, i);
+    double gx = (G0 * (1.0 - AT(x, j, i))) * AT(bndshape, j, i);
+    AT(Gx, j, i) = gx;
+    double dxdt = (-aX + AT(dffn_X, j, i)) + gx;
+    AT(dXdt, j, i) = dxdt;
+    double Xc = AT(X, j, i);
+    double res = ((a1 * Xc - a2 * AT(Xo, j, i)) - a3 * AT(Xoo, j, i)) -
+                 (((b1 * dxdt + b2 * AT(dXdto, j, i)) + b3 * AT(dXdtoo, j, i)) * dt);
+    double upd = ((-alpha) * res) / a1;
+    double Xn = Xc + upd;
+    double r = AT(rho, j, i);
+    double lo = r * XC_EPS, hi = r * (1.0 - XC_EPS);
+    Xn = Xn > hi ? hi : (Xn < lo ? lo : Xn);
+    AT(X, j, i) = Xn;
+    double Mn = r - Xn;
+    AT(M, j, i) = Mn;
+    AT(x, j, i) = Xn / r;
+    AT(m, j, i) = Mn / r;
+  });
 }
 
 template <int S>
@@ -502,7 +502,8 @@ int phsevo_impl(xc_ctx* c, int scheme, const double coefs[6], double dt, double 
   XC_TRY(pad_face_fluxes(F(c, FLD_qx_advn_M), F(c, FLD_qz_advn_M), Nz, Nx, xBC, zBC, s));
   XC_TRY(pad_face_fluxes(F(c, FLD_qx_dffn_X), F(c, FLD_qz_dffn_X), Nz, Nx, xBC, zBC, s));
   dim3 blk(32, 8);
-  xc_launch(phsevo_tail_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, coefs[0], coefs[1], coefs[2], coefs[3],
+  xc_launch(phsevo_tail_kernel, dim3(persistent_grid((const void*)phsevo_tail_kernel, Nz, Nx)), blk, 0, s, Nz, Nx,
+      coefs[0], coefs[1], coefs[2], coefs[3],
       coefs[4], coefs[5], dt, alpha, c->p.G0,
       X, CF(c, FLD_Xo), CF(c, FLD_Xoo), M, F(c, FLD_x), F(c, FLD_m), CF(c, FLD_rho),
       CF(c, FLD_advn_X), CF(c, FLD_advn_M), F(c, FLD_advn_rho), CF(c, FLD_dffn_X),

@@ -86,34 +86,34 @@ __global__ void interp_kernel(int Nz, int Nx, int xBC, int zBC, double rhom0, do
                               DView chiu, DView muu, DView x_w, DView m_w, DView x_u,
                               DView m_u) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz + 1 || i > Nx + 1) return;
-  if (j <= Nz && i < Nx) {   // (Nz+1, Nx)
-    int a = icz_at(j, Nz, zBC), b = icz_at(j + 1, Nz, zBC);
-    double rw = (AT(rho, a, i) + AT(rho, b, i)) / 2.0;
-    AT(rhow, j, i) = rw;
-    AT(Drhom, j, i) = rhom0 - rw;
-    AT(Drhox, j, i) = rhox0 - rw;
-    AT(x_w, j, i) = (AT(x, a, i) + AT(x, b, i)) / 2.0;
-    AT(m_w, j, i) = (AT(m, a, i) + AT(m, b, i)) / 2.0;
-  }
-  if (j < Nz && i <= Nx) {   // (Nz, Nx+1)
-    int a = icx_at(i, Nx, xBC), b = icx_at(i + 1, Nx, xBC);
-    AT(rhou, j, i) = (AT(rho, j, a) + AT(rho, j, b)) / 2.0;
-    AT(x_u, j, i) = (AT(x, j, a) + AT(x, j, b)) / 2.0;
-    AT(m_u, j, i) = (AT(m, j, a) + AT(m, j, b)) / 2.0;
-  }
-  if (j <= Nz) {             // (Nz+1, Nx+2)
-    int a = icz_at(j, Nz, zBC), b = icz_at(j + 1, Nz, zBC), ci = icx_at(i, Nx, xBC);
-    AT(chiw, j, i) = (AT(chi, a, ci) + AT(chi, b, ci)) / 2.0;
-    AT(muw, j, i) = (AT(mu, a, ci) + AT(mu, b, ci)) / 2.0;
-  }
-  if (i <= Nx) {             // (Nz+2, Nx+1)
-    int cj = icz_at(j, Nz, zBC), a = icx_at(i, Nx, xBC), b = icx_at(i + 1, Nx, xBC);
-    AT(chiu, j, i) = (AT(chi, cj, a) + AT(chi, cj, b)) / 2.0;
-    AT(muu, j, i) = (AT(mu, cj, a) + AT(mu, cj, b)) / 2.0;
-  }
+  for_tiles(Nz + 2, Nx + 2, [&](int j, int i) {
+    if (j > Nz + 1 || i > Nx + 1) return;
+    if (j <= Nz && i < Nx) {   // (Nz+1, Nx)
+      int a = icz_at(j, Nz, zBC), b = icz_at(j + 1, Nz, zBC);
+      double rw = (AT(rho, a, i) + AT(rho, b, i)) / 2.0;
+      AT(rhow, j, i) = rw;
+      AT(Drhom, j, i) = rhom0 - rw;
+      AT(Drhox, j, i) = rhox0 - rw;
+      AT(x_w, j, i) = (AT(x, a, i) + AT(x, b, i)) / 2.0;
+      AT(m_w, j, i) = (AT(m, a, i) + AT(m, b, i)) / 2.0;
+    }
+    if (j < Nz && i <= Nx) {   // (Nz, Nx+1)
+      int a = icx_at(i, Nx, xBC), b = icx_at(i + 1, Nx, xBC);
+      AT(rhou, j, i) = (AT(rho, j, a) + AT(rho, j, b)) / 2.0;
+      AT(x_u, j, i) = (AT(x, j, a) + AT(x, j, b)) / 2.0;
+      AT(m_u, j, i) = (AT(m, j, a) + AT(m, j, b)) / 2.0;
+    }
+    if (j <= Nz) {             // (Nz+1, Nx+2)
+      int a = icz_at(j, Nz, zBC), b = icz_at(j + 1, Nz, zBC), ci = icx_at(i, Nx, xBC);
+      AT(chiw, j, i) = (AT(chi, a, ci) + AT(chi, b, ci)) / 2.0;
+      AT(muw, j, i) = (AT(mu, a, ci) + AT(mu, b, ci)) / 2.0;
+    }
+    if (i <= Nx) {             // (Nz+2, Nx+1)
+      int cj = icz_at(j, Nz, zBC), a = icx_at(i, Nx, xBC), b = icx_at(i + 1, Nx, xBC);
+      AT(chiu, j, i) = (AT(chi, cj, a) + AT(chi, cj, b)) / 2.0;
+      AT(muu, j, i) = (AT(mu, cj, a) + AT(mu, cj, b)) / 2.0;
+    }
+  });
 }
 
 // mean(rhow, dims=2) (sequential over columns, as Julia reduces a
@@ -183,15 +183,15 @@ __global__ void drho_pressure_kernel(int Nz, int Nx, double Ptop, const double* 
                                      const double* plcol, CView rhow, DView Drho, CView P,
                                      DView Pl, DView Pt) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz || i >= Nx) return;
-  AT(Drho, j, i) = AT(rhow, j, i) - rhoref[j];
-  if (j < Nz) {
-    double pl = plcol[j];
-    AT(Pl, j, i) = pl;
-    AT(Pt, j, i) = jmax(Ptop / 100.0, pl + AT(P, j + 1, i + 1));
-  }
+  for_tiles(Nz + 1, Nx, [&](int j, int i) {
+    if (j > Nz || i >= Nx) return;
+    AT(Drho, j, i) = AT(rhow, j, i) - rhoref[j];
+    if (j < Nz) {
+      double pl = plcol[j];
+      AT(Pl, j, i) = pl;
+      AT(Pt, j, i) = jmax(Ptop / 100.0, pl + AT(P, j + 1, i + 1));
+    }
+  });
 }
 
 __device__ __forceinline__ double exz_at(CView W, CView U, int j, int i, double invh) {
@@ -235,20 +235,20 @@ __global__ void viscblend_kernel(int Nz, int Nx, double L0, CView etamix, CView 
                                  CView V, DView etai, DView etae, DView ke, DView kx, DView ReL,
                                  DView fReL) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  double r = AT(rho, j, i), em = AT(etamix, j, i);
-  double k = (AT(eII, j, i) * L0) * L0;
-  double Re = ((AT(V, j, i) * L0) * r) / em;   // (V L0) / (em / r) with one division (1e-12 fields)
-  double f = 1.0 - exp(-Re);
-  double ee = (f * k) * r;
-  AT(etai, j, i) = em + ee;
-  AT(etae, j, i) = ee;
-  AT(ke, j, i) = k;
-  AT(kx, j, i) = k;
-  AT(ReL, j, i) = Re;
-  AT(fReL, j, i) = f;
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    double r = AT(rho, j, i), em = AT(etamix, j, i);
+    double k = (AT(eII, j, i) * L0) * L0;
+    double Re = ((AT(V, j, i) * L0) * r) / em;   // (V L0) / (em / r) with one division (1e-12 fields)
+    double f = 1.0 - exp(-Re);
+    double ee = (f * k) * r;
+    AT(etai, j, i) = em + ee;
+    AT(etae, j, i) = ee;
+    AT(ke, j, i) = k;
+    AT(kx, j, i) = k;
+    AT(ReL, j, i) = Re;
+    AT(fReL, j, i) = f;
+  });
 }
 
 // contrast cap + Picard blend of eta (update.jl:331-337) fused with
@@ -292,16 +292,16 @@ __global__ void etas_blend_kernel(int Nz, int Nx, const double* min_etasi, doubl
                                   double d0, CView etasi, DView etas, CView vx, CView rho,
                                   DView Red) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j >= Nz || i >= Nx) return;
-  // one division each, as in blend_segvisc_kernel
-  double emax = (*min_etasi) * etacntr;
-  const double ei = AT(etasi, j, i);
-  double e = (emax * ei) / (emax + ei);
-  double en = 0.5 * e + 0.5 * AT(etas, j, i);
-  AT(etas, j, i) = en;
-  AT(Red, j, i) = ((AT(vx, j, i) * d0) * AT(rho, j, i)) / en;
+  for_tiles(Nz, Nx, [&](int j, int i) {
+    if (j >= Nz || i >= Nx) return;
+    // one division each, as in blend_segvisc_kernel
+    double emax = (*min_etasi) * etacntr;
+    const double ei = AT(etasi, j, i);
+    double e = (emax * ei) / (emax + ei);
+    double en = 0.5 * e + 0.5 * AT(etas, j, i);
+    AT(etas, j, i) = en;
+    AT(Red, j, i) = ((AT(vx, j, i) * d0) * AT(rho, j, i)) / en;
+  });
 }
 
 // compute_corner_eta! (update.jl:411-426, always periodic x / closed z as
@@ -309,19 +309,19 @@ __global__ void etas_blend_kernel(int Nz, int Nx, const double* min_etasi, doubl
 __global__ void corner_eta_etasw_kernel(int Nz, int Nx, int zBC, CView eta, DView etaco,
                                         CView etas, DView etasw) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz || i > Nx) return;
-  int a = icz_at(j, Nz, XC_CLOSED), b = icz_at(j + 1, Nz, XC_CLOSED);
-  int c = icx_at(i, Nx, XC_PERIODIC), d = icx_at(i + 1, Nx, XC_PERIODIC);
-  double e00 = AT(eta, a, c), e10 = AT(eta, b, c), e01 = AT(eta, a, d), e11 = AT(eta, b, d);
-  // the fourth root as two correctly rounded square roots: within one ulp,
-  // as pow is, at a fraction of pow's FP64 work
-  AT(etaco, j, i) = sqrt(sqrt(((e00 * e10) * e01) * e11));
-  if (i < Nx) {
-    int p = icz_at(j, Nz, zBC), q = icz_at(j + 1, Nz, zBC);
-    AT(etasw, j, i) = sqrt(AT(etas, p, i) * AT(etas, q, i));
-  }
+  for_tiles(Nz + 1, Nx + 1, [&](int j, int i) {
+    if (j > Nz || i > Nx) return;
+    int a = icz_at(j, Nz, XC_CLOSED), b = icz_at(j + 1, Nz, XC_CLOSED);
+    int c = icx_at(i, Nx, XC_PERIODIC), d = icx_at(i + 1, Nx, XC_PERIODIC);
+    double e00 = AT(eta, a, c), e10 = AT(eta, b, c), e01 = AT(eta, a, d), e11 = AT(eta, b, d);
+    // the fourth root as two correctly rounded square roots: within one ulp,
+    // as pow is, at a fraction of pow's FP64 work
+    AT(etaco, j, i) = sqrt(sqrt(((e00 * e10) * e01) * e11));
+    if (i < Nx) {
+      int p = icz_at(j, Nz, zBC), q = icz_at(j + 1, Nz, zBC);
+      AT(etasw, j, i) = sqrt(AT(etas, p, i) * AT(etas, q, i));
+    }
+  });
 }
 
 // update_stresses! (update.jl:432-476)
@@ -329,21 +329,21 @@ __global__ void stress_kernel(int Nz, int Nx, double D0, CView etaco, CView exz,
                               CView eta, CView exx, CView ezz, DView txx, DView tzz, DView tII,
                               CView V, CView kx, DView Ra) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz || i > Nx) return;
-  AT(txz, j, i) = AT(etaco, j, i) * AT(exz, j, i);
-  if (j >= Nz || i >= Nx) return;
-  double e = AT(eta, j, i);
-  double tx = e * AT(exx, j, i), tz = e * AT(ezz, j, i);
-  AT(txx, j, i) = tx;
-  AT(tzz, j, i) = tz;
-  double t1 = AT(etaco, j, i) * AT(exz, j, i), t2 = AT(etaco, j + 1, i) * AT(exz, j + 1, i);
-  double t3 = AT(etaco, j, i + 1) * AT(exz, j, i + 1);
-  double t4 = AT(etaco, j + 1, i + 1) * AT(exz, j + 1, i + 1);
-  double txz_sq = (((t1 * t1 + t2 * t2) + t3 * t3) + t4 * t4) / 4.0;
-  AT(tII, j, i) = sqrt((XC_EPS + (tx * tx + tz * tz) / 2.0) + txz_sq);
-  AT(Ra, j, i) = (AT(V, j, i) * D0) / AT(kx, j, i);
+  for_tiles(Nz + 1, Nx + 1, [&](int j, int i) {
+    if (j > Nz || i > Nx) return;
+    AT(txz, j, i) = AT(etaco, j, i) * AT(exz, j, i);
+    if (j >= Nz || i >= Nx) return;
+    double e = AT(eta, j, i);
+    double tx = e * AT(exx, j, i), tz = e * AT(ezz, j, i);
+    AT(txx, j, i) = tx;
+    AT(tzz, j, i) = tz;
+    double t1 = AT(etaco, j, i) * AT(exz, j, i), t2 = AT(etaco, j + 1, i) * AT(exz, j + 1, i);
+    double t3 = AT(etaco, j, i + 1) * AT(exz, j, i + 1);
+    double t4 = AT(etaco, j + 1, i + 1) * AT(exz, j + 1, i + 1);
+    double txz_sq = (((t1 * t1 + t2 * t2) + t3 * t3) + t4 * t4) / 4.0;
+    AT(tII, j, i) = sqrt((XC_EPS + (tx * tx + tz * tz) / 2.0) + txz_sq);
+    AT(Ra, j, i) = (AT(V, j, i) * D0) / AT(kx, j, i);
+  });
 }
 
 // update_segregation_speed! + update_phase_velocities! (store.jl:47-105),
@@ -355,33 +355,33 @@ __global__ void phase_velocities_kernel(int Nz, int Nx, int xBC, int zBC, double
                                         CView xixu, CView xieu, DView wx, DView wm, DView Wx,
                                         DView Wm, DView Ux, DView Um) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz + 1 || i > Nx + 1) return;
-  if (j <= Nz) {   // W-shaped (Nz+1, Nx+2)
-    // the ghost columns copy the tapered interior columns periodically
-    // (store.jl:272-273 applies the copy for every xBC)
-    int is = (i == 0) ? Nx : (i == Nx + 1 ? 1 : i);
-    double w = (((d0 * d0) / AT(etasw, j, is - 1)) * AT(Drhox, j, is - 1)) * g0;
-    w = w * AT(bndtaperw, j, is);
-    AT(wx, j, i) = w;
-    int ci = icx_at(i, Nx, xBC);
-    double xe = AT(x_w, j, ci), me = jmax(AT(m_w, j, ci), XC_EPS);
-    double wmv = ((-xe) / me) * w;
-    AT(wm, j, i) = wmv;
-    double sx = AT(xisw, j, i) + AT(xixw, j, i);
-    double Wv = AT(W, j, i), xe_w = AT(xiew, j, i);
-    AT(Wx, j, i) = ((Wv + w) + sx) + xe_w;
-    AT(Wm, j, i) = ((Wv + wmv) - ((xe / me) * sx)) + xe_w;
-  }
-  if (i <= Nx) {   // U-shaped (Nz+2, Nx+1)
-    int cj = icz_at(j, Nz, zBC);
-    double xe = AT(x_u, cj, i), me = jmax(AT(m_u, cj, i), XC_EPS);
-    double sx = AT(xisu, j, i) + AT(xixu, j, i);
-    double Uv = AT(U, j, i), xe_u = AT(xieu, j, i);
-    AT(Ux, j, i) = (Uv + sx) + xe_u;
-    AT(Um, j, i) = (Uv + (((-xe) / me) * sx)) + xe_u;
-  }
+  for_tiles(Nz + 2, Nx + 2, [&](int j, int i) {
+    if (j > Nz + 1 || i > Nx + 1) return;
+    if (j <= Nz) {   // W-shaped (Nz+1, Nx+2)
+      // the ghost columns copy the tapered interior columns periodically
+      // (store.jl:272-273 applies the copy for every xBC)
+      int is = (i == 0) ? Nx : (i == Nx + 1 ? 1 : i);
+      double w = (((d0 * d0) / AT(etasw, j, is - 1)) * AT(Drhox, j, is - 1)) * g0;
+      w = w * AT(bndtaperw, j, is);
+      AT(wx, j, i) = w;
+      int ci = icx_at(i, Nx, xBC);
+      double xe = AT(x_w, j, ci), me = jmax(AT(m_w, j, ci), XC_EPS);
+      double wmv = ((-xe) / me) * w;
+      AT(wm, j, i) = wmv;
+      double sx = AT(xisw, j, i) + AT(xixw, j, i);
+      double Wv = AT(W, j, i), xe_w = AT(xiew, j, i);
+      AT(Wx, j, i) = ((Wv + w) + sx) + xe_w;
+      AT(Wm, j, i) = ((Wv + wmv) - ((xe / me) * sx)) + xe_w;
+    }
+    if (i <= Nx) {   // U-shaped (Nz+2, Nx+1)
+      int cj = icz_at(j, Nz, zBC);
+      double xe = AT(x_u, cj, i), me = jmax(AT(m_u, cj, i), XC_EPS);
+      double sx = AT(xisu, j, i) + AT(xixu, j, i);
+      double Uv = AT(U, j, i), xe_u = AT(xieu, j, i);
+      AT(Ux, j, i) = (Uv + sx) + xe_u;
+      AT(Um, j, i) = (Uv + (((-xe) / me) * sx)) + xe_u;
+    }
+  });
 }
 
 // store_previous! (store.jl:13-30)
@@ -392,24 +392,24 @@ __global__ void store_previous_kernel(int Nz, int Nx, DView X, DView Xo, DView X
                                       DView rhoWo, DView rhoWoo, CView rhou, CView U,
                                       DView rhoUo, DView rhoUoo) {
   XC_PDL_WAIT();
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j > Nz || i > Nx) return;
-  if (j < Nz && i < Nx) {
-    AT(Xoo, j, i) = AT(Xo, j, i); AT(Xo, j, i) = AT(X, j, i);
-    AT(Moo, j, i) = AT(Mo, j, i); AT(Mo, j, i) = AT(M, j, i);
-    AT(dXdtoo, j, i) = AT(dXdto, j, i); AT(dXdto, j, i) = AT(dXdt, j, i);
-    AT(rhooo, j, i) = AT(rhoo, j, i); AT(rhoo, j, i) = AT(rho, j, i);
-    AT(drhodtoo, j, i) = AT(drhodto, j, i); AT(drhodto, j, i) = AT(drhodt, j, i);
-  }
-  if (i < Nx) {    // (Nz+1, Nx)
-    AT(rhoWoo, j, i) = AT(rhoWo, j, i);
-    AT(rhoWo, j, i) = AT(rhow, j, i) * AT(W, j, i + 1);
-  }
-  if (j < Nz) {    // (Nz, Nx+1)
-    AT(rhoUoo, j, i) = AT(rhoUo, j, i);
-    AT(rhoUo, j, i) = AT(rhou, j, i) * AT(U, j + 1, i);
-  }
+  for_tiles(Nz + 1, Nx + 1, [&](int j, int i) {
+    if (j > Nz || i > Nx) return;
+    if (j < Nz && i < Nx) {
+      AT(Xoo, j, i) = AT(Xo, j, i); AT(Xo, j, i) = AT(X, j, i);
+      AT(Moo, j, i) = AT(Mo, j, i); AT(Mo, j, i) = AT(M, j, i);
+      AT(dXdtoo, j, i) = AT(dXdto, j, i); AT(dXdto, j, i) = AT(dXdt, j, i);
+      AT(rhooo, j, i) = AT(rhoo, j, i); AT(rhoo, j, i) = AT(rho, j, i);
+      AT(drhodtoo, j, i) = AT(drhodto, j, i); AT(drhodto, j, i) = AT(drhodt, j, i);
+    }
+    if (i < Nx) {    // (Nz+1, Nx)
+      AT(rhoWoo, j, i) = AT(rhoWo, j, i);
+      AT(rhoWo, j, i) = AT(rhow, j, i) * AT(W, j, i + 1);
+    }
+    if (j < Nz) {    // (Nz, Nx+1)
+      AT(rhoUoo, j, i) = AT(rhoUo, j, i);
+      AT(rhoUo, j, i) = AT(rhou, j, i) * AT(U, j + 1, i);
+    }
+  });
 }
 
 }  // namespace
@@ -425,11 +425,13 @@ int update_impl(xc_ctx* c) {
          std::log(p.BB[3]),
          1.0 / p.CC[0], 1.0 / p.CC[1], 1.0 / p.CC[2], 1.0 / p.CC[3], p.etax0, p.etam0,
          std::log(p.etam0 / p.etax0), std::log(p.etax0 / p.etam0)};
-  xc_launch(volfrac_rheology_kernel, dim3(persistent_grid((const void*)volfrac_rheology_kernel, Nz, Nx)), blk, 0, s, Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x),
+  xc_launch(volfrac_rheology_kernel, dim3(persistent_grid((const void*)volfrac_rheology_kernel, Nz, Nx)), blk, 0, s,
+      Nz, Nx, p.rhom0, p.rhox0, r, CF(c, FLD_x),
       CF(c, FLD_m), F(c, FLD_rho), F(c, FLD_chi),
       F(c, FLD_mu), (uint8_t*)c->field[FLD_hasx], (uint8_t*)c->field[FLD_hasm], F(c, FLD_etamix));
   XC_LAUNCH_CHECK();
-  xc_launch(interp_kernel, grid2d(Nz + 2, Nx + 2, blk), blk, 0, s, Nz, Nx, p.xBC, p.zBC, p.rhom0, p.rhox0,
+  xc_launch(interp_kernel, dim3(persistent_grid((const void*)interp_kernel, Nz + 2, Nx + 2)), blk, 0, s, Nz, Nx,
+      p.xBC, p.zBC, p.rhom0, p.rhox0,
       CF(c, FLD_rho), CF(c, FLD_chi), CF(c, FLD_mu),
       CF(c, FLD_x), CF(c, FLD_m), F(c, FLD_rhow), F(c, FLD_rhou), F(c, FLD_Drhom),
       F(c, FLD_Drhox), F(c, FLD_chiw), F(c, FLD_muw), F(c, FLD_chiu), F(c, FLD_muu),
@@ -448,19 +450,22 @@ int update_impl(xc_ctx* c) {
   xc_launch(rowmean_kernel, (Nz + 1 + 31) / 32, 256, 0, side, Nz, Nx, CF(c, FLD_rhow), rhoref);
   xc_launch(pressure_scan_kernel, 1, 256, 0, side, Nz, p.g0, p.h, p.Ptop, rhoref, plcol);
   XC_LAUNCH_CHECK();
-  xc_launch(drho_pressure_kernel, grid2d(Nz + 1, Nx, blk), blk, 0, side, Nz, Nx, p.Ptop, rhoref, plcol,
+  xc_launch(drho_pressure_kernel, dim3(persistent_grid((const void*)drho_pressure_kernel, Nz + 1, Nx)), blk, 0,
+      side, Nz, Nx, p.Ptop, rhoref, plcol,
       CF(c, FLD_rhow), F(c, FLD_Drho), CF(c, FLD_P), F(c, FLD_Pl),
       F(c, FLD_Pt));
   XC_LAUNCH_CHECK();
   XC_CUDA_TRY(cudaEventRecord(c->ev_join, side));
   const double invh = 1.0 / p.h;
-  xc_launch(kinematics_kernel, dim3(persistent_grid((const void*)kinematics_kernel, Nz + 1, Nx + 1)), blk, 0, s, Nz, Nx, invh, CF(c, FLD_W), CF(c, FLD_U),
+  xc_launch(kinematics_kernel, dim3(persistent_grid((const void*)kinematics_kernel, Nz + 1, Nx + 1)), blk, 0, s, Nz,
+      Nx, invh, CF(c, FLD_W), CF(c, FLD_U),
       CF(c, FLD_wx), CF(c, FLD_wm), F(c, FLD_exz),
       F(c, FLD_exx), F(c, FLD_ezz), F(c, FLD_Div_V), F(c, FLD_eII), F(c, FLD_V), F(c, FLD_vx),
       F(c, FLD_vm));
   XC_LAUNCH_CHECK();
   DView etai{c->tmp[0], Nz}, etasi{c->tmp[1], Nz};
-  xc_launch(viscblend_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx, p.L0, CF(c, FLD_etamix), CF(c, FLD_eII),
+  xc_launch(viscblend_kernel, dim3(persistent_grid((const void*)viscblend_kernel, Nz, Nx)), blk, 0, s, Nz, Nx, p.L0,
+      CF(c, FLD_etamix), CF(c, FLD_eII),
       CF(c, FLD_rho), CF(c, FLD_V), etai,
       F(c, FLD_etae), F(c, FLD_ke), F(c, FLD_kx), F(c, FLD_ReL), F(c, FLD_fReL));
   XC_LAUNCH_CHECK();
@@ -472,14 +477,16 @@ int update_impl(xc_ctx* c) {
       F(c, FLD_etat), etasi, F(c, FLD_kx), F(c, FLD_Rc));
   XC_LAUNCH_CHECK();
   XC_TRY(reduce_view(c, RED_MIN, CView{etasi.p, Nz}, CView{nullptr, 0}, Nz, Nx, SC_EMAX_ETAS));
-  xc_launch(etas_blend_kernel, grid2d(Nz, Nx, blk), blk, 0, s, Nz, Nx,
+  xc_launch(etas_blend_kernel, dim3(persistent_grid((const void*)etas_blend_kernel, Nz, Nx)), blk, 0, s, Nz, Nx,
       c->dscal + SC_EMAX_ETAS, p.etacntr, p.d0, CView{etasi.p, Nz}, F(c, FLD_etas),
       CF(c, FLD_vx), CF(c, FLD_rho), F(c, FLD_Red));
   XC_LAUNCH_CHECK();
-  xc_launch(corner_eta_etasw_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, s, Nz, Nx, p.zBC, CF(c, FLD_eta),
+  xc_launch(corner_eta_etasw_kernel, dim3(persistent_grid((const void*)corner_eta_etasw_kernel, Nz + 1, Nx + 1)),
+      blk, 0, s, Nz, Nx, p.zBC, CF(c, FLD_eta),
       F(c, FLD_etaco), CF(c, FLD_etas), F(c, FLD_etasw));
   XC_LAUNCH_CHECK();
-  xc_launch(stress_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, s, Nz, Nx, p.D0, CF(c, FLD_etaco), CF(c, FLD_exz),
+  xc_launch(stress_kernel, dim3(persistent_grid((const void*)stress_kernel, Nz + 1, Nx + 1)), blk, 0, s, Nz, Nx,
+      p.D0, CF(c, FLD_etaco), CF(c, FLD_exz),
       F(c, FLD_txz), CF(c, FLD_eta),
       CF(c, FLD_exx), CF(c, FLD_ezz), F(c, FLD_txx), F(c, FLD_tzz), F(c, FLD_tII), CF(c, FLD_V),
       CF(c, FLD_kx), F(c, FLD_Ra));
@@ -491,7 +498,8 @@ int update_impl(xc_ctx* c) {
 int phase_velocities_impl(xc_ctx* c) {
   const int Nz = c->Nz, Nx = c->Nx;
   dim3 blk(32, 8);
-  xc_launch(phase_velocities_kernel, grid2d(Nz + 2, Nx + 2, blk), blk, 0,
+  xc_launch(phase_velocities_kernel, dim3(persistent_grid((const void*)phase_velocities_kernel, Nz + 2, Nx + 2)),
+      blk, 0,
       c->stream, Nz, Nx, c->p.xBC, c->p.zBC, c->p.d0, c->p.g0, CF(c, FLD_etasw), CF(c, FLD_Drhox),
       CF(c, FLD_bndtaperw), CF(c, FLD_x_w), CF(c, FLD_m_w), CF(c, FLD_x_u), CF(c, FLD_m_u),
       CF(c, FLD_W), CF(c, FLD_U), CF(c, FLD_xisw), CF(c, FLD_xixw), CF(c, FLD_xiew),
@@ -504,7 +512,8 @@ int phase_velocities_impl(xc_ctx* c) {
 int store_previous_impl(xc_ctx* c) {
   const int Nz = c->Nz, Nx = c->Nx;
   dim3 blk(32, 8);
-  xc_launch(store_previous_kernel, grid2d(Nz + 1, Nx + 1, blk), blk, 0, c->stream, Nz, Nx, F(c, FLD_X), F(c,
+  xc_launch(store_previous_kernel, dim3(persistent_grid((const void*)store_previous_kernel, Nz + 1, Nx + 1)), blk,
+      0, c->stream, Nz, Nx, F(c, FLD_X), F(c,
       FLD_Xo), F(c, FLD_Xoo), F(c, FLD_M), F(c, FLD_Mo), F(c, FLD_Moo),
       F(c, FLD_dXdt), F(c, FLD_dXdto), F(c, FLD_dXdtoo), F(c, FLD_rho), F(c, FLD_rhoo),
       F(c, FLD_rhooo), F(c, FLD_drhodt), F(c, FLD_drhodto), F(c, FLD_drhodtoo), CF(c, FLD_rhow),
