@@ -124,3 +124,32 @@ def test_julia_solver_opts_calls_have_six_or_all_arguments():
     for args in calls:
         k = len([a for a in args.split(",") if a.strip()])
         assert k in (6, n), (k, args)
+
+
+def _julia_extension_methods():
+    """(name, positional arguments) of every method the binding adds to a
+    function of the xcore module (`function xcore.f(...)` or `xcore.f(...) =`)."""
+    src = re.sub(r"#.*", "", open(JULIA).read())
+    out = []
+    for m in re.finditer(r"(?:^function\s+|^)xcore\.(\w+!?)\(", src, flags=re.M):
+        depth, k = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(src[k], 0)
+            k += 1
+        args = src[m.end():k - 1].split(";")[0]
+        out.append((m.group(1), [a.strip() for a in args.split(",") if a.strip()]))
+    return out
+
+
+def test_julia_gpu_methods_type_every_positional_argument():
+    """A GPU method that leaves a positional argument untyped ties with the
+    reference's own method (which types every one) and makes the call
+    ambiguous; each must be strictly more specific."""
+    methods = _julia_extension_methods()
+    assert {n for n, _ in methods} >= {"store_previous!", "snapshot!", "phsevo!", "fluidmech!", "noise!",
+                                       "update_phase_velocities!", "update!", "compute_resnorm", "update_dt"}
+    for name, args in methods:
+        assert args, name
+        for a in args:
+            assert "::" in a, (name, a)
+        assert any(a.endswith(("::GPUPhase", "::GPUFluid")) for a in args), name

@@ -266,6 +266,15 @@ using Random
 
 const GPUFluid = xcore.FluidState{Float64,<:CuArray}
 const GPUPhase = xcore.PhaseState{Float64,<:CuArray}
+# Every positional argument below carries the reference's type at T = Float64:
+# each method is then strictly more specific than the reference's own
+# (a method that left grid, par, ... untyped would tie with it and make every
+# call ambiguous).
+const Grid64 = xcore.Grid{Float64}
+const Par64 = xcore.Parameters{Float64}
+const Scales64 = xcore.Scales{Float64}
+const Noise64 = xcore.NoiseState{Float64}
+const Res = xcore.StepResidual
 const BOUND = IdDict{Any,Context}()
 const BOUND_BC = IdDict{Any,NTuple{4,Int}}()   # (sds, top_cnv, bot_cnv, open_cnv) of each bound context
 
@@ -301,17 +310,17 @@ function xcore.store_previous!(fluid::GPUFluid, phase::GPUPhase)
     store_noise!(ctx)
 end
 
-xcore.snapshot!(res, phase::GPUPhase, fluid::GPUFluid) = snapshot!(bound_context(phase))
+xcore.snapshot!(res::Res, phase::GPUPhase, fluid::GPUFluid) = snapshot!(bound_context(phase))
 
-function xcore.phsevo!(phase::GPUPhase, fluid::GPUFluid, grid, par, scales; ADVN = par.ADVN, xBC = :periodic,
-                       zBC = :closed, a1, a2, a3, b1, b2, b3, dt, alpha = par.alpha)
+function xcore.phsevo!(phase::GPUPhase, fluid::GPUFluid, grid::Grid64, par::Par64, scales::Scales64;
+                       ADVN = par.ADVN, xBC = :periodic, zBC = :closed, a1, a2, a3, b1, b2, b3, dt, alpha = par.alpha)
     ctx = bound_context(phase, fluid, grid, par, scales; xBC, zBC)
     phsevo!(ctx; ADVN, a1, a2, a3, b1, b2, b3, dt, alpha)
 end
 
-function xcore.fluidmech!(fluid::GPUFluid, grid, par; phase::GPUPhase, sds = -1, top_cnv = 1, bot_cnv = 1,
-                          open_cnv = false, xBC = :periodic, zBC = :closed, dt = 1e32, a1 = 1.0, a2 = 1.0,
-                          a3 = 0.0, b1 = 1.0, b2 = 0.0, b3 = 0.0)
+function xcore.fluidmech!(fluid::GPUFluid, grid::Grid64, par::Par64; phase::GPUPhase, sds = -1, top_cnv = 1,
+                          bot_cnv = 1, open_cnv = false, xBC = :periodic, zBC = :closed, dt = 1e32, a1 = 1.0,
+                          a2 = 1.0, a3 = 0.0, b1 = 1.0, b2 = 0.0, b3 = 0.0)
     # run! calls phsevo! first in every sweep, which binds the context; the
     # Stokes boundary keywords are the context's (call bound_context with
     # them before run! when they are not the defaults)
@@ -324,7 +333,8 @@ function xcore.fluidmech!(fluid::GPUFluid, grid, par; phase::GPUPhase, sds = -1,
     return nothing
 end
 
-function xcore.noise!(ns, phase::GPUPhase, grid, par, scales, dt; first_iter::Bool = true)
+function xcore.noise!(ns::Noise64, phase::GPUPhase, grid::Grid64, par::Par64, scales::Scales64, dt::Real;
+                      first_iter::Bool = true)
     ctx = bound_context(phase)
     if first_iter
         randn!(ns.rng, ns.re)
@@ -335,11 +345,15 @@ function xcore.noise!(ns, phase::GPUPhase, grid, par, scales, dt; first_iter::Bo
     end
 end
 
-xcore.update_phase_velocities!(phase::GPUPhase, fluid::GPUFluid, ns, grid, par; xBC = :periodic, zBC = :closed) =
+xcore.update_phase_velocities!(phase::GPUPhase, fluid::GPUFluid, ns::Noise64, grid::Grid64, par::Par64;
+                               xBC = :periodic, zBC = :closed) =
     update_phase_velocities!(bound_context(phase))
-xcore.update!(phase::GPUPhase, fluid::GPUFluid, grid, par, scales; xBC = :periodic, zBC = :closed) =
+xcore.update!(phase::GPUPhase, fluid::GPUFluid, grid::Grid64, par::Par64, scales::Scales64; xBC = :periodic,
+              zBC = :closed) =
     update!(bound_context(phase))
-xcore.compute_resnorm(res, phase::GPUPhase, fluid::GPUFluid, dt) = compute_resnorm(bound_context(phase), dt)
-xcore.update_dt(phase::GPUPhase, fluid::GPUFluid, grid, par, dt_prev) = update_dt(bound_context(phase), dt_prev)
+xcore.compute_resnorm(res::Res, phase::GPUPhase, fluid::GPUFluid, dt::Real) =
+    compute_resnorm(bound_context(phase), dt)
+xcore.update_dt(phase::GPUPhase, fluid::GPUFluid, grid::Grid64, par::Par64, dt_prev::Real) =
+    update_dt(bound_context(phase), dt_prev)
 
 end # module
