@@ -46,6 +46,48 @@ import numpy as np
 EPS = float(np.finfo(np.float64).eps)
 SQRT_EPS = math.sqrt(EPS)
 
+
+def jl_max(a, b):
+    """Julia's ``max`` of Float64 values, elementwise with broadcasting: NaN
+    if either argument is NaN, and -0.0 < +0.0, so max(0.0, -0.0) is +0.0
+    in either order (numpy's maximum returns its second argument for two
+    zeros)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    r = np.where(a > b, a, np.where(b > a, b, np.where(np.signbit(a), b, a)))
+    return np.where(np.isnan(a) | np.isnan(b), a + b, r)
+
+
+def jl_min(a, b):
+    """Julia's ``min`` of Float64 values (NaN propagates; min(0.0, -0.0) is
+    -0.0 in either order)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    r = np.where(a < b, a, np.where(b < a, b, np.where(np.signbit(a), a, b)))
+    return np.where(np.isnan(a) | np.isnan(b), a + b, r)
+
+
+def jl_maximum(a) -> float:
+    """Julia's ``maximum`` of a Float64 array: NaN if any element is NaN
+    (numpy's max agrees), and +0.0 when the largest value is a zero and any
+    zero is +0.0 (numpy may return either zero)."""
+    a = np.asarray(a, dtype=np.float64)
+    m = float(a.max())
+    if m == 0.0:
+        return 0.0 if (~np.signbit(a[a == 0.0])).any() else -0.0
+    return m
+
+
+def jl_minimum(a) -> float:
+    """Julia's ``minimum`` of a Float64 array (NaN propagates; -0.0 when the
+    smallest value is a zero and any zero is -0.0)."""
+    a = np.asarray(a, dtype=np.float64)
+    m = float(a.min())
+    if m == 0.0:
+        return -0.0 if np.signbit(a[a == 0.0]).any() else 0.0
+    return m
+
+
 # ---------------------------------------------------------------------------
 # parameters, grid, scales  (src/parameters.jl:12-89, src/grid.jl:311-334,
 #                            src/scales.jl:85-185)
@@ -292,7 +334,7 @@ def tvd_flux(fm, fc, fp, vm, vp):
     num = vm * (fc - fm)
     den = vp * (fp - fc)
     R = num / (den + np.copysign(EPS, den))
-    lim = np.maximum(0.0, np.maximum(np.minimum(1.0, 2.0 * R), np.minimum(2.0, R)))
+    lim = jl_max(0.0, jl_max(jl_min(1.0, 2.0 * R), jl_min(2.0, R)))
     return fc + (0.5 * lim) * (fp - fc)
 
 
@@ -600,7 +642,7 @@ def update_segregation_speed(st: State, grid: Grid, par: Params, xBC="periodic")
     st.wx[:, -1] = st.wx[:, 1]
     x_w_ext = st.x_w[:, icx]
     m_w_ext = st.m_w[:, icx]
-    st.wm = ((-x_w_ext) / np.maximum(m_w_ext, EPS)) * st.wx
+    st.wm = ((-x_w_ext) / jl_max(m_w_ext, EPS)) * st.wx
 
 
 def update_phase_velocities(st: State, grid: Grid, par: Params, xBC="periodic", zBC="closed"):
@@ -614,8 +656,8 @@ def update_phase_velocities(st: State, grid: Grid, par: Params, xBC="periodic", 
     m_u_ext = st.m_u[icz, :]
     st.Wx = ((st.W + st.wx) + (st.xisw + st.xixw)) + st.xiew
     st.Ux = (st.U + (st.xisu + st.xixu)) + st.xieu
-    st.Wm = ((st.W + st.wm) - ((x_w_ext / np.maximum(m_w_ext, EPS)) * (st.xisw + st.xixw))) + st.xiew
-    st.Um = (st.U + (((-x_u_ext) / np.maximum(m_u_ext, EPS)) * (st.xisu + st.xixu))) + st.xieu
+    st.Wm = ((st.W + st.wm) - ((x_w_ext / jl_max(m_w_ext, EPS)) * (st.xisw + st.xixw))) + st.xiew
+    st.Um = (st.U + (((-x_u_ext) / jl_max(m_u_ext, EPS)) * (st.xisu + st.xixu))) + st.xieu
 
 
 # ---------------------------------------------------------------------------
@@ -675,7 +717,7 @@ def update_pressure(st: State, grid: Grid, par: Params):
     for j in range(1, Nz):
         col[j] = col[j - 1] + (rhoref[j] * par.g0) * h
     st.Pl = np.repeat(col[:, None], grid.Nx, axis=1)
-    st.Pt = np.maximum(par.Ptop / 100.0, st.Pl + st.P[1:-1, 1:-1])
+    st.Pt = jl_max(par.Ptop / 100.0, st.Pl + st.P[1:-1, 1:-1])
 
 
 def rheology(chi, mu, par: Params):
@@ -754,7 +796,7 @@ def update_viscosity(st: State, grid: Grid, par: Params, sc: dict):
     etae = (fReL * ke) * st.rho
     etai = st.etamix + etae
     st.etae, st.ke, st.kx, st.ReL, st.fReL = etae, ke, ke.copy(), ReL, fReL
-    emax = etai.min() * par.etacntr
+    emax = jl_minimum(etai) * par.etacntr
     eta = 1.0 / (1.0 / emax + 1.0 / etai)
     st.eta = 0.5 * eta + 0.5 * eta_prev
     st.ReD = (st.V * sc["D0"]) / (st.eta / st.rho)
@@ -773,8 +815,8 @@ def update_segregation_viscosity(st: State, par: Params, sc: dict, zBC="closed")
     etasi = etamix + etat
     st.Rel, st.fRel, st.ks, st.etat = Rel, fRel, ks, etat
     st.kx = ks + st.fReL * st.ke
-    st.Rc = st.V / np.maximum(vx, EPS)
-    emax = etasi.min() * par.etacntr
+    st.Rc = st.V / jl_max(vx, EPS)
+    emax = jl_minimum(etasi) * par.etacntr
     etas = 1.0 / (1.0 / emax + 1.0 / etasi)
     st.etas = 0.5 * etas + 0.5 * etas_prev
     st.Red = (vx * par.d0) / (st.etas / rho)
@@ -807,22 +849,30 @@ def update(st: State, grid: Grid, par: Params, sc: dict, xBC="periodic", zBC="cl
 
 
 def jmax(*v):
-    """Julia's max of Float64 scalars: NaN if any argument is NaN (Python's
-    builtin max keeps or drops a NaN depending on argument order)."""
-    return float(np.max(np.array(v, dtype=np.float64)))
+    """Julia's max of Float64 scalars, max(max(a, b), c)...: NaN if any
+    argument is NaN (Python's builtin max keeps or drops a NaN depending on
+    argument order)."""
+    r = v[0]
+    for x in v[1:]:
+        r = jl_max(r, x)
+    return float(r)
 
 
 def jmin(*v):
     """Julia's min of Float64 scalars (NaN propagates)."""
-    return float(np.min(np.array(v, dtype=np.float64)))
+    r = v[0]
+    for x in v[1:]:
+        r = jl_min(r, x)
+    return float(r)
 
 
 def update_dt(st: State, grid: Grid, par: Params, dt_prev: float) -> float:
-    """src/update.jl:494-502 (numpy's max / min propagate NaN as Julia's
-    maximum / minimum do)."""
+    """src/update.jl:494-502, with Julia's maximum / max / min (NaN
+    propagates, -0.0 < +0.0)."""
     h = grid.h
-    dtk = (h / 2.0) * (h / 2.0) / st.kx.max()
-    vmax = jmax(np.abs(st.Wx).max(), np.abs(st.Wm).max(), np.abs(st.Ux).max(), np.abs(st.Um).max()) + EPS
+    dtk = (h / 2.0) * (h / 2.0) / jl_maximum(st.kx)
+    vmax = jmax(jl_maximum(np.abs(st.Wx)), jl_maximum(np.abs(st.Wm)), jl_maximum(np.abs(st.Ux)),
+                jl_maximum(np.abs(st.Um))) + EPS
     dta = (h / 2.0) / vmax
     return jmin(1.5 * dt_prev, jmin(dtk, par.CFL * dta), par.dtmax)
 
@@ -901,17 +951,17 @@ def noise(st: State, grid: Grid, par: Params, sc: dict, ns: NoiseStatic, dt: flo
     taue = L0h / (2.0 * (st.V + EPS))
     taus = l0h / (2.0 * (st.vx + EPS))
     St = txi0 / (taue + EPS)
-    sge = Xi * np.sqrt(np.maximum(0.0, (st.fReL * st.ke) / taue))
-    sgx = Xi * np.sqrt(np.maximum(0.0, ((((st.chi * st.fReL) * st.ke) / taue) * St) / (1.0 + St * St)))
-    sgs = Xi * np.sqrt(np.maximum(0.0, (st.chi * st.ks) / taus))
+    sge = Xi * np.sqrt(jl_max(0.0, (st.fReL * st.ke) / taue))
+    sgx = Xi * np.sqrt(jl_max(0.0, ((((st.chi * st.fReL) * st.ke) / taue) * St) / (1.0 + St * St)))
+    sgs = Xi * np.sqrt(jl_max(0.0, (st.chi * st.ks) / taus))
     taue = 1.0 / (1.0 / taue + 1.0 / (1e2 * dt)) + dt
     taus = 1.0 / (1.0 / taus + 1.0 / (1e2 * dt)) + dt
     Fte = np.exp((-dt) / taue)
     Fts = np.exp((-dt) / taus)
     fL = 2.0 / math.sqrt(1.0 - math.exp(-(h * h) / (2 * (L0h * L0h))))
     fl = 2.0 / math.sqrt(1.0 - math.exp(-(h * h) / (2 * (l0h * l0h))))
-    ae = np.sqrt(np.maximum(0.0, 1.0 - Fte * Fte))
-    as_ = np.sqrt(np.maximum(0.0, 1.0 - Fts * Fts))
+    ae = np.sqrt(jl_max(0.0, 1.0 - Fte * Fte))
+    as_ = np.sqrt(jl_max(0.0, 1.0 - Fts * Fts))
     st.psie = Fte * st.psieo + ((ae * sge) * fL) * st.re
     st.psix = Fte * st.psixo + ((ae * sgx) * fL) * st.re
     st.psis = Fts * st.psiso + ((as_ * sgs) * fl) * st.rs
@@ -924,8 +974,8 @@ def noise(st: State, grid: Grid, par: Params, sc: dict, ns: NoiseStatic, dt: flo
     xiew_int = -(psiec[:, 1:] - psiec[:, :-1])
     st.xieu = xieu_int[icz, :]
     st.xiew = xiew_int[:, icx]
-    xtaperw = (1.0 - np.exp((-st.chiw) / 1e-4)) * (1.0 - np.exp((-np.maximum(0.0, st.muw - 0.4)) / 0.05))
-    xtaperu = (1.0 - np.exp((-st.chiu) / 1e-4)) * (1.0 - np.exp((-np.maximum(0.0, st.muu - 0.4)) / 0.05))
+    xtaperw = (1.0 - np.exp((-st.chiw) / 1e-4)) * (1.0 - np.exp((-jl_max(0.0, st.muw - 0.4)) / 0.05))
+    xtaperu = (1.0 - np.exp((-st.chiu) / 1e-4)) * (1.0 - np.exp((-jl_max(0.0, st.muu - 0.4)) / 0.05))
     px_ext = px[icz][:, icx]
     ps_ext = ps[icz][:, icx]
     st.xixu = (-(px_ext[:, 1:] - px_ext[:, :-1])) * xtaperu
@@ -1257,28 +1307,29 @@ def print_step_stats(st: State) -> dict:
     """The statistics print_step! prints beyond record_history!'s
     (src/diagnose.jl:92-182) on the raw fields, with
     _gm(A) = exp(sum(log(max(A, 1e-300))) / length(A)) (diagnose.jl:10)."""
-    out = {"m_min": float(st.m.min()), "m_mean": float(st.m.mean()), "m_max": float(st.m.max())}
+    out = {"m_min": jl_minimum(st.m), "m_mean": float(st.m.mean()), "m_max": jl_maximum(st.m)}
     for f in ("rho", "V", "vx", "vm", "xie", "xix", "xis"):
         a = getattr(st, f)
-        out[f + "_min"] = float(a.min())
-        out[f + "_gm"] = math.exp(float(np.log(np.maximum(a, 1e-300)).sum()) / a.size)
-        out[f + "_max"] = float(a.max())
+        out[f + "_min"] = jl_minimum(a)
+        out[f + "_gm"] = math.exp(float(np.log(jl_max(a, 1e-300)).sum()) / a.size)
+        out[f + "_max"] = jl_maximum(a)
     return out
 
 
 def history_stats(st: State) -> dict:
     """Field statistics pushed by record_history! (src/history.jl:183-222), with
     _rms = sqrt(mean(x^2)) and _geomean = exp(mean(log(max(x, eps)))) (history.jl:8-9)."""
-    out = {"x_min": float(st.x.min()), "x_mean": float(st.x.mean()), "x_max": float(st.x.max()),
+    out = {"x_min": jl_minimum(st.x), "x_mean": float(st.x.mean()), "x_max": jl_maximum(st.x),
            "x_std": std1(st.x)}
     for f in ("V", "vx", "vm", "xie", "xix", "xis"):
         a = getattr(st, f)
-        out[f + "_min"], out[f + "_rms"], out[f + "_max"] = float(a.min()), math.sqrt(float((a * a).mean())), float(a.max())
+        out[f + "_min"], out[f + "_max"] = jl_minimum(a), jl_maximum(a)
+        out[f + "_rms"] = math.sqrt(float((a * a).mean()))
     for f in ("Ra", "Rc", "ReD", "Red", "ks", "ke", "kx", "eta", "etamix", "etae", "etas", "etat"):
         a = getattr(st, f)
-        out[f + "_min"] = float(a.min())
-        out[f + "_gm"] = math.exp(float(np.log(np.maximum(a, EPS)).mean()))
-        out[f + "_max"] = float(a.max())
+        out[f + "_min"] = jl_minimum(a)
+        out[f + "_gm"] = math.exp(float(np.log(jl_max(a, EPS)).mean()))
+        out[f + "_max"] = jl_maximum(a)
     return out
 
 

@@ -1,6 +1,7 @@
 // Internal declarations shared by the translation units of libxcore_gb300.
 #pragma once
 
+#include <cmath>
 #include <functional>
 #include <utility>
 
@@ -227,13 +228,28 @@ __device__ __forceinline__ void for_tiles(int rows, int cols, F&& f) {
 // CTAs of such a launch of `kernel` over rows x cols
 unsigned persistent_grid(const void* kernel, int rows, int cols);
 
-// Julia's max / min of two Float64 (a NaN argument gives NaN; CUDA's fmax /
-// fmin return the other argument instead)
+// Julia's max / min of two Float64 (Base.max / Base.min on IEEE floats): a
+// NaN argument gives NaN -- CUDA's fmax / fmin return the other argument
+// instead -- and zeros are ordered -0.0 < +0.0, so max(0.0, -0.0) is +0.0 and
+// min(0.0, -0.0) is -0.0 whatever the argument order (a plain a > b ? a : b
+// returns the second argument for two zeros).  Either result is independent
+// of the order in which a reduction combines its values.
+__host__ __device__ __forceinline__ bool jsignbit(double a) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(a) < 0;
+#else
+  return std::signbit(a);
+#endif
+}
 __host__ __device__ __forceinline__ double jmax(double a, double b) {
-  return (a != a || b != b) ? a + b : (a > b ? a : b);
+  if (a > b) return a;
+  if (b > a) return b;
+  return (a != a || b != b) ? a + b : (jsignbit(a) ? b : a);
 }
 __host__ __device__ __forceinline__ double jmin(double a, double b) {
-  return (a != a || b != b) ? a + b : (a < b ? a : b);
+  if (a < b) return a;
+  if (b < a) return b;
+  return (a != a || b != b) ? a + b : (jsignbit(a) ? a : b);
 }
 
 // deterministic reductions (xc_reduce.cu): CTA partials, combined in a fixed
