@@ -1274,20 +1274,30 @@ def fluidmech(st: State, grid: Grid, par: Params, coefs, dt, bn: Bnchm | None = 
 # ---------------------------------------------------------------------------
 
 
-def snapshot(st: State) -> dict:
-    """snapshot! (src/diagnose.jl:42-49)."""
-    return dict(W=st.W.copy(), U=st.U.copy(), P=st.P.copy(), X=st.X.copy(), MFS=st.MFS.copy())
+def snapshot(st: State, res: dict | None = None) -> dict:
+    """snapshot! (src/diagnose.jl:42-49): the StepResidual's buffers as a dict.
+    Given a StepResidual ``res`` (a dict from an earlier call), its buffers
+    are replaced and its ``resnorm0`` kept, as snapshot! leaves that field
+    alone; a fresh one starts with resnorm0 = 1.0 (diagnose.jl:26-33)."""
+    out = res if res is not None else {"resnorm0": 1.0}
+    out.update(W=st.W.copy(), U=st.U.copy(), P=st.P.copy(), X=st.X.copy(), MFS=st.MFS.copy())
+    return out
 
 
 def resnorm(st: State, snap: dict, dt: float):
-    """compute_resnorm (src/diagnose.jl:57-71) -> (resnorm, res_mass, res_mmnt)."""
+    """compute_resnorm (src/diagnose.jl:57-71) -> (resnorm, res_mass, res_mmnt);
+    raises the StepResidual's resnorm0 to resnorm + 1e-32 when it is below
+    resnorm (diagnose.jl:67-69)."""
     nrm = np.linalg.norm
     ep = EPS
     nrho = float(nrm(st.rho))
     res_mass = nrm(st.X - snap["X"]) / (nrho + ep) + nrm(st.MFS - snap["MFS"]) / (nrho / dt + ep)
     res_mmnt = (nrm(st.W - snap["W"]) / (nrm(st.W) + ep) + nrm(st.U - snap["U"]) / (nrm(st.U) + ep)
                 + nrm(st.P - snap["P"]) / (nrm(st.P) + ep))
-    return float(res_mass + res_mmnt), float(res_mass), float(res_mmnt)
+    r = float(res_mass + res_mmnt)
+    if "resnorm0" in snap and snap["resnorm0"] < r:
+        snap["resnorm0"] = r + 1e-32
+    return r, float(res_mass), float(res_mmnt)
 
 
 def conservation_sums(st: State, grid: Grid) -> dict:

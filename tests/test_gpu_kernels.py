@@ -207,6 +207,16 @@ def test_dt_resnorm_sums():
     got = ds.compute_resnorm(dt)
     ref = O.resnorm(st, snap, dt)
     np.testing.assert_allclose(got, ref, rtol=1e-12)
+    # compute_resnorm's resnorm0 rule as the oracle's StepResidual has it
+    # (test/test_diagnose.jl:80-91)
+    res = O.snapshot(st)
+    ds.snapshot()
+    res["resnorm0"] = ds.resnorm0 = 1e-10
+    st.W = st.W + 1.0
+    ds["W"] = st.W
+    rn = ds.compute_resnorm(dt)[0]
+    assert rn == pytest.approx(O.resnorm(st, res, dt)[0], rel=1e-12)
+    assert ds.resnorm0 == pytest.approx(rn + 1e-32) and res["resnorm0"] == pytest.approx(ds.resnorm0, rel=1e-12)
     s = ds.conservation_sums()
     r = O.conservation_sums(st, g)
     for k, v in r.items():

@@ -358,6 +358,26 @@ def test_resnorm_positive_after_change():
     assert O.resnorm(st, snap, sc["dt0"])[0] > 0
 
 
+def test_resnorm_raises_resnorm0_when_the_residual_rises():
+    """test/test_diagnose.jl:80-91: with resnorm0 = 1e-10, a change of W makes
+    compute_resnorm set resnorm0 to resnorm + 1e-32; snapshot! keeps it."""
+    par, g, sc, ns, st, _ = _small_run(N=8)
+    res = O.snapshot(st)
+    assert res["resnorm0"] == 1.0
+    res["resnorm0"] = 1e-10
+    res = O.snapshot(st, res)
+    assert res["resnorm0"] == 1e-10
+    st.W = st.W + 1.0
+    rn = O.resnorm(st, res, sc["dt0"])[0]
+    assert rn > 1e-10
+    assert res["resnorm0"] == pytest.approx(rn + 1e-32)
+    # a smaller residual leaves it where it is
+    res = O.snapshot(st, res)
+    st.W = st.W + 1e-6
+    O.resnorm(st, res, sc["dt0"])
+    assert res["resnorm0"] == pytest.approx(rn + 1e-32)
+
+
 def _noise_setup(N=16, seed=42):
     """test/test_noise.jl:8-19: Parameters(D = 10, N, L = 10, etam0 = 10,
     x0 = 0.1, Da = 0, Xi = 0.5) after initialize! (the initial draw supplied)."""

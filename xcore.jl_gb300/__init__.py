@@ -384,6 +384,9 @@ class State:
         _check(lib().xc_ctx_create(ctypes.byref(P), ctypes.byref(h)))
         self._h = h
         self._ids = {n: i for i, n in enumerate(field_names())}
+        # StepResidual.resnorm0 (src/diagnose.jl:23, 1.0 at construction):
+        # compute_resnorm raises it, nothing else touches it
+        self.resnorm0 = 1.0
 
     # -- lifetime ----------------------------------------------------------
     def close(self):
@@ -513,9 +516,13 @@ class State:
         return out.value
 
     def compute_resnorm(self, dt):
-        """compute_resnorm(res, phase, fluid, dt) -- src/diagnose.jl:57-71."""
+        """compute_resnorm(res, phase, fluid, dt) -- src/diagnose.jl:57-71:
+        (resnorm, res_mass, res_mmnt) against the last snapshot; raises
+        ``self.resnorm0`` to resnorm + 1e-32 when it is below resnorm."""
         out = (ctypes.c_double * 3)()
         _check(lib().xc_resnorm(self._h, float(dt), out))
+        if self.resnorm0 < out[0]:
+            self.resnorm0 = out[0] + 1e-32
         return tuple(out)
 
     def conservation_sums(self):
