@@ -6,13 +6,13 @@ The reference has no temperature field and its viscosity is the
 permission-weight mixture capped by etacntr (src/update.jl:144-177, 330-335),
 so each configuration maps onto the reference's own inputs:
 
-* c1: 100 x 100 box (D = L = 10), x0 = 0.05, Da = 0, dxr = 0, L0 = l0 = 3h,
+* box100: 100 x 100 box (D = L = 10), x0 = 0.05, Da = 0, dxr = 0, L0 = l0 = 3h,
   etacntr 1e2, WENO5, BD2; the initial crystal fraction is
   x = 0.05 (1 + 1e-3 G2 * xi), xi ~ N(0, 1) from seed 0 and G2 a Gaussian
   smoothing over 2 cells (periodic in x, mirrored in z), in place of the
   reference's MersenneTwister perturbation (src/run.jl:98-108);
-* c2: 400 x 400, x ~ U[0.02, 0.10] (seed 1), etacntr 1e3, WENO5 or QUICK;
-* c3: N x N, x ~ lognormal (median 0.1, sigma 0.5) clipped to [0, 0.4],
+* box400: 400 x 400, x ~ U[0.02, 0.10] (seed 1), etacntr 1e3, WENO5 or QUICK;
+* lognormal: N x N, x ~ lognormal (median 0.1, sigma 0.5) clipped to [0, 0.4],
   etacntr 1e4, WENO5.
 
 White-noise draws come from numpy's default_rng(seed + 1000) as two
@@ -30,11 +30,11 @@ N_SAMPLES = 64
 
 
 def params(cfg, N=None, scheme="weno5"):
-    N = N or {"c1": 100, "c2": 400, "c3": 256}[cfg]
+    N = N or {"box100": 100, "box400": 400, "lognormal": 256}[cfg]
     D = 10.0
     h = D / N
-    etacntr = {"c1": 1e2, "c2": 1e3, "c3": 1e4}[cfg]
-    x0 = {"c1": 0.05, "c2": 0.06, "c3": 0.1}[cfg]
+    etacntr = {"box100": 1e2, "box400": 1e3, "lognormal": 1e4}[cfg]
+    x0 = {"box100": 0.05, "box400": 0.06, "lognormal": 0.1}[cfg]
     return O.Params(D=D, N=N, L=D, etam0=10.0, x0=x0, Da=0.0, dxr=0.0, L0=3 * h, l0=3 * h, etacntr=etacntr,
                     ADVN=scheme, TINT="bd2im")
 
@@ -61,10 +61,10 @@ def smooth2(a):
 
 
 def initial_x(cfg, N):
-    if cfg == "c1":
+    if cfg == "box100":
         xi = np.random.default_rng(0).standard_normal((N, N))
         return 0.05 * (1.0 + 1e-3 * smooth2(xi))
-    if cfg == "c2":
+    if cfg == "box400":
         return np.random.default_rng(1).uniform(0.02, 0.10, (N, N))
     rng = np.random.default_rng(2)
     return np.clip(np.exp(np.log(0.1) + 0.5 * rng.standard_normal((N, N))), 0.0, 0.4)
@@ -74,7 +74,7 @@ class Draws:
     """Per-step white-noise draws (re, rs) of a configuration."""
 
     def __init__(self, cfg, N):
-        self.rng = np.random.default_rng({"c1": 1000, "c2": 1001, "c3": 1002}[cfg])
+        self.rng = np.random.default_rng({"box100": 1000, "box400": 1001, "lognormal": 1002}[cfg])
         self.N = N
 
     def next(self):

@@ -2,18 +2,20 @@
 oracle (numpy stencils, SciPy SuperLU for the Stokes solve), for the GPU
 trajectory tests in tests/test_gpu_configs.py.
 
-  c1_100.npz        100 x 100, WENO5, 100 time steps (3 Picard sweeps each):
+  box100_weno5_100steps.npz
+                    100 x 100, WENO5, 100 time steps (3 Picard sweeps each):
                     per step dt, the sweeps' residual norms and a digest of
                     every field of tests/configs.py DIGEST_FIELDS; the full
                     fields x, W, U, P after steps 1 and 10
-  c2_400_<s>.npz    400 x 400, s = weno5 or quick, 3 time steps, same content
+  box400_<s>_3steps.npz
+                    400 x 400, s = weno5 or quick, 3 time steps, same content
                     (one 400^2 sparse-LU solve takes about 100 s here)
 
 The initial conditions and the white-noise draws are regenerated from their
 seeds (tests/configs.py) by whoever reads the files; each file keeps a
 checksum of the draws it used.  Run from the repository root:
 
-    python tests/golden/make_configs.py [c1] [c2_weno5] [c2_quick]
+    python tests/golden/make_configs.py [box100] [box400_weno5] [box400_quick]
 """
 import os
 import sys
@@ -57,9 +59,9 @@ def run(cfg, scheme, steps, full_at, out_name):
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["c1", "c2_weno5", "c2_quick"]
-    if "c1" in which:
-        run("c1", "weno5", 100, (1, 10), "c1_100.npz")
+    which = sys.argv[1:] or ["box100", "box400_weno5", "box400_quick"]
+    if "box100" in which:
+        run("box100", "weno5", 100, (1, 10), "box100_weno5_100steps.npz")
     for s in ("weno5", "quick"):
-        if f"c2_{s}" in which:
-            run("c2", s, 3, (), f"c2_400_{s}.npz")
+        if f"box400_{s}" in which:
+            run("box400", s, 3, (), f"box400_{s}_3steps.npz")

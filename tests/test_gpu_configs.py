@@ -1,8 +1,8 @@
 """Parity at the sizes of the benchmark configurations (tests/configs.py), on
 the GPU through the C ABI against the CPU oracle.
 
-1. Identical inputs, per sweep (c1 100^2 for 10 steps; c2 400^2 for one
-   step, WENO5 and QUICK): before every Picard sweep the oracle's whole state
+1. Identical inputs, per sweep (the 100^2 box for 10 steps; the 400^2 box
+   for one step, WENO5 and QUICK): before every Picard sweep the oracle's whole state
    is copied into the GPU context, both run the sweep, and the oracle takes
    the GPU's Stokes solution (W, U, P) in place of its sparse LU; every other
    field of FluidState, PhaseState and NoiseState -- the stencils, phsevo!,
@@ -10,15 +10,15 @@ the GPU through the C ABI against the CPU oracle.
    within 1e-12 (normwise relative), and dt and the residual norms with them.
    (Without the copy, the last-bit differences of the exp / pow fields carry
    into the next sweep, and fields that are small differences of nearly
-   equal terms -- advn_rho = advn_X + advn_M, Drho, MFS, drhodt at c1's
-   1e-3 perturbation -- show them at 1e-11 of their own norm; the trajectory
+   equal terms -- advn_rho = advn_X + advn_M, Drho, MFS, drhodt at the 100^2
+   box's 1e-3 perturbation -- show them at 1e-11 of their own norm; the trajectory
    tests below bound that accumulation.)
 2. Whole trajectories against the committed oracle digests
-   (tests/golden/make_configs.py): 100 steps of c1 and 3 steps of c2 (WENO5,
-   QUICK), the GPU solving Stokes with FP64 FGMRES to 1e-11 where the oracle
+   (tests/golden/make_configs.py): 100 steps of the 100^2 box and 3 steps of
+   the 400^2 box (WENO5, QUICK), the GPU solving Stokes with FP64 FGMRES to 1e-11 where the oracle
    factorises; the per-step field digests stay within the bounds stated at
-   each test.  The oracle itself must reproduce the c1 digests on this host.
-3. c3 (lognormal crystal fraction, etacntr 1e4): the FP64 and the mixed
+   each test.  The oracle itself must reproduce the 100^2 digests on this host.
+3. Lognormal crystal fraction, etacntr 1e4: the FP64 and the mixed
    solver against the sparse LU at 256^2, and the mixed solver against the
    FP64 solver at 1024^2, field by field (W, U, P)."""
 import os
@@ -96,19 +96,19 @@ def _lockstep(cfg, scheme, steps, **kw):
     ds.close()
 
 
-def test_c1_identical_stokes_inputs_ten_steps():
-    _lockstep("c1", "weno5", 10)
+def test_box100_identical_stokes_inputs_ten_steps():
+    _lockstep("box100", "weno5", 10)
 
 
 @pytest.mark.parametrize("scheme", ["weno5", "quick"])
-def test_c2_identical_stokes_inputs_one_step(scheme):
-    _lockstep("c2", scheme, 1)
+def test_box400_identical_stokes_inputs_one_step(scheme):
+    _lockstep("box400", scheme, 1)
 
 
-def test_c2_weno5_one_division_weights_identical_stokes_inputs():
+def test_box400_weno5_one_division_weights_identical_stokes_inputs():
     """WENO5 with its weights over a common denominator (weno_weights = 1):
     every field within the same 1e-12 of the oracle's four-division form."""
-    _lockstep("c2", "weno5", 1, weno_weights=1)
+    _lockstep("box400", "weno5", 1, weno_weights=1)
 
 
 def _trajectory(cfg, scheme, name, steps, bound_fields, bound_dt):
@@ -143,27 +143,28 @@ def _trajectory(cfg, scheme, name, steps, bound_fields, bound_dt):
     ds.close()
 
 
-def test_c1_trajectory_100_steps_matches_oracle_digests():
+def test_box100_trajectory_100_steps_matches_oracle_digests():
     """100 steps at 100^2: iterative Stokes (FP64 FGMRES, 1e-11) against the
     oracle's sparse LU; the fields stay within 1e-8 of the oracle's digests
     (norms, sums, extremes, 64 fixed samples per field) at every step
     (measured on a GB300: 3.4e-10 worst, in U)."""
-    _trajectory("c1", "weno5", "c1_100.npz", 100, 1e-8, 1e-8)
+    _trajectory("box100", "weno5", "box100_weno5_100steps.npz", 100, 1e-8, 1e-8)
 
 
 @pytest.mark.parametrize("scheme", ["weno5", "quick"])
-def test_c2_trajectory_three_steps_matches_oracle_digests(scheme):
-    name = f"c2_400_{scheme}.npz"
+def test_box400_trajectory_three_steps_matches_oracle_digests(scheme):
+    name = f"box400_{scheme}_3steps.npz"
     if not os.path.exists(os.path.join(GOLD, name)):
         pytest.skip(f"{name} not generated")
-    _trajectory("c2", scheme, name, 3, 1e-7, 1e-8)
+    _trajectory("box400", scheme, name, 3, 1e-7, 1e-8)
 
 
-def test_oracle_reproduces_c1_digests_on_this_host():
-    """The oracle run here (numpy, SciPy SuperLU) reproduces the committed c1
-    digests for the first ten steps: the checker is the same on every host."""
-    z = np.load(os.path.join(GOLD, "c1_100.npz"))
-    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup("c1")
+def test_oracle_reproduces_box100_digests_on_this_host():
+    """The oracle run here (numpy, SciPy SuperLU) reproduces the committed
+    100^2 digests for the first ten steps: the oracle gives the same digests
+    on every host."""
+    z = np.load(os.path.join(GOLD, "box100_weno5_100steps.npz"))
+    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup("box100")
     st = O.initialize(g, par, sc, ns, x0, re0, rs0)
     dt = sc["dt0"]
     for step in range(1, 11):
@@ -174,8 +175,8 @@ def test_oracle_reproduces_c1_digests_on_this_host():
             assert e <= 1e-9, (step, f, e)
 
 
-def _c3_state(N):
-    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup("c3", N=N)
+def _lognormal_state(N):
+    par, g, sc, ns, x0, draws, (re0, rs0) = C.setup("lognormal", N=N)
     ds = device_state(par, g, sc)
     ds.initialize(x0, re0, rs0)
     coefs = O.time_coefs(par.TINT, 1)
@@ -186,12 +187,12 @@ def _c3_state(N):
     return par, g, sc, ds, coefs, sc["dt0"]
 
 
-def test_c3_fp64_and_mixed_against_lu_256():
+def test_lognormal_fp64_and_mixed_against_lu_256():
     """Per-field error of both GPU solvers against the sparse LU at 256^2
     (lognormal crystal fraction, viscosity contrast cap 1e4): FP64 FGMRES to
     1e-10 within 1e-8, the mixed solver to 1e-9 within 1e-7 (max-norm,
     relative to each field's max)."""
-    par, g, sc, ds, coefs, dt = _c3_state(256)
+    par, g, sc, ds, coefs, dt = _lognormal_state(256)
     state = ds.checkpoint()
     st = O.State(g.Nz, g.Nx)
     for name, arr in state.items():
@@ -206,18 +207,18 @@ def test_c3_fp64_and_mixed_against_lu_256():
         for k in ("W", "U", "P"):
             errs[(solver, k)] = _maxrel(ds[k], getattr(st, k))
             assert errs[(solver, k)] <= tol, (solver, k, errs[(solver, k)], info)
-    print("c3 256^2 max-norm relative error against the sparse LU:",
+    print("lognormal 256^2 max-norm relative error against the sparse LU:",
           {f"{s}/{k}": f"{v:.2e}" for (s, k), v in errs.items()})
     ds.close()
 
 
-def test_c3_mixed_against_fp64_1024():
+def test_lognormal_mixed_against_fp64_1024():
     """The mixed solver (FP32 Krylov and multigrid in FP64 refinement, 1e-9)
     against the plain FP64 solver (1e-11) at 1024^2, field by field: W and U
     within 1e-7, P within 1e-6 (max-norm relative; the pressure carries the
     saddle system's conditioning, measured 4.1e-7 against 2.6e-8 and 5.2e-8
     for W and U)."""
-    par, g, sc, ds, coefs, dt = _c3_state(1024)
+    par, g, sc, ds, coefs, dt = _lognormal_state(1024)
     state = {k: ds[k] for k in ("W", "U", "P", "MFS", "drhodt")}
     info = ds.fluidmech(coefs, dt, solver="fgmres64", rtol=1e-11, maxit=3000)
     assert info["converged"], info
@@ -228,7 +229,7 @@ def test_c3_mixed_against_fp64_1024():
                         pressure_sweeps=1)
     assert info["converged"], info
     errs = {k: _maxrel(ds[k], ref[k]) for k in ("W", "U", "P")}
-    print("c3 1024^2 mixed vs FP64 max-norm relative error:", {k: f"{v:.2e}" for k, v in errs.items()})
+    print("lognormal 1024^2 mixed vs FP64 max-norm relative error:", {k: f"{v:.2e}" for k, v in errs.items()})
     for k, e in errs.items():
         assert e <= (1e-6 if k == "P" else 1e-7), (k, e)
     ds.close()
