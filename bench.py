@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time an ensemble of this many independent instances instead (grid sides drawn from "
                          "64..512, per-member noise seed, amplitude and initial crystal fraction; member-steps/s)")
+    ap.add_argument("--ensemble-graphs", action="store_true",
+                    help="with --ensemble: one CUDA graph launch per explicit stage for all members "
+                         "(xc_ensemble_step) instead of one host thread per member")
     ap.add_argument("--weno-weights", type=int, default=1, choices=[0, 1],
                     help="WENO5 weights: 0 the reference's four-division form (bit for bit), 1 over a common "
                          "denominator (one division per reconstruction; within the 1e-12 stencil tolerance, "
@@ -227,8 +230,10 @@ def gpu_steps_per_second(xc, N, sweeps, steps, sopt, seed=5, weno_weights=0):
 
 
 def run_ensemble(a):
-    """member-steps/s of xcore_gb300.Ensemble (one context, stream and host
-    thread per member) on instances of the batched-ensemble configuration:
+    """member-steps/s of xcore_gb300.Ensemble (one context and stream per
+    member; one host thread per member, or with --ensemble-graphs one graph
+    launch per explicit stage for all members) on instances of the
+    batched-ensemble configuration:
     grid sides drawn from {64, 128, 192, 256, 384, 512}, each member with its
     own noise seed, noise amplitude Xi in [1e-4, 1e-2] and uniform initial
     crystal fraction in [0.02, 0.2]; 3 Picard sweeps, mixed Stokes to 1e-9."""
@@ -251,7 +256,7 @@ def run_ensemble(a):
         members.append(st)
         dts.append(st.scales["dt0"])
         gens.append(g)
-    ens = xc.Ensemble(members)
+    ens = xc.Ensemble(members, graphs=a.ensemble_graphs)
     solver = dict(solver="mixed", rtol=1e-9, maxit=400, inner_rtol=5e-2, inner_maxit=30, pressure_sweeps=1)
 
     def step(k):
@@ -275,7 +280,10 @@ def run_ensemble(a):
            "cell_steps_per_s": cells * a.steps / sec, "dtype": "f64+f32", "data": "synthetic",
            "config": {"workload": f"{a.ensemble} instances, sides {sorted(set(int(s) for s in sides))}",
                       "members_per_side": {str(int(s)): int((sides == s).sum()) for s in sorted(set(sides))},
-                      "implementation": "one device context, CUDA stream and host thread per member",
+                      "implementation": ("one device context and CUDA stream per member; every explicit stage one "
+                                         "CUDA graph launch for all members, the Stokes solves on one host thread "
+                                         "per member" if a.ensemble_graphs else
+                                         "one device context, CUDA stream and host thread per member"),
                       "timing": "host wall clock over the K ensemble steps (host draws included)"}}
     print(json.dumps(out), flush=True)
     ens.close()

@@ -312,6 +312,37 @@ int xc_step_converge(xc_ctx* ctx, int step, double dt, double rtol, double atol,
                      xc_step_stats* stats);
 
 /* ------------------------------------------------------------------ */
+/* ensembles: independent contexts advanced together                   */
+/* ------------------------------------------------------------------ */
+
+/* The loop of run! (src/run.jl:204-275) over many independent instances at
+   once (uneven grid sizes, parameters and noise seeds; no reference
+   counterpart beyond that loop).  Each explicit stage of a Picard sweep is one
+   CUDA graph launch for the whole ensemble -- store_previous! /
+   store_noise! / snapshot! / phsevo!; noise!; update_phase_velocities! /
+   update! / compute_resnorm's reductions; update_dt's reductions -- the
+   graph holding every member's kernels of that stage as parallel branches,
+   while the members' Stokes solves run concurrently on `threads` host
+   threads (0: one per member).  Members must be distinct contexts on one
+   device and must not be used elsewhere during a step, and the ensemble must
+   be destroyed before them. */
+typedef struct xc_ensemble xc_ensemble;
+int xc_ensemble_create(xc_ctx* const* members, int n, int threads, xc_ensemble** out);
+int xc_ensemble_destroy(xc_ensemble* ens);
+/* One time step of every member: xc_step(members[i], steps[i], dts[i],
+   sweeps, re[i], rs[i], opts, &stats[i]) for all i, with the same kernels,
+   arguments and order per member, so each member ends bit-identical to that
+   call.  re / rs (arrays of n host pointers, or NULL; an entry may be NULL)
+   are the members' white-noise draws; stats (n entries) may be NULL.
+   Status: XC_NAN when a sweep's residual norm is NaN in any member (the
+   ensemble step stops after that sweep), the first member's error otherwise,
+   XC_NOT_CONVERGED when the step was completed but some member's Stokes
+   solve stopped at its iteration cap. */
+int xc_ensemble_step(xc_ensemble* ens, const int* steps, const double* dts, int sweeps,
+                     const double* const* re, const double* const* rs, const xc_solver_opts* opts,
+                     xc_step_stats* stats);
+
+/* ------------------------------------------------------------------ */
 /* stencil-level entry points on caller device pointers                */
 /* (sizes exactly as the reference's; stream = cudaStream_t or NULL)   */
 /* ------------------------------------------------------------------ */

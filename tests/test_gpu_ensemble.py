@@ -1,6 +1,8 @@
 """Ensemble of independent instances (uneven grid sizes, separate seeds)
-stepped concurrently, one host thread and one CUDA stream per member: every
-member ends bit-identical to the same instance stepped alone."""
+stepped together -- one host thread and one CUDA stream per member, or one
+CUDA graph launch per explicit stage for all members with the Stokes solves
+on a pool of host threads: every member ends bit-identical to the same
+instance stepped alone."""
 import numpy as np
 import pytest
 
@@ -24,7 +26,8 @@ def _member(N, seed):
     return st, draws
 
 
-def test_ensemble_matches_members_stepped_alone():
+@pytest.mark.parametrize("graphs,threads", [(False, None), (True, None), (True, 2)])
+def test_ensemble_matches_members_stepped_alone(graphs, threads):
     solo = []
     for N, seed in SIZES:
         st, draws = _member(N, seed)
@@ -35,11 +38,12 @@ def test_ensemble_matches_members_stepped_alone():
         st.close()
 
     members, draws = zip(*[_member(N, seed) for N, seed in SIZES])
-    ens = xc.Ensemble(members)
+    ens = xc.Ensemble(members, threads=threads, graphs=graphs)
     dts = [m.scales["dt0"] for m in members]
     for k in range(2):
         infos = ens.step([k + 1] * len(members), dts, [d[k] for d in draws], **SOLVER)
         dts = [i["dt_next"] for i in infos]
+        assert all(i["sweeps"] == SOLVER["sweeps"] and i["solver_iterations"] > 0 for i in infos)
     for m, dt, (ref, dt_ref) in zip(members, dts, solo):
         assert dt == dt_ref
         got = m.checkpoint()

@@ -169,6 +169,10 @@ def lib():
             "xc_step_converge": (ip, [vp, ip, dp, dp, dp, ip, vp, vp, ctypes.POINTER(SolverOpts),
                                       ctypes.POINTER(StepStats)]),
             "xc_print_step_stats": (ip, [vp, D6]),
+            "xc_ensemble_create": (ip, [ctypes.POINTER(vp), ip, ip, ctypes.POINTER(vp)]),
+            "xc_ensemble_destroy": (ip, [vp]),
+            "xc_ensemble_step": (ip, [vp, ctypes.POINTER(ip), D6, ip, ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                      ctypes.POINTER(SolverOpts), ctypes.POINTER(StepStats)]),
             "xc_fill_ghosts": (ip, [vp, ip, ip, ip, ip, ip, vp]),
             "xc_advect": (ip, [vp, vp, vp, vp, ip, ip, dp, ip, vp]),
             "xc_advect_with_flux": (ip, [vp, vp, vp, vp, vp, vp, ip, ip, dp, ip, ip, ip, vp]),
@@ -643,29 +647,70 @@ class State:
 
 class Ensemble:
     """Independent instances -- grid sizes, parameters and noise seeds may all
-    differ -- advanced together on one GPU.  Every member is a ``State`` with
-    its own device context and CUDA stream; one host thread per member drives
-    it (ctypes releases the GIL for the duration of each library call), so the
-    kernels of different members overlap on the GPU where one small instance
-    alone would leave it idle between launches.  Results are those of the
-    members stepped one after another: each context computes deterministically
-    on its own stream."""
+    differ -- advanced together on one GPU, each member a ``State`` with its
+    own device context and CUDA stream.  Two drivers, both leaving every
+    member bit-identical to the same instance stepped alone:
 
-    def __init__(self, members, threads=None):
-        from concurrent.futures import ThreadPoolExecutor
+    * ``graphs=False``: one host thread per member runs ``State.step`` (ctypes
+      releases the GIL for each library call), so the kernels of different
+      members overlap on the GPU where one small instance alone would leave
+      it idle between launches;
+    * ``graphs=True``: one ``xc_ensemble_step`` call per time step, in which
+      every explicit stage of a Picard sweep is one CUDA graph launch holding
+      all members' kernels of that stage, and the Stokes solves run on
+      ``threads`` host threads of the library (default one per member).  Only
+      the fixed-sweep step (``sweeps``) is available this way."""
+
+    def __init__(self, members, threads=None, graphs=False):
         self.members = list(members)
-        self._pool = ThreadPoolExecutor(max_workers=threads or max(1, len(self.members)))
+        self.graphs = bool(graphs)
+        self._pool = None
+        self._h = None
+        if self.graphs:
+            n = len(self.members)
+            arr = (ctypes.c_void_p * n)(*[m._h.value for m in self.members])
+            h = ctypes.c_void_p()
+            _check(lib().xc_ensemble_create(arr, n, int(threads or 0), ctypes.byref(h)))
+            self._h = h
+        else:
+            from concurrent.futures import ThreadPoolExecutor
+            self._pool = ThreadPoolExecutor(max_workers=threads or max(1, len(self.members)))
 
     def step(self, steps, dts, draws, **solver):
         """One time step of every member: ``steps[i]``, ``dts[i]`` and the
-        noise draws ``draws[i] = (re, rs)`` of member i; returns the members'
-        step statistics in order."""
-        futs = [self._pool.submit(m.step, steps[i], dts[i], draws[i][0], draws[i][1], **solver)
-                for i, m in enumerate(self.members)]
-        return [f.result() for f in futs]
+        noise draws ``draws[i] = (re, rs)`` of member i (either may be None:
+        the device draws are kept); ``solver`` as for ``State.step``.  Returns
+        the members' step statistics in order."""
+        if not self.graphs:
+            futs = [self._pool.submit(m.step, steps[i], dts[i], draws[i][0], draws[i][1], **solver)
+                    for i, m in enumerate(self.members)]
+            return [f.result() for f in futs]
+        n = len(self.members)
+        kw = dict(solver)
+        sweeps = int(kw.pop("sweeps", 3))
+        o = SolverOpts.make(kw.pop("solver", "fgmres64"), kw.pop("rtol", 1e-10), kw.pop("maxit", 500),
+                            kw.pop("restart", 30), kw.pop("inner_rtol", 1e-4), kw.pop("inner_maxit", 60), **kw)
+        host = [m._draws(re, rs) for m, (re, rs) in zip(self.members, draws)]   # kept alive for the call
+        re_p = (ctypes.c_void_p * n)(*[h[2] for h in host])
+        rs_p = (ctypes.c_void_p * n)(*[h[3] for h in host])
+        st = (StepStats * n)()
+        status = lib().xc_ensemble_step(self._h, (ctypes.c_int * n)(*[int(k) for k in steps]),
+                                        (ctypes.c_double * n)(*[float(d) for d in dts]), sweeps, re_p, rs_p,
+                                        ctypes.byref(o), st)
+        infos = [s.as_dict() for s in st]
+        if status == XC_NOT_CONVERGED:
+            err = NotConverged(status, lib().xc_last_error().decode())
+            err.info = infos
+            raise err
+        _check(status)
+        return infos
 
     def close(self):
-        self._pool.shutdown()
+        if self._h is not None:
+            lib().xc_ensemble_destroy(self._h)
+            self._h = None
+        if self._pool is not None:
+            self._pool.shutdown()
         for m in self.members:
             m.close()
 

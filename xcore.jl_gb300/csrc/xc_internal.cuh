@@ -309,6 +309,13 @@ int store_noise_impl(xc_ctx* c);
 int snapshot_impl(xc_ctx* c);
 int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out);
 int resnorm_impl(xc_ctx* c, double dt, double out[3]);
+// the two above as their device reductions (into c->dscal, on s or c->stream;
+// nothing synchronises, so a graph can hold them) and the host arithmetic on
+// the fetched sums (c->hscal)
+int update_dt_reduce(xc_ctx* c, cudaStream_t s = nullptr);
+void update_dt_finish(const xc_ctx* c, double dt_prev, double* dt_out);
+int resnorm_reduce(xc_ctx* c, cudaStream_t s = nullptr);
+void resnorm_finish(const xc_ctx* c, double dt, double out[3]);
 int sums_impl(xc_ctx* c, double out[12]);
 int history_impl(xc_ctx* c, double out[58]);
 int print_stats_impl(xc_ctx* c, double out[24]);

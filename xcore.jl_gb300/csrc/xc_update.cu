@@ -546,7 +546,7 @@ int snapshot_impl(xc_ctx* c) {
 static inline CView whole(xc_ctx* c, int id) { return CF(c, id); }
 static const CView kNone{nullptr, 0};
 
-int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out) {
+int update_dt_reduce(xc_ctx* c, cudaStream_t s) {
   const int Nz = c->Nz, Nx = c->Nx;
   double* d = c->dscal + SC_DT;
   const RedJob jobs[5] = {
@@ -555,8 +555,17 @@ int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out) {
       red_job(RED_MAXABS, whole(c, FLD_Wm), kNone, nullptr, Nz + 1, Nx + 2, d + 2),
       red_job(RED_MAXABS, whole(c, FLD_Ux), kNone, nullptr, Nz + 2, Nx + 1, d + 3),
       red_job(RED_MAXABS, whole(c, FLD_Um), kNone, nullptr, Nz + 2, Nx + 1, d + 4)};
-  XC_TRY(reduce_batch(c, jobs, 5, c->stream));
+  return reduce_batch(c, jobs, 5, s ? s : c->stream);
+}
+
+int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out) {
+  XC_TRY(update_dt_reduce(c));
   XC_TRY(fetch_scalars(c, SC_DT, 5));
+  update_dt_finish(c, dt_prev, dt_out);
+  return XC_OK;
+}
+
+void update_dt_finish(const xc_ctx* c, double dt_prev, double* dt_out) {
   const double* m = c->hscal + SC_DT;
   const double h = c->p.h;
   // Julia's min / max (a NaN speed or diffusivity gives a NaN step)
@@ -564,10 +573,9 @@ int update_dt_impl(xc_ctx* c, double dt_prev, double* dt_out) {
   double vmax = jmax(jmax(jmax(m[1], m[2]), m[3]), m[4]) + XC_EPS;
   double dta = (h / 2.0) / vmax;
   *dt_out = jmin(jmin(1.5 * dt_prev, jmin(dtk, c->p.CFL * dta)), c->p.dtmax);
-  return XC_OK;
 }
 
-int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
+int resnorm_reduce(xc_ctx* c, cudaStream_t s) {
   const int Nz = c->Nz, Nx = c->Nx;
   double* d = c->dscal + SC_RESNORM;
   const RedJob jobs[9] = {
@@ -580,8 +588,17 @@ int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
       red_job(RED_SUMSQ, whole(c, FLD_U), kNone, nullptr, Nz + 2, Nx + 1, d + 6),
       red_job(RED_SUMSQDIFF, whole(c, FLD_P), whole(c, FLD_res_Po), nullptr, Nz + 2, Nx + 2, d + 7),
       red_job(RED_SUMSQ, whole(c, FLD_P), kNone, nullptr, Nz + 2, Nx + 2, d + 8)};
-  XC_TRY(reduce_batch(c, jobs, 9, c->stream));
+  return reduce_batch(c, jobs, 9, s ? s : c->stream);
+}
+
+int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
+  XC_TRY(resnorm_reduce(c));
   XC_TRY(fetch_scalars(c, SC_RESNORM, 9));
+  resnorm_finish(c, dt, out);
+  return XC_OK;
+}
+
+void resnorm_finish(const xc_ctx* c, double dt, double out[3]) {
   const double* q = c->hscal + SC_RESNORM;
   const double ep = XC_EPS;
   double nrho = std::sqrt(q[0]);
@@ -591,7 +608,6 @@ int resnorm_impl(xc_ctx* c, double dt, double out[3]) {
   out[0] = res_mass + res_mmnt;
   out[1] = res_mass;
   out[2] = res_mmnt;
-  return XC_OK;
 }
 
 int sums_impl(xc_ctx* c, double out[12]) {

@@ -251,6 +251,45 @@ function step_converge!(ctx::Context, step::Integer, dt, re, rs, par; solver::Sy
     return (s.dt_next, Int(s.sweeps))
 end
 
+# ---- ensembles: independent contexts stepped together (xc_ensemble_*) ---------------
+# every explicit stage of a Picard sweep one CUDA graph launch for all members,
+# the Stokes solves on `threads` library threads (0: one per member); each
+# member ends bit-identical to step! on it alone
+mutable struct Ensemble
+    h::Ptr{Cvoid}
+    members::Vector{Context}
+end
+
+function Ensemble(members::Vector{Context}; threads::Integer = 0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    hs = Ptr{Cvoid}[m.h for m in members]
+    check(ccall((:xc_ensemble_create, LIB), Cint, (Ptr{Ptr{Cvoid}}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                hs, length(hs), threads, h))
+    e = Ensemble(h[], members)
+    finalizer(x -> ccall((:xc_ensemble_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), e)
+    return e
+end
+
+# one time step of every member with `sweeps` Picard sweeps (steps[i], dts[i],
+# draws re[i], rs[i]); returns the members' next dt
+function step!(e::Ensemble, steps::AbstractVector{<:Integer}, dts::AbstractVector{<:Real}, re, rs;
+               sweeps = 3, solver::Symbol = :mixed, rtol = 1e-9)
+    n = length(e.members)
+    st = Vector{StepStats}(undef, n)
+    hre = [Matrix{Float64}(r) for r in re]
+    hrs = [Matrix{Float64}(r) for r in rs]
+    status = GC.@preserve hre hrs begin
+        ccall((:xc_ensemble_step, LIB), Cint,
+              (Ptr{Cvoid}, Ptr{Cint}, Ptr{Cdouble}, Cint, Ptr{Ptr{Cdouble}}, Ptr{Ptr{Cdouble}}, Ref{SolverOpts},
+               Ptr{StepStats}),
+              e.h, Cint.(steps), Cdouble.(dts), sweeps, [pointer(r) for r in hre], [pointer(r) for r in hrs],
+              step_solver_opts(solver, rtol), st)
+    end
+    status == 2 && error("xcore_gb300: " * unsafe_string(ccall((:xc_last_error, LIB), Cstring, ())))
+    check(status)
+    return [s.dt_next for s in st]
+end
+
 # ---- call-site drop-in on CuArray-backed states -------------------------------------
 # With CUDA.jl loaded and the reference's FluidState / PhaseState built on
 # CuArrays (xcore_zeros with a CUDA backend, src/backend.jl:12-13), the methods
