@@ -228,16 +228,14 @@ int run_line_filter(const LineFilter& lf, CView in, DView out, int rows, int col
   int P = 1;
   while (P * 2 * lf.M * (int)sizeof(double2) <= 64 * 1024 && P * 2 <= 8) P *= 2;
   size_t smem = (size_t)P * lf.M * sizeof(double2);
-  {
-    // the kernel's dynamic shared-memory limit only ever rises: a graph may
-    // hold launches of several filter lengths, captured in any order
+  if (smem > 48 * 1024) {
+    // set to the largest need seen so far, never lowered: a graph may hold
+    // launches of several filter lengths, captured in any order
     static std::mutex mu;
-    static size_t limit = 48 * 1024;
+    static size_t limit = 0;
     std::lock_guard<std::mutex> lock(mu);
-    if (smem > limit) {
-      XC_CUDA_TRY(cudaFuncSetAttribute(line_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      limit = smem;
-    }
+    if (smem > limit) limit = smem;
+    XC_CUDA_TRY(cudaFuncSetAttribute(line_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
   }
   int threads = lf.M * P >= 1024 ? 512 : 256;
   xc_launch(line_filter_kernel, (npairs + P - 1) / P, threads, smem, s, in, out, rows, cols, axis, lf.M,
