@@ -68,3 +68,15 @@ def test_bad_parameters_rejected_before_any_device_work():
     with pytest.raises(xc.XcoreError) as e:
         xc.State(xc.Parameters(N=2))
     assert e.value.status == xc.XC_BAD_ARG
+
+
+def test_ensemble_arguments_rejected_before_any_device_work(lib):
+    out = ctypes.c_void_p()
+    assert lib.xc_ensemble_create(None, 0, 0, ctypes.byref(out)) == xc.XC_BAD_ARG
+    members = (ctypes.c_void_p * 2)(None, None)
+    assert lib.xc_ensemble_create(members, 2, 0, ctypes.byref(out)) == xc.XC_BAD_ARG
+    assert b"null" in lib.xc_last_error()
+    assert lib.xc_ensemble_create(members, 2, -1, ctypes.byref(out)) == xc.XC_BAD_ARG
+    steps, dts = (ctypes.c_int * 1)(1), (ctypes.c_double * 1)(1e-3)
+    assert lib.xc_ensemble_step(None, steps, dts, 3, None, None, None, None) == xc.XC_BAD_ARG
+    assert lib.xc_ensemble_destroy(None) == xc.XC_OK
