@@ -706,6 +706,7 @@ class Ensemble:
         return infos
 
     def close(self):
+        """Release the ensemble and close its members."""
         if self._h is not None:
             lib().xc_ensemble_destroy(self._h)
             self._h = None
@@ -713,6 +714,16 @@ class Ensemble:
             self._pool.shutdown()
         for m in self.members:
             m.close()
+
+    def __del__(self):
+        # the library's ensemble (streams, events, host threads); the members
+        # close themselves
+        try:
+            if self._h is not None:
+                lib().xc_ensemble_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------
