@@ -215,9 +215,10 @@ function print_step_stats(ctx::Context)
 end
 
 # the measured optimum of the 1024^2 time step: FP32 inner solves to a 5e-2
-# reduction in at most 30 iterations, one pressure-multigrid sweep
+# reduction in at most 30 iterations, one pressure-multigrid sweep; at most 400
+# FP32 iterations per mixed solve, 3000 per plain FP64 solve
 step_solver_opts(solver::Symbol, rtol; learned = 0) =
-    SolverOpts(solver === :mixed ? 1 : 0, rtol, 400, 30, 5e-2, 30,
+    SolverOpts(solver === :mixed ? 1 : 0, rtol, solver === :mixed ? 400 : 3000, 30, 5e-2, 30,
                0, 0.0, 0.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, learned, 0, 0)
 
 # status 2 (XC_NOT_CONVERGED) from a step means the step was completed but a
@@ -316,6 +317,11 @@ const Noise64 = xcore.NoiseState{Float64}
 const Res = xcore.StepResidual
 const BOUND = IdDict{Any,Context}()
 const BOUND_BC = IdDict{Any,NTuple{4,Int}}()   # (sds, top_cnv, bot_cnv, open_cnv) of each bound context
+# the Stokes solver of the fluidmech! method below: the plain FP64 drop-in to
+# relative residual 1e-10 (within 1e-8 of the reference's LU solution) by
+# default; `XcoreGPU.CALLSITE_SOLVER[] = (:mixed, 1e-9)` selects the mixed
+# FP32/FP64 solver (about 2.8x faster per step at 1024^2)
+const CALLSITE_SOLVER = Ref{Tuple{Symbol,Float64}}((:fgmres64, 1e-10))
 
 function bind!(ctx::Context, name::Symbol, a::CuArray)
     id = fieldid(name)
@@ -368,7 +374,7 @@ function xcore.fluidmech!(fluid::GPUFluid, grid::Grid64, par::Par64; phase::GPUP
         error("XcoreGPU.fluidmech!: boundary keywords differ from the bound context's $(BOUND_BC[phase])")
     s = Ref{SolverStats}()
     check(ccall((:xc_fluidmech, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cdouble, Ref{SolverOpts}, Ref{SolverStats}),
-                ctx.h, coefs(a1, a2, a3, b1, b2, b3), dt, step_solver_opts(:mixed, 1e-9), s))
+                ctx.h, coefs(a1, a2, a3, b1, b2, b3), dt, step_solver_opts(CALLSITE_SOLVER[]...), s))
     return nothing
 end
 
