@@ -17,79 +17,16 @@
 // graphs hold the step's dt and time coefficients and are re-captured each step
 // (and updated in place when their topology is unchanged); post and dt are
 // captured once.
-#include <atomic>
 #include <cmath>
-#include <condition_variable>
 #include <cstring>
 #include <functional>
-#include <mutex>
-#include <thread>
+#include <string>
 #include <vector>
 
 #include "xc_internal.cuh"
+#include "xc_pool.h"
 
 namespace {
-
-// A fixed set of host threads running job(i) for i in [0, n), each thread
-// taking the next index until none is left; run() returns when all are done.
-class WorkerPool {
- public:
-  WorkerPool(int nthreads, int device) : device_(device) {
-    for (int t = 0; t < nthreads; ++t) th_.emplace_back([this] { loop(); });
-  }
-  ~WorkerPool() {
-    {
-      std::lock_guard<std::mutex> l(mu_);
-      quit_ = true;
-    }
-    go_.notify_all();
-    for (auto& t : th_) t.join();
-  }
-  void run(int n, const std::function<void(int)>& job) {
-    {
-      std::lock_guard<std::mutex> l(mu_);
-      job_ = &job;
-      n_ = n;
-      next_.store(0);
-      busy_ = (int)th_.size();
-      ++gen_;
-    }
-    go_.notify_all();
-    std::unique_lock<std::mutex> l(mu_);
-    done_.wait(l, [this] { return busy_ == 0; });
-  }
-
- private:
-  void loop() {
-    cudaSetDevice(device_);
-    int seen = 0;
-    for (;;) {
-      const std::function<void(int)>* job;
-      int n;
-      {
-        std::unique_lock<std::mutex> l(mu_);
-        go_.wait(l, [&] { return quit_ || gen_ != seen; });
-        if (quit_) return;
-        seen = gen_;
-        job = job_;
-        n = n_;
-      }
-      for (int i; (i = next_.fetch_add(1)) < n;) (*job)(i);
-      {
-        std::lock_guard<std::mutex> l(mu_);
-        if (--busy_ == 0) done_.notify_all();
-      }
-    }
-  }
-  std::vector<std::thread> th_;
-  std::mutex mu_;
-  std::condition_variable go_, done_;
-  const std::function<void(int)>* job_ = nullptr;
-  int n_ = 0, gen_ = 0, busy_ = 0;
-  std::atomic<int> next_{0};
-  bool quit_ = false;
-  int device_;
-};
 
 struct Stage {
   cudaGraphExec_t exec = nullptr;
@@ -105,7 +42,7 @@ struct xc_ensemble {
   cudaEvent_t ev_fork = nullptr, ev_pre = nullptr, ev_noise = nullptr;
   std::vector<cudaEvent_t> ev_m;              // per member: joins its branch back
   Stage pre_first, pre_rest, noise, post, dt;
-  WorkerPool* pool = nullptr;
+  xc::WorkerPool* pool = nullptr;
 };
 
 namespace {
@@ -248,7 +185,7 @@ extern "C" int xc_ensemble_create(xc_ctx* const* members, int n, int threads, xc
       xc_set_error("xc_ensemble_create: event creation failed");
       return fail(XC_CUDA);
     }
-  e->pool = new WorkerPool(threads > 0 ? (threads < n ? threads : n) : n, e->device);
+  e->pool = new xc::WorkerPool(threads > 0 ? (threads < n ? threads : n) : n, e->device);
   *out = e;
   return XC_OK;
 }
