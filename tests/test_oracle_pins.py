@@ -492,3 +492,25 @@ def test_snapshot_copies_primary_fields():
     assert snap["W"][1, 1] == 42.0 and snap["U"][2, 1] == -7.0 and snap["X"][0, 0] == 0.3
     st.W[1, 1] = 0.0
     assert snap["W"][1, 1] == 42.0
+
+
+# src/parameters.jl:14-86, the defaults of Parameters{Float64}() the path reads
+REFERENCE_DEFAULTS = dict(
+    D=10.0, N=100, L=10.0, x0=float(np.finfo(np.float64).eps), dxr=0.1, dxg=0.0, rhom0=2700.0, rhox0=3200.0,
+    d0=0.01, g0=10.0, etam0=10.0, etax0=1e18, AA=((0.72, 0.19), (0.81, 0.20)), BB=((0.63, 0.37), (0.999, 0.001)),
+    CC=((2.09, 0.09), (0.37, 1.45)), L0=0.1, l0=0.1, Da=0.01, Xi=0.5, Ptop=1e5, open_sgr=False, TINT="bd2im",
+    ADVN="weno5", CFL=0.5, rtol=1e-4, atol=1e-9, maxit=15, alpha=0.9, gamma=1e-3, dtmax=1e32, etacntr=1e8)
+
+
+def test_parameter_defaults_match_the_reference():
+    """test/test_parameters.jl:1-6 (D = 10, N = 100, ADVN = :weno5) and every
+    other default the path reads, for the oracle's Params and the library's
+    Python Parameters alike."""
+    import xcore_gb300 as xc
+    for cls in (O.Params, xc.Parameters):
+        p = cls()
+        for k, v in REFERENCE_DEFAULTS.items():
+            if hasattr(p, k):
+                assert getattr(p, k) == v, (cls.__name__, k)
+    p = O.Params()
+    assert all(hasattr(p, k) for k in REFERENCE_DEFAULTS), "the oracle carries every default"
