@@ -80,3 +80,39 @@ def test_ensemble_arguments_rejected_before_any_device_work(lib):
     steps, dts = (ctypes.c_int * 1)(1), (ctypes.c_double * 1)(1e-3)
     assert lib.xc_ensemble_step(None, steps, dts, 3, None, None, None, None) == xc.XC_BAD_ARG
     assert lib.xc_ensemble_destroy(None) == xc.XC_OK
+
+
+def _registry_shapes(Nz, Nx):
+    """The library's field registry (the XC_FIELDS table of its internal
+    header) as {name: (rows, cols)} for an Nz x Nx grid."""
+    src = open(os.path.join(ROOT, "xcore.jl_gb300", "csrc", "xc_internal.cuh")).read()
+    body = src[src.index("#define XC_FIELDS(F)"):src.index("enum FieldId")]
+    dims = {"SH_C": (0, 0), "SH_ZF": (1, 0), "SH_XF": (0, 1), "SH_W": (1, 2), "SH_U": (2, 1), "SH_CO": (1, 1),
+            "SH_P": (2, 2)}
+    out = {}
+    for name, code, _eb in re.findall(r"F\((\w+), (SH_\w+), (\d)\)", body):
+        dz, dx = dims[code]
+        out[name] = (Nz + dz, Nx + dx)
+    return out
+
+
+def test_registry_sizes_are_the_reference_sizes():
+    """Every field the library allocates has the reference's size: the
+    oracle's table of FluidState / PhaseState / NoiseState (state.jl:101-122,
+    218-258; noise.jl:82-92), the StepResidual buffers of
+    test/test_diagnose.jl:18-33 and the NoiseState sizes of
+    test/test_noise.jl:21-43."""
+    Nz, Nx = 10, 7
+    reg = _registry_shapes(Nz, Nx)
+    assert len(reg) == len(xc.field_names())
+    ref = O.field_shapes(Nz, Nx)
+    for name, shp in ref.items():
+        assert reg[name] == shp, name
+    residual = {"res_Wo": (Nz + 1, Nx + 2), "res_Uo": (Nz + 2, Nx + 1), "res_Po": (Nz + 2, Nx + 2),
+                "res_Xo": (Nz, Nx), "res_MFSo": (Nz, Nx)}
+    noise = {"psie": (Nz, Nx), "psieo": (Nz, Nx), "re": (Nz, Nx), "rs": (Nz, Nx), "xiew": (Nz + 1, Nx + 2),
+             "xieu": (Nz + 2, Nx + 1), "xixw": (Nz + 1, Nx + 2), "xixu": (Nz + 2, Nx + 1),
+             "xisw": (Nz + 1, Nx + 2), "xisu": (Nz + 2, Nx + 1), "xie": (Nz, Nx), "xix": (Nz, Nx),
+             "xis": (Nz, Nx)}
+    for name, shp in {**residual, **noise}.items():
+        assert reg[name] == shp, name
