@@ -404,6 +404,43 @@ function xcore.compute_resnorm(res::Res, phase::GPUPhase, fluid::GPUFluid, dt::R
     end
     return r
 end
+# record_history! (src/history.jl:101-222): the mass sums, boundary-flux
+# integrals and the 58 field statistics come from the device
+# (xc_conservation_sums, xc_history_stats, whose keys are the History field
+# names); the rate shift, the BD2-integrated drift and the conservation
+# errors are the reference's host arithmetic on them
+function xcore.record_history!(hst::xcore.History{Float64}, time::Real, dt::Real, phase::GPUPhase,
+                               fluid::GPUFluid, ns::Noise64, grid::Grid64, a1::Real = 1.0, a2::Real = 1.0,
+                               a3::Real = 0.0, b1::Real = 1.0, b2::Real = 0.0, b3::Real = 0.0)
+    ctx = bound_context(phase)
+    hst.dsumBdtoo = hst.dsumBdto;  hst.dsumBdto = hst.dsumBdt
+    hst.dsumMdtoo = hst.dsumMdto;  hst.dsumMdto = hst.dsumMdt
+    hst.dsumXdtoo = hst.dsumXdto;  hst.dsumXdto = hst.dsumXdt
+    push!(hst.time, Float64(time))
+    push!(hst.dt, Float64(dt))
+    sumB, sumM, sumX, sumGx, top_aX, bot_aX, top_aM, bot_aM, top_dX, bot_dX, top_dM, bot_dM = conservation_sums(ctx)
+    push!(hst.sumB, sumB); push!(hst.sumM, sumM); push!(hst.sumX, sumX)
+    hst.dsumBdt = (top_aX - bot_aX) + (top_aM - bot_aM) + (top_dX - bot_dX) + (top_dM - bot_dM)
+    hst.dsumMdt = -sumGx + (top_aM - bot_aM) + (top_dM - bot_dM)
+    hst.dsumXdt = +sumGx + (top_aX - bot_aX) + (top_dX - bot_dX)
+    stp = length(hst.time)
+    T = Float64
+    drift(D, rate, rate_o, rate_oo) = stp >= 2 ?
+        (T(a2) * D[stp - 1] + T(a3) * D[max(1, stp - 2)] + (T(b1) * rate + T(b2) * rate_o + T(b3) * rate_oo) * T(dt)) /
+        T(a1) : zero(T)
+    push!(hst.DB, drift(hst.DB, hst.dsumBdt, hst.dsumBdto, hst.dsumBdtoo))
+    push!(hst.DM, drift(hst.DM, hst.dsumMdt, hst.dsumMdto, hst.dsumMdtoo))
+    push!(hst.DX, drift(hst.DX, hst.dsumXdt, hst.dsumXdto, hst.dsumXdtoo))
+    sumB0 = hst.sumB[1]
+    push!(hst.EB, (sumB - hst.DB[stp] - sumB0) / sumB0)
+    push!(hst.EM, (sumM - hst.DM[stp] - hst.sumM[1]) / sumB0)
+    push!(hst.EX, (sumX - hst.DX[stp] - hst.sumX[1]) / sumB0)
+    for (k, v) in history_stats(ctx)
+        push!(getfield(hst, Symbol(k)), v)
+    end
+    return nothing
+end
+
 xcore.update_dt(phase::GPUPhase, fluid::GPUFluid, grid::Grid64, par::Par64, dt_prev::Real) =
     update_dt(bound_context(phase), dt_prev)
 
