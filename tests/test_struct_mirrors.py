@@ -147,7 +147,8 @@ def test_julia_gpu_methods_type_every_positional_argument():
     ambiguous; each must be strictly more specific."""
     methods = _julia_extension_methods()
     assert {n for n, _ in methods} >= {"store_previous!", "snapshot!", "phsevo!", "fluidmech!", "noise!",
-                                       "update_phase_velocities!", "update!", "compute_resnorm", "update_dt"}
+                                       "update_phase_velocities!", "update!", "compute_resnorm", "update_dt",
+                                       "record_history!"}
     for name, args in methods:
         assert args, name
         for a in args:
